@@ -1,0 +1,271 @@
+"""Scene description and a driver that bakes it through any ``ltr_*`` library.
+
+`bake(lib, desc)` replays a `SceneDesc` through the public C API exactly as an
+application would (lighter_test.cpp:183-544 is the reference's own caller):
+create scene, set config, add meshes/parts/instances, seed ``rand()`` and add
+lights, add probe samples, ``ltr_Start``, poll ``ltr_GetStatus``, then read the
+work outputs. The same driver runs the GPU library, the CPU oracle port and the
+reference build, which is what makes their outputs comparable.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from dataclasses import dataclass, field
+from typing import Callable, Optional
+
+import numpy as np
+
+from . import abi
+
+_libc = C.CDLL(None)
+_libc.srand.argtypes = [C.c_uint]
+_libc.srand.restype = None
+
+
+def srand(seed: int) -> None:
+    """Seed glibc's process-wide rand(); the bake draws one value per light at
+    ltr_LightAdd and one per AO texel (lighter.cpp:1300, 819)."""
+    _libc.srand(int(seed) & 0xFFFFFFFF)
+
+
+@dataclass
+class Part:
+    positions: np.ndarray          # (V,3) f32
+    normals: np.ndarray            # (V,3) f32
+    uv1: np.ndarray                # (V,2) f32, passed to sample_fn (face id in u)
+    uv2: np.ndarray                # (V,2) f32, lightmap UVs
+    indices: np.ndarray            # (I,) u32
+    shadow: int = 1
+
+
+@dataclass
+class Mesh:
+    ident: str
+    parts: list
+
+
+@dataclass
+class Instance:
+    mesh: int
+    matrix: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32))
+    importance: float = 1.0
+    shadow: int = 1
+    ident: str = ""
+
+
+@dataclass
+class Light:
+    type: int
+    position: tuple = (0.0, 0.0, 0.0)
+    direction: tuple = (0.0, 0.0, 0.0)
+    up: tuple = (0.0, 0.0, 0.0)
+    color: tuple = (1.0, 1.0, 1.0)
+    range: float = 10.0
+    power: float = 1.0
+    light_radius: float = 0.1
+    shadow_sample_count: int = 1
+    spot_angle_out: float = 0.0
+    spot_angle_in: float = 0.0
+    spot_curve: float = 0.0
+
+
+@dataclass
+class SceneDesc:
+    name: str
+    meshes: list
+    instances: list
+    lights: list
+    config: dict = field(default_factory=dict)
+    fixed_lm_size: Optional[tuple] = None          # size_fn forcing (w, h)
+    sample_table: Optional[tuple] = None           # (diffuse (F,3), emissive (F,3) or None)
+    sample_fn_py: Optional[Callable] = None        # python sample_fn(req) -> bool
+    probes: list = field(default_factory=list)     # [(id, pos3, nrm3)]
+    seed: int = 1
+
+    def triangle_count(self) -> int:
+        n = 0
+        for inst in self.instances:
+            n += sum(len(p.indices) // 3 for p in self.meshes[inst.mesh].parts)
+        return n
+
+
+@dataclass
+class BakeResult:
+    lightmaps: list                 # [(uid, mesh_ident, inst_ident, rgb (h,w,3), normals (h,w,4)|None)]
+    sample_colors: np.ndarray       # (S,3) probe outputs
+    stages: list
+    wall_s: float
+    debug: list = field(default_factory=list)   # per instance dict of sample arrays
+    final_stage: str = ""
+
+
+def _vec3(v):
+    return abi.VEC3(*[float(x) for x in v])
+
+
+def bake(lib, desc: SceneDesc, threads: int = 1, debug: bool = True, poll_s: float = 0.001,
+         timeout_s: float = 3600.0, before_start: Optional[Callable] = None) -> BakeResult:
+    keep = []
+    scene = lib.ltr_CreateScene()
+    if not scene:
+        raise RuntimeError("ltr_CreateScene returned NULL")
+    try:
+        cfg = abi.Config()
+        lib.ltr_GetConfig(C.byref(cfg), scene)
+        for k, v in desc.config.items():
+            if isinstance(v, (tuple, list)):
+                setattr(cfg, k, _vec3(v))
+            else:
+                setattr(cfg, k, v)
+        cfg.max_num_threads = threads
+        if desc.fixed_lm_size is not None:
+            w, h = desc.fixed_lm_size
+
+            def _size(cfgp, mi, mis, ii, iis, area, imp, out):
+                out[0] = w
+                out[1] = h
+                return 1
+            cb = abi.SIZE_FN(_size)
+            keep.append(cb)
+            cfg.size_fn = C.cast(cb, C.c_void_p).value
+        if desc.sample_table is not None:
+            dif, emi = desc.sample_table
+            dif = np.ascontiguousarray(dif, dtype=np.float32)
+            keep.append(dif)
+            tab = abi.SampleTable()
+            tab.count = dif.shape[0]
+            tab.diffuse_rgb = dif.ctypes.data_as(C.POINTER(C.c_float))
+            if emi is not None:
+                emi = np.ascontiguousarray(emi, dtype=np.float32)
+                keep.append(emi)
+                tab.emissive_rgb = emi.ctypes.data_as(C.POINTER(C.c_float))
+            keep.append(tab)
+            cfg.userdata = C.cast(C.pointer(tab), C.c_void_p).value
+            cfg.sample_fn = C.cast(lib.ltrg_TableSampleFn, C.c_void_p).value
+        elif desc.sample_fn_py is not None:
+            fn = desc.sample_fn_py
+
+            def _sample(cfgp, reqp):
+                return 1 if fn(reqp.contents) else 0
+            cb = abi.SAMPLE_FN(_sample)
+            keep.append(cb)
+            cfg.sample_fn = C.cast(cb, C.c_void_p).value
+        lib.ltr_SetConfig(scene, C.byref(cfg))
+
+        mesh_handles = []
+        for m in desc.meshes:
+            ident = m.ident.encode()
+            mh = lib.ltr_CreateMesh(scene, ident, len(ident))
+            mesh_handles.append(mh)
+            for p in m.parts:
+                pos = np.ascontiguousarray(p.positions, dtype=np.float32)
+                nrm = np.ascontiguousarray(p.normals, dtype=np.float32)
+                t1 = np.ascontiguousarray(p.uv1, dtype=np.float32)
+                t2 = np.ascontiguousarray(p.uv2, dtype=np.float32)
+                idx = np.ascontiguousarray(p.indices, dtype=np.uint32)
+                info = abi.MeshPartInfo()
+                info.positions_f3 = pos.ctypes.data
+                info.normals_f3 = nrm.ctypes.data
+                info.texcoords1_f2 = t1.ctypes.data
+                info.texcoords2_f2 = t2.ctypes.data
+                info.stride_positions = 12
+                info.stride_normals = 12
+                info.stride_texcoords1 = 8
+                info.stride_texcoords2 = 8
+                info.indices = idx.ctypes.data_as(C.POINTER(abi.u32))
+                info.vertex_count = pos.shape[0]
+                info.index_count = idx.shape[0]
+                info.shadow = int(p.shadow)
+                if not lib.ltr_MeshAddPart(mh, C.byref(info)):
+                    raise RuntimeError(f"ltr_MeshAddPart rejected a part of {m.ident}")
+        for inst in desc.instances:
+            ii = abi.MeshInstanceInfo()
+            mat = np.asarray(inst.matrix, dtype=np.float32).reshape(4, 4)
+            for r in range(4):
+                for c in range(4):
+                    ii.matrix[r][c] = float(mat[r, c])
+            ii.importance = inst.importance
+            ii.shadow = inst.shadow
+            ident = inst.ident.encode()
+            keep.append(ident)
+            ii.ident = ident
+            ii.ident_size = len(ident)
+            lib.ltr_MeshAddInstance(mesh_handles[inst.mesh], C.byref(ii))
+
+        srand(desc.seed)
+        for L in desc.lights:
+            li = abi.LightInfo()
+            li.type = L.type
+            li.position = _vec3(L.position)
+            li.direction = _vec3(L.direction)
+            li.up_direction = _vec3(L.up)
+            li.color_rgb = _vec3(L.color)
+            li.range = L.range
+            li.power = L.power
+            li.light_radius = L.light_radius
+            li.shadow_sample_count = L.shadow_sample_count
+            li.spot_angle_out = L.spot_angle_out
+            li.spot_angle_in = L.spot_angle_in
+            li.spot_curve = L.spot_curve
+            lib.ltr_LightAdd(scene, C.byref(li))
+        for (sid, pos, nrm) in desc.probes:
+            si = abi.SampleInfo()
+            si.id = sid
+            si.position = _vec3(pos)
+            si.normal = _vec3(nrm)
+            lib.ltr_SampleAdd(scene, C.byref(si))
+
+        if before_start is not None:
+            before_start(scene)
+        stages = []
+        st = abi.WorkStatus()
+        t0 = time.perf_counter()
+        lib.ltr_Start(scene)
+        while lib.ltr_GetStatus(scene, C.byref(st)):
+            s = st.stage.decode() if st.stage else ""
+            if not stages or stages[-1] != s:
+                stages.append(s)
+            if time.perf_counter() - t0 > timeout_s:
+                lib.ltr_Abort(scene)
+            time.sleep(poll_s)
+        wall = time.perf_counter() - t0
+        final = st.stage.decode() if st.stage else ""
+
+        info = abi.WorkOutputInfo()
+        lib.ltr_GetWorkOutputInfo(scene, C.byref(info))
+        lms = []
+        for k in range(info.lightmap_count):
+            wo = abi.WorkOutput()
+            if not lib.ltr_GetWorkOutput(scene, k, C.byref(wo)):
+                raise RuntimeError("ltr_GetWorkOutput failed")
+            n = wo.width * wo.height
+            rgb = np.ctypeslib.as_array(wo.lightmap_rgb, shape=(n * 3,)).copy().reshape(wo.height, wo.width, 3)
+            nrm = None
+            if wo.normals_xyzf:
+                nrm = np.ctypeslib.as_array(wo.normals_xyzf, shape=(n * 4,)).copy().reshape(wo.height, wo.width, 4)
+            mid = C.string_at(wo.mesh_ident, wo.mesh_ident_size).decode() if wo.mesh_ident else ""
+            iid = C.string_at(wo.inst_ident, wo.inst_ident_size).decode() if wo.inst_ident else ""
+            lms.append((wo.uid, mid, iid, rgb, nrm))
+        colors = np.zeros((info.sample_count, 3), np.float32)
+        for k in range(info.sample_count):
+            colors[k] = info.samples[k].out_color[:]
+
+        dbg = []
+        if debug and hasattr(lib, "ltrdbg_InstanceCount"):
+            for i in range(lib.ltrdbg_InstanceCount(scene)):
+                n = lib.ltrdbg_SampleCount(scene, i)
+                d = {
+                    "pos": np.zeros((n, 3), np.float32),
+                    "nrm": np.zeros((n, 3), np.float32),
+                    "loc": np.zeros((n,), np.uint32),
+                    "radinfo": np.zeros((n, 4), np.float32),
+                    "color": np.zeros((n, 3), np.float32),
+                }
+                if n:
+                    lib.ltrdbg_GetSamples(scene, i, d["pos"].ctypes.data, d["nrm"].ctypes.data,
+                                          d["loc"].ctypes.data, d["radinfo"].ctypes.data, d["color"].ctypes.data)
+                dbg.append(d)
+        return BakeResult(lms, colors, stages, wall, dbg, final)
+    finally:
+        lib.ltr_DestroyScene(scene)
