@@ -1,0 +1,94 @@
+/*
+ * lighter_gb300.h -- GPU extensions of the lighter C ABI (liblighter_gb300.so).
+ *
+ * Everything here is additive: an application that only uses lighter.h gets
+ * the reference behaviour. The extensions select the CUDA device, opt into
+ * the physically-based radiosity link predicate and the mixed-precision
+ * gather, expose per-stage timings and counters, batch many scenes into one
+ * bake, and provide read-only introspection used by the parity tests.
+ */
+#pragma once
+
+#include "lighter.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Radiosity link predicate. The reference keeps a pair only when
+ * ltr_Scene::VisibilityTest reports an occluder between the two samples
+ * (lighter.cpp:751, `VisibilityTest(...) == false` skips unoccluded pairs). */
+#define LTRG_LINKS_REFERENCE 0   /* link occluded pairs, as lighter.cpp:751 */
+#define LTRG_LINKS_VISIBLE   1   /* link mutually visible pairs */
+
+/* Storage type of the dense form-factor matrix F used by the gather. */
+#define LTRG_F_FP32 0
+#define LTRG_F_FP16 1
+#define LTRG_F_BF16 2
+
+typedef struct ltrg_Options {
+    int device;               /* CUDA device ordinal, default 0 */
+    int keep_samples;         /* keep per-sample arrays for ltrdbg_* after the bake, default 0 */
+    int radiosity_links;      /* LTRG_LINKS_*, default LTRG_LINKS_REFERENCE */
+    int radiosity_precision;  /* LTRG_F_*, default LTRG_F_FP32 */
+    int refine_steps;         /* FP32 residual-refinement sweeps for FP16/BF16 F, default 1 */
+    uint32_t reserved[11];
+} ltrg_Options;
+
+/* Per-stage device times (CUDA events on the bake stream) and work counters
+ * of the last finished bake. */
+typedef struct ltrg_Stats {
+    double ms_total;          /* host wall time from ltr_Start to finished */
+    double ms_upload;         /* host->device copies of the scene */
+    double ms_bvh;            /* BVH build */
+    double ms_samples;        /* raster, compaction, offset and correction */
+    double ms_direct;         /* direct light */
+    double ms_rad_links;      /* form factors and their visibility rays */
+    double ms_rad_bounce;     /* all bounces */
+    double ms_ao;             /* ambient occlusion */
+    double ms_finalize;       /* scatter, dilate, blur, ds2x, normal data */
+    double ms_download;       /* device->host copies of the outputs */
+    uint64_t texels;          /* lightmap texels rasterised */
+    uint64_t samples;         /* covered texels + probe samples */
+    uint64_t triangles;       /* shadow-casting triangles in the BVH */
+    uint64_t shadow_evals;    /* (sample, light) shadow evaluations traced */
+    uint64_t distance_queries;/* sphere-trace steps (nearest-triangle queries) */
+    uint64_t ao_rays;         /* AO segment queries */
+    uint64_t rad_pairs;       /* radiosity pairs i<j examined */
+    uint64_t rad_vis_rays;    /* pairs that passed the facing/form-factor tests */
+    uint64_t node_visits;     /* BVH internal nodes visited by the direct-light queries */
+    uint64_t reserved[7];
+} ltrg_Stats;
+
+/* Options are read at ltr_Start; returns 0 on an invalid value. */
+LTRAPI void ltrg_GetOptions(ltr_Scene* scene, ltrg_Options* out);
+LTRAPI LTRBOOL ltrg_SetOptions(ltr_Scene* scene, const ltrg_Options* opt);
+LTRAPI LTRBOOL ltrg_GetStats(ltr_Scene* scene, ltrg_Stats* out);
+/* Text of the error that ended the last bake, or NULL. */
+LTRAPI const char* ltrg_LastError(ltr_Scene* scene);
+/* Blocks until the bake started by ltr_Start has finished; returns 1 on success. */
+LTRAPI LTRBOOL ltrg_Wait(ltr_Scene* scene);
+
+/* Table-driven sample_fn: config->userdata points at an ltrg_SampleTable and
+ * the entry is chosen by (u32) request->tex0u, i.e. the mesh's first UV channel
+ * carries a face id. Entries out of range keep the defaults (returns 0). */
+typedef struct ltrg_SampleTable {
+    u32 count;
+    const float* diffuse_rgb;    /* count x 3, may be NULL */
+    const float* emissive_rgb;   /* count x 3, may be NULL */
+} ltrg_SampleTable;
+LTRAPI LTRBOOL ltrg_TableSampleFn(ltr_Config* config, ltr_SampleRequest* req);
+
+/* Read-only introspection of a finished bake (requires keep_samples = 1).
+ * Instance 0 is the probe-sample container of ltr_SampleAdd, as in the
+ * reference (lighter_int.hpp:975-980). */
+LTRAPI u32 ltrdbg_InstanceCount(ltr_Scene* scene);
+LTRAPI u32 ltrdbg_SampleCount(ltr_Scene* scene, u32 inst);
+LTRAPI LTRBOOL ltrdbg_LightmapSize(ltr_Scene* scene, u32 inst, u32* wh);
+LTRAPI LTRBOOL ltrdbg_GetSamples(ltr_Scene* scene, u32 inst, float* pos3, float* nrm3, u32* loc, float* radinfo4,
+                                 float* color3);
+LTRAPI u32 ltrdbg_RadLinkCount(ltr_Scene* scene);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,323 @@
+// The ltr_* C API of lighter.h (lighter.cpp:7-28, 101-109, 1147-1357) over
+// the GPU bake. Ingest, configuration and output ownership keep the
+// reference's contract: parts are copied at ltr_MeshAddPart time, outputs are
+// owned by the scene until ltr_DestroyScene, ltr_Start returns at once and
+// ltr_GetStatus polls a bake running on a host thread of its own.
+#include <chrono>
+#include <cstring>
+#include <stdexcept>
+
+#include "scene.hpp"
+
+using namespace lg;
+
+ltr_Scene::ltr_Scene()
+{
+    ltr_GetConfig(&cfg, nullptr);
+    memset(&opt, 0, sizeof(opt));
+    opt.refine_steps = 1;
+    memset(&stats, 0, sizeof(stats));
+    HostInst* c = new HostInst;   // probe-sample container, lighter_int.hpp:975-980
+    c->container = true;
+    c->w = c->h = 0;
+    insts.push_back(c);
+}
+
+void ltr_Scene::clear_outputs()
+{
+    for (auto& o : outputs) {
+        delete[] o.lightmap_rgb;
+        delete[] o.normals_xyzf;
+    }
+    outputs.clear();
+    dump.clear();
+}
+
+ltr_Scene::~ltr_Scene()
+{
+    if (worker.joinable()) worker.join();
+    clear_outputs();
+    for (HostInst* mi : insts) delete mi;
+    for (ltr_Mesh* m : meshes) delete m;
+}
+
+static u32 next_pow2(u32 x)
+{
+    x--;
+    x |= x >> 1; x |= x >> 2; x |= x >> 4; x |= x >> 8; x |= x >> 16;
+    return x + 1;
+}
+
+extern "C" {
+
+LTRAPI u32 ltr_NextPowerOfTwo(u32 x) { return next_pow2(x); }
+
+// size = global_size_factor * sqrt(area) * importance, at least 1, rounded up
+// to a power of two; rejected above max_lightmap_size (lighter.cpp:7-28).
+LTRAPI LTRBOOL ltr_DefaultSizeFunc(ltr_Config* config, const char*, size_t, const char*, size_t,
+                                   float computed_surface_area, float inst_importance, u32 out_size[2])
+{
+    float size = config->global_size_factor * sqrtf(computed_surface_area) * inst_importance;
+    if (size < 1) size = 1;
+    u32 s = next_pow2((u32) size);
+    if (s > config->max_lightmap_size) return 0;
+    out_size[0] = s;
+    out_size[1] = s;
+    return 1;
+}
+
+// Defaults of lighter.cpp:1171-1208.
+LTRAPI void ltr_GetConfig(ltr_Config* cfg, ltr_Scene* opt_scene)
+{
+    if (opt_scene) { memcpy(cfg, &opt_scene->cfg, sizeof(*cfg)); return; }
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->size_fn = ltr_DefaultSizeFunc;
+    cfg->max_num_threads = 0x7fff;
+    cfg->max_tree_memory = 128 * 1024 * 1024;
+    cfg->max_lightmap_size = 1024;
+    cfg->default_width = 64;
+    cfg->default_height = 64;
+    cfg->global_size_factor = 4;
+    cfg->max_correct_dist = 0.1f;
+    cfg->max_correct_angle = 60;
+    cfg->ao_multiplier = 1.2f;
+    cfg->ao_falloff = 1;
+    cfg->ao_num_samples = 17;
+    cfg->blur_size = 0.5f;
+}
+
+LTRAPI LTRCODE ltr_SetConfig(ltr_Scene* scene, ltr_Config* cfg)
+{
+    memcpy(&scene->cfg, cfg, sizeof(*cfg));
+    return 1;
+}
+
+LTRAPI ltr_Scene* ltr_CreateScene(void) { return new ltr_Scene; }
+
+LTRAPI void ltr_DestroyScene(ltr_Scene* scene)
+{
+    if (!scene) return;
+    scene->abort_flag = true;
+    delete scene;
+}
+
+LTRAPI void ltr_Start(ltr_Scene* scene)
+{
+    if (scene->worker.joinable()) scene->worker.join();
+    scene->clear_outputs();
+    scene->error.clear();
+    scene->abort_flag = false;
+    scene->completion = 0;
+    scene->stage = "starting";
+    scene->running = true;
+    scene->worker = std::thread([scene]() {
+        auto t0 = std::chrono::steady_clock::now();
+        try {
+            run_bake(scene);
+            scene->stats.ms_total =
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            scene->completion = 1;
+            scene->stage = nullptr;
+        } catch (const std::exception& e) {
+            scene->clear_outputs();
+            scene->error = e.what();
+            scene->completion = 1;
+            scene->stage = scene->abort_flag ? "aborted" : "error: bake failed (see ltrg_LastError)";
+        }
+        scene->running = false;
+    });
+}
+
+// The reference leaves this empty (lighter.cpp:1154-1157); here the bake
+// stops at the next stage boundary and reports stage "aborted".
+LTRAPI void ltr_Abort(ltr_Scene* scene) { scene->abort_flag = true; }
+
+// Returns 1 while the bake runs (lighter.cpp:1159-1164). A finished bake
+// reports "finished"; a failed or aborted one returns 0 with a stage text
+// starting with "error:" or "aborted" and no work outputs.
+LTRAPI LTRBOOL ltr_GetStatus(ltr_Scene* scene, ltr_WorkStatus* wsout)
+{
+    bool running = scene->running.load();
+    const char* st = scene->stage.load();
+    wsout->completion = scene->completion.load();
+    wsout->stage = st ? st : "finished";
+    if (!running && scene->worker.joinable()) scene->worker.join();
+    return running ? 1 : 0;
+}
+
+LTRAPI void ltr_Sleep(int ms) { std::this_thread::sleep_for(std::chrono::milliseconds(ms)); }
+
+LTRAPI ltr_Mesh* ltr_CreateMesh(ltr_Scene* scene, const char* ident, size_t ident_size)
+{
+    ltr_Mesh* m = new ltr_Mesh;
+    m->scene = scene;
+    if (ident) m->ident.assign(ident, ident_size);
+    scene->meshes.push_back(m);
+    return m;
+}
+
+// Copies strided streams (lighter.cpp:1226-1264). The reference's validity
+// test `index_count < 3 && index_count % 3 != 0` is kept; a part whose
+// indices point past its vertices is rejected as well, since the GPU raster
+// would otherwise read outside the vertex arrays.
+LTRAPI LTRBOOL ltr_MeshAddPart(ltr_Mesh* mesh, ltr_MeshPartInfo* p)
+{
+    if (!mesh || !p) return 0;
+    if (p->index_count < 3 && p->index_count % 3 != 0) return 0;
+    if (p->index_count && !p->indices) return 0;
+    for (u32 i = 0; i < p->index_count; ++i)
+        if (p->indices[i] >= p->vertex_count) return 0;
+    if (p->vertex_count && (!p->positions_f3 || !p->normals_f3 || !p->texcoords1_f2 || !p->texcoords2_f2)) return 0;
+    HostPart hp = {p->vertex_count, (u32) mesh->pos.size(), p->index_count, (u32) mesh->idx.size(), p->shadow};
+    for (u32 i = 0; i < p->vertex_count; ++i) {
+        V3 a, b;
+        V2 t1, t2;
+        memcpy(&a, (const char*) p->positions_f3 + (size_t) p->stride_positions * i, 12);
+        memcpy(&b, (const char*) p->normals_f3 + (size_t) p->stride_normals * i, 12);
+        memcpy(&t1, (const char*) p->texcoords1_f2 + (size_t) p->stride_texcoords1 * i, 8);
+        memcpy(&t2, (const char*) p->texcoords2_f2 + (size_t) p->stride_texcoords2 * i, 8);
+        mesh->pos.push_back(a);
+        mesh->nrm.push_back(b);
+        mesh->tex1.push_back(t1);
+        mesh->tex2.push_back(t2);
+    }
+    mesh->idx.insert(mesh->idx.end(), p->indices, p->indices + p->index_count);
+    mesh->parts.push_back(hp);
+    return 1;
+}
+
+LTRAPI LTRBOOL ltr_MeshAddInstance(ltr_Mesh* mesh, ltr_MeshInstanceInfo* mii)
+{
+    HostInst* mi = new HostInst;
+    mi->mesh = mesh;
+    mi->importance = mii->importance;
+    mi->shadow = !!mii->shadow;
+    if (mii->ident) mi->ident.assign(mii->ident, mii->ident_size);
+    memcpy(mi->matrix, mii->matrix, sizeof(float) * 16);
+    mesh->scene->insts.push_back(mi);
+    return 1;
+}
+
+// Direction vectors normalised, at least one shadow sample, and one rand()
+// draw per light as the reference makes (lighter.cpp:1282-1317), so that a
+// caller's srand() sequence reaches the AO stage in the same state.
+LTRAPI void ltr_LightAdd(ltr_Scene* scene, ltr_LightInfo* li)
+{
+    HostLight L;
+    L.type = li->type;
+    L.pos = mk(li->position[0], li->position[1], li->position[2]);
+    L.dir = normalized(mk(li->direction[0], li->direction[1], li->direction[2]));
+    L.up = normalized(mk(li->up_direction[0], li->up_direction[1], li->up_direction[2]));
+    L.color = mk(li->color_rgb[0], li->color_rgb[1], li->color_rgb[2]);
+    L.range = li->range;
+    L.power = li->power;
+    L.radius = li->light_radius;
+    L.nsamples = li->shadow_sample_count > 1 ? li->shadow_sample_count : 1;
+    L.out = li->spot_angle_out;
+    L.in = li->spot_angle_in;
+    L.curve = li->spot_curve;
+    (void) rand();
+    scene->lights.push_back(L);
+}
+
+LTRAPI void ltr_SampleAdd(ltr_Scene* scene, ltr_SampleInfo* si)
+{
+    ltr_SampleInfo c = *si;
+    c.out_color[0] = c.out_color[1] = c.out_color[2] = 0;
+    scene->samples.push_back(c);
+}
+
+LTRAPI void ltr_GetWorkOutputInfo(ltr_Scene* scene, ltr_WorkOutputInfo* o)
+{
+    o->lightmap_count = (u32) scene->outputs.size();
+    o->sample_count = (u32) scene->samples.size();
+    o->samples = scene->samples.empty() ? nullptr : scene->samples.data();
+}
+
+LTRAPI LTRBOOL ltr_GetWorkOutput(ltr_Scene* scene, u32 which, ltr_WorkOutput* wout)
+{
+    if (which >= scene->outputs.size()) return 0;
+    *wout = scene->outputs[which];
+    return 1;
+}
+
+// ---- extensions (lighter_gb300.h)
+
+LTRAPI void ltrg_GetOptions(ltr_Scene* scene, ltrg_Options* out) { *out = scene->opt; }
+
+LTRAPI LTRBOOL ltrg_SetOptions(ltr_Scene* scene, const ltrg_Options* o)
+{
+    if (o->device < 0 || o->radiosity_links < 0 || o->radiosity_links > 1 || o->radiosity_precision < 0 ||
+        o->radiosity_precision > 2 || o->refine_steps < 0 || o->refine_steps > 16)
+        return 0;
+    scene->opt = *o;
+    return 1;
+}
+
+LTRAPI LTRBOOL ltrg_GetStats(ltr_Scene* scene, ltrg_Stats* out)
+{
+    if (scene->running.load()) return 0;
+    *out = scene->stats;
+    return scene->stage.load() == nullptr ? 1 : 0;
+}
+
+LTRAPI const char* ltrg_LastError(ltr_Scene* scene)
+{
+    if (scene->running.load()) return nullptr;
+    return scene->error.empty() ? nullptr : scene->error.c_str();
+}
+
+LTRAPI LTRBOOL ltrg_Wait(ltr_Scene* scene)
+{
+    if (scene->worker.joinable()) scene->worker.join();
+    return scene->error.empty() && scene->stage.load() == nullptr ? 1 : 0;
+}
+
+LTRAPI LTRBOOL ltrg_TableSampleFn(ltr_Config* cfg, ltr_SampleRequest* req)
+{
+    const ltrg_SampleTable* t = (const ltrg_SampleTable*) cfg->userdata;
+    if (!t) return 0;
+    float fid = req->tex0u;
+    if (!(fid >= 0.0f)) return 0;
+    u32 id = (u32) fid;
+    if (id >= t->count) return 0;
+    if (t->diffuse_rgb)
+        for (int c = 0; c < 3; ++c) req->out_diffuse_color[c] = t->diffuse_rgb[id * 3 + c];
+    if (t->emissive_rgb)
+        for (int c = 0; c < 3; ++c) req->out_emissive_color[c] = t->emissive_rgb[id * 3 + c];
+    return 1;
+}
+
+LTRAPI u32 ltrdbg_InstanceCount(ltr_Scene* s) { return (u32) s->insts.size(); }
+
+LTRAPI u32 ltrdbg_SampleCount(ltr_Scene* s, u32 inst)
+{
+    if (inst >= s->dump.size()) return 0;
+    return (u32) s->dump[inst].loc.size();
+}
+
+LTRAPI LTRBOOL ltrdbg_LightmapSize(ltr_Scene* s, u32 inst, u32* wh)
+{
+    if (inst >= s->insts.size()) return 0;
+    wh[0] = s->insts[inst]->w;
+    wh[1] = s->insts[inst]->h;
+    return 1;
+}
+
+LTRAPI LTRBOOL ltrdbg_GetSamples(ltr_Scene* s, u32 inst, float* pos3, float* nrm3, u32* loc, float* radinfo4,
+                                 float* color3)
+{
+    if (inst >= s->dump.size()) return 0;
+    const SampleDump& d = s->dump[inst];
+    size_t n = d.loc.size();
+    if (pos3) memcpy(pos3, d.pos.data(), n * 12);
+    if (nrm3) memcpy(nrm3, d.nrm.data(), n * 12);
+    if (loc) memcpy(loc, d.loc.data(), n * 4);
+    if (radinfo4) memcpy(radinfo4, d.radinfo.data(), n * 16);
+    if (color3) memcpy(color3, d.color.data(), n * 12);
+    return 1;
+}
+
+LTRAPI u32 ltrdbg_RadLinkCount(ltr_Scene* s) { return s->rad_links; }
+
+}  // extern "C"

@@ -1,0 +1,1413 @@
+// The bake on the GPU: the stage order of ltr_Scene::Job_MainProc
+// (lighter.cpp:1046-1145) with every per-texel, per-light, per-pair and
+// per-ray loop of the reference turned into CUDA kernels.
+//
+//   host   transform instances, size lightmaps (size_fn), build triangle and
+//          raster records, cull lights against instance boxes
+//   GPU    BVH build (bvh.cu)
+//   GPU    sample generation: two raster passes with last-writer-wins keys,
+//          compaction, concave-edge offset and overlap correction
+//   GPU    direct light (sphere-traced penumbra per (light, sample))
+//   GPU    radiosity: dense form factors + visibility, bounces as F x colours
+//   GPU    ambient occlusion (one warp per sample, one lane per ray)
+//   GPU    finalize: scatter, 3 dilation sweeps, separable blur, ds2x, normals
+//   host   readback into scene-owned output buffers
+#include <cuda_runtime.h>
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <thread>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "bvh.cuh"
+#include "radiosity.cuh"
+#include "reftree.hpp"
+#include "scene.hpp"
+
+namespace lg {
+
+namespace {
+
+void ck(cudaError_t e, const char* what, int line)
+{
+    if (e != cudaSuccess)
+        throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(e) + " at bake.cu:" +
+                                 std::to_string(line) + " (" + what + ")");
+}
+#define CK(x) ck((x), #x, __LINE__)
+
+constexpr int kThreads = 256;
+constexpr u32 kNoLoc = 0xffffffffu;
+
+inline unsigned blocks_for(size_t n, int threads = kThreads, size_t cap = 152 * 64)
+{
+    size_t b = (n + threads - 1) / threads;
+    if (b > cap) b = cap;
+    return (unsigned) (b ? b : 1);
+}
+
+// ----------------------------------------------------------------------------- device-side records
+
+struct DLight {
+    int type;
+    float pos[3], dir[3], color[3];
+    float range, power, radius, out_rad, diff, curve;
+};
+
+// Raster record of one triangle (RasterizeInstance, lighter.cpp:32-66):
+//   [0..5] lightmap-space p1,p2,p3  [6..14] world pos  [15..23] world normal
+//   [24..29] uv1  [30] part  [31] sample area
+constexpr int kRT = 32;
+
+struct Counters {
+    unsigned long long shadow_evals, distance_queries, ao_rays, rad_pairs, rad_vis_rays, node_visits, links, pad;
+};
+
+// Warp total of a per-thread count, added once per warp; every lane of the
+// warp must call it (used after grid-stride loops, where all lanes arrive).
+__device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long long v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(dst, v);
+}
+
+// ----------------------------------------------------------------------------- raster
+
+// Texel (x, y) is covered by the triangle when it lies within `margin` of all
+// three edges for either winding (lighter_math.cpp:281-300).
+__device__ __forceinline__ bool raster_inside(const float* r, int x, int y, float margin)
+{
+    V2 p1 = mk2(r[0], r[1]), p2 = mk2(r[2], r[3]), p3 = mk2(r[4], r[5]);
+    V2 e12 = p2 - p1, e13 = p3 - p1, e23 = p3 - p2;
+    V2 n1 = normalized2(mk2(e12.y, -e12.x));
+    V2 n2 = normalized2(mk2(e23.y, -e23.x));
+    V2 n3t = normalized2(mk2(e13.y, -e13.x));
+    V2 n3 = mk2(-n3t.x, -n3t.y);
+    float d1 = dot2(n1, p1), d2 = dot2(n2, p2), d3 = dot2(n3, p3);
+    V2 p = mk2((float) x, (float) y);
+    float pd1 = dot2(p, n1), pd2 = dot2(p, n2), pd3 = dot2(p, n3);
+    return (pd1 <= d1 + margin && pd2 <= d2 + margin && pd3 <= d3 + margin) ||
+           (pd1 + margin >= d1 && pd2 + margin >= d2 && pd3 + margin >= d3);
+}
+
+__global__ void k_raster_mark(int pass, float margin, const float* __restrict__ rt, const u32* __restrict__ rinst,
+                              const int4* __restrict__ bbox, const unsigned long long* __restrict__ off, int ntri,
+                              unsigned long long nwork, const unsigned long long* __restrict__ tex_off,
+                              const u32* __restrict__ inst_w, u32* __restrict__ keys)
+{
+    for (unsigned long long w = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; w < nwork;
+         w += (unsigned long long) gridDim.x * blockDim.x) {
+        int lo = 0, hi = ntri - 1;   // largest k with off[k] <= w
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (off[mid] <= w) lo = mid; else hi = mid - 1;
+        }
+        int k = lo;
+        int4 b = bbox[k];
+        unsigned long long local = w - off[k];
+        int x = b.x + (int) (local % (unsigned) b.z);
+        int y = b.y + (int) (local / (unsigned) b.z);
+        if (!raster_inside(rt + (size_t) k * kRT, x, y, margin)) continue;
+        u32 inst = rinst[k];
+        unsigned long long g = tex_off[inst] + (unsigned long long) x + (unsigned long long) inst_w[inst] * y;
+        atomicMax(&keys[g], 1u + ((u32) pass << 30) + (u32) k);
+    }
+}
+
+// Attribute interpolation of the winning triangle (lighter_math.cpp:285-299).
+__global__ void k_raster_resolve(unsigned long long ntex, const u32* __restrict__ keys, const float* __restrict__ rt,
+                                 const u32* __restrict__ rinst, const unsigned long long* __restrict__ tex_off,
+                                 const u32* __restrict__ inst_w, float4* __restrict__ R1, float4* __restrict__ R2,
+                                 float4* __restrict__ R3, u32* __restrict__ flags)
+{
+    for (unsigned long long g = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; g < ntex;
+         g += (unsigned long long) gridDim.x * blockDim.x) {
+        u32 key = keys[g];
+        if (key == 0) { flags[g] = 0; continue; }
+        u32 k = (key - 1u) & ((1u << 30) - 1u);
+        const float* r = rt + (size_t) k * kRT;
+        u32 inst = rinst[k];
+        unsigned long long local = g - tex_off[inst];
+        u32 w = inst_w[inst];
+        int x = (int) (local % w), y = (int) (local / w);
+        V2 p1 = mk2(r[0], r[1]), p2 = mk2(r[2], r[3]), p3 = mk2(r[4], r[5]);
+        V2 e12 = p2 - p1, e13 = p3 - p1;
+        float vc = cross2(e12, e13);
+        V2 q = mk2(x - p1.x, y - p1.y);
+        float s = cross2(q, e13) / vc;
+        float t = cross2(e12, q) / vc;
+        s = fmax_(fmin_(s, 1.0f), 0.0f);
+        t = fmax_(fmin_(t, 1.0f), 0.0f);
+        V3 a1 = mk(r[6], r[7], r[8]), a2 = mk(r[9], r[10], r[11]), a3 = mk(r[12], r[13], r[14]);
+        V3 b1 = mk(r[15], r[16], r[17]), b2 = mk(r[18], r[19], r[20]), b3 = mk(r[21], r[22], r[23]);
+        V3 pa = a1 + (a2 - a1) * s + (a3 - a1) * t;
+        V3 pb = b1 + (b2 - b1) * s + (b3 - b1) * t;
+        float c1x = r[24], c1y = r[25], c2x = r[26], c2y = r[27], c3x = r[28], c3y = r[29];
+        float part = r[30], area = r[31];
+        float4 pc = make_float4(c1x + (c2x - c1x) * s + (c3x - c1x) * t, c1y + (c2y - c1y) * s + (c3y - c1y) * t,
+                                part + (part - part) * s + (part - part) * t, area + (area - area) * s + (area - area) * t);
+        R1[g] = st4(pa, 0.0f);
+        R2[g] = st4(pb, 0.0f);
+        R3[g] = pc;
+        flags[g] = is_zero(pb) ? 0u : 1u;
+    }
+}
+
+__global__ void k_compact(unsigned long long ntex, const u32* __restrict__ flags, const u32* __restrict__ scan,
+                          const float4* __restrict__ R1, const float4* __restrict__ R2, const float4* __restrict__ R3,
+                          const unsigned long long* __restrict__ tex_off, int n_inst, u32 n_probe,
+                          float4* __restrict__ spos, float4* __restrict__ snrm, float4* __restrict__ srad,
+                          u32* __restrict__ sloc, u32* __restrict__ sinst)
+{
+    for (unsigned long long g = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; g < ntex;
+         g += (unsigned long long) gridDim.x * blockDim.x) {
+        if (!flags[g]) continue;
+        int lo = 1, hi = n_inst - 1;   // instance with tex_off[inst] <= g (instance 0 owns no texels)
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (tex_off[mid] <= g) lo = mid; else hi = mid - 1;
+        }
+        u32 s = n_probe + scan[g];
+        spos[s] = R1[g];
+        snrm[s] = st4(normalized(ld3(R2[g])), 0.0f);
+        srad[s] = R3[g];
+        sloc[s] = (u32) (g - tex_off[lo]);
+        sinst[s] = (u32) lo;
+    }
+}
+
+// ----------------------------------------------------------------------------- sample offset + correction
+
+struct FixupArgs {
+    BvhView bvh;
+    ErrFlag err;
+    const float4* ref_nodes;   // 2 per node: (mn.xyz, mx.x), (mx.yz, ch, ido)
+    const int* ref_items;      // <count, ids...> lists
+    const int4* ref_inst;      // per instance: node offset, item offset, triangle offset, node count
+    const float* tri_xyz;      // shadow-part triangles, instance by instance in local order
+    int n_inst;
+    u32 n_probe, n_samples;
+    float max_correct_dist, corr_min_dot;
+    float4* spos;
+    const float4* snrm;
+    const float4* srad;
+};
+
+// Concave-edge push of TriTree::OffsetSample (lighter_math.cpp:991-1044) for
+// one triangle (instance-local index `local`) of instance `inst`.
+__device__ __forceinline__ void offset_one(const FixupArgs& a, V3 P1, V3 P2, V3 P3, int local, u32 inst, V3& P, V3 N,
+                                           float dist)
+{
+    float nd = point_tri_dist(P, P1, P2, P3);
+    if (!(nd < dist)) return;
+    V3 TPN = -tri_normal_rev(P1, P2, P3);
+    float TPD = dot(TPN, P1);
+    float sig = dot(TPN, P) - TPD;
+    if (!(sig <= kSmall)) return;
+    V3 Pextr = P + normalized(TPN + N) * -sig * 1.41f;
+    if (!point_proj_on_tri(Pextr, P1, P2, P3)) return;
+    float pdot = dot(TPN, N);
+    if (!(fabsf(pdot) < 0.95f)) return;
+    V3 proj = normalized(TPN - N * pdot);
+    float df = 1.0f - fabsf(pdot);
+    V3 Pnew = P + proj * (-sig / df + kSmall);
+    int hit_local = -1;
+    float r = bvh_closest_inst(a.bvh, P + (N + proj) * kSmall, Pnew, inst, a.err, &hit_local);
+    if (r >= 0.9f || hit_local == local) P = Pnew;
+}
+
+__global__ void k_fixup(FixupArgs a)
+{
+    u32 s = a.n_probe + blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.n_samples) return;
+    V3 P = ld3(a.spos[s]);
+    V3 N = ld3(a.snrm[s]);
+    float dist = sqrtf(a.srad[s].w);
+    // every instance's tree in instance order (lighter.cpp:445-446): a
+    // depth-first walk (node items, left subtree, right subtree) of the
+    // reference-shaped tree with a query box fixed at the start, while P moves
+    for (int k = 1; k < a.n_inst; ++k) {
+        int4 ri = a.ref_inst[k];
+        if (ri.w == 0) continue;
+        V3 qmn = P - splat(dist), qmx = P + splat(dist);
+        int stack[40];
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp > 0) {
+            int node = stack[--sp];
+            float4 n0 = __ldg(&a.ref_nodes[2 * (ri.x + node)]);
+            float4 n1 = __ldg(&a.ref_nodes[2 * (ri.x + node) + 1]);
+            if (qmn.x > n0.w || qmx.x < n0.x || qmn.y > n1.x || qmx.y < n0.y || qmn.z > n1.y || qmx.z < n0.z) continue;
+            int ch = __float_as_int(n1.z), ido = __float_as_int(n1.w);
+            if (ido != -1) {
+                const int* it = a.ref_items + ri.y + ido;
+                int cnt = it[0];
+                for (int i = 0; i < cnt; ++i) {
+                    int id = it[1 + i];
+                    const float* p = a.tri_xyz + 9 * (size_t) (ri.z + id);
+                    offset_one(a, mk(p[0], p[1], p[2]), mk(p[3], p[4], p[5]), mk(p[6], p[7], p[8]), id, (u32) k, P, N,
+                               dist);
+                }
+            }
+            if (ch != -1) {
+                if (sp + 2 <= 40) { stack[sp++] = ch; stack[sp++] = node + 1; }
+                else raise_err(a.err, 1u);
+            }
+        }
+    }
+    // push in front of overlapping faces (lighter.cpp:449-465); the
+    // reference's BSP query is replaced by the closest hit over occluders
+    if (a.max_correct_dist != 0.0f) {
+        int left = 100;
+        float md = a.max_correct_dist;
+        V3 PEnd = P + N * md;
+        while (md > kSmall && left-- > 0) {
+            V3 dn = normalized(PEnd - P);
+            V3 mA = P + dn * kSmall, mB = PEnd - dn * kSmall;
+            int ht = -1;
+            float q = bvh_closest(a.bvh, mA, mB, a.err, &ht);
+            V3 hn = mk(0, 0, 0);
+            if (ht >= 0) {
+                V3 P1, P2, P3; u32 meta, local;
+                load_tri(a.bvh, ht, P1, P2, P3, meta, local);
+                hn = tri_normal_rev(P1, P2, P3);
+            }
+            if (-dot(hn, N) < a.corr_min_dot) break;
+            if (q < kSmall) q = kSmall;
+            P = P * (1.0f - q) + PEnd * q;
+            md *= (1.0f - q);
+        }
+    }
+    a.spos[s] = st4(P, 0.0f);
+}
+
+// ----------------------------------------------------------------------------- direct light
+
+// Sphere-traced soft-shadow factor (ltr_Scene::CalcInvShadowFactor, lighter.cpp:190-207).
+__device__ __forceinline__ float inv_shadow(const BvhView& bvh, V3 from, V3 to, float k, ErrFlag err, u32& nq, u32& nv)
+{
+    V3 rd = normalized(to - from);
+    float maxt = len(to - from);
+    float res = 1.0f;
+    for (float t = 0.001f; t < maxt;) {
+        float h = bvh_distance(bvh, from + rd * t, kMaxPenumbraSize, err, &nv);
+        ++nq;
+        if (h < 0.001f) return 0.0f;
+        res = fmin_(res, h / fmin_(t * k, kMaxPenumbraSize));
+        h = fmin_(h, kMaxPenumbraStep);
+        t += h;
+    }
+    return res;
+}
+
+struct DirectArgs {
+    BvhView bvh;
+    ErrFlag err;
+    const DLight* lights;
+    int n_lights, n_inst;
+    const unsigned char* lit;   // [light][instance]
+    u32 n_samples;
+    const float4* spos;
+    const float4* snrm;
+    const u32* sinst;
+    float* kval;                // [light][sample] colour multiplier, 0 when nothing is added
+    float4* ndir;               // [light][sample] normal-map contribution, w = 1 when recorded (may be null)
+    Counters* counters;
+};
+
+// One (light, sample) pair of Job_LMRender_{Point,Spot,Direct}_Inner (lighter.cpp:485-600).
+__global__ void k_direct(DirectArgs a)
+{
+    unsigned long long total = (unsigned long long) a.n_lights * a.n_samples;
+    unsigned long long c_traced = 0, c_nq = 0, c_nv = 0;
+    for (unsigned long long w = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; w < total;
+         w += (unsigned long long) gridDim.x * blockDim.x) {
+        int l = (int) (w / a.n_samples);
+        u32 s = (u32) (w % a.n_samples);
+        const DLight L = a.lights[l];
+        u32 inst = a.sinst[s];
+        float kv = 0.0f;
+        float4 nd = make_float4(0, 0, 0, 0);
+        u32 nq = 0, nv = 0, traced = 0;
+        if (a.lit[(size_t) l * a.n_inst + inst]) {
+            V3 SP = ld3(a.spos[s]), SN = ld3(a.snrm[s]);
+            V3 Lpos = mk(L.pos[0], L.pos[1], L.pos[2]);
+            V3 Ldir = mk(L.dir[0], L.dir[1], L.dir[2]);
+            V3 Lcol = mk(L.color[0], L.color[1], L.color[2]);
+            if (L.type == 1 || L.type == 2) {
+                V3 s2l = Lpos - SP;
+                float dist = len(s2l);
+                if (dist) s2l = s2l / dist;
+                float f_dist = powf(1 - fmin_(1.0f, dist / L.range), L.power);
+                float f_ndotl = fmax_(0.0f, dot(s2l, SN));
+                float f_dir = 1.0f;
+                bool go;
+                if (L.type == 2) {
+                    float ang = acosf(fmin_(1.0f, dot(s2l, -Ldir)));
+                    f_dir = fmax_(0.0f, fmin_(1.0f, (ang - L.out_rad) / L.diff));
+                    f_dir = powf(f_dir, L.curve);
+                    go = !(f_dist * f_ndotl * f_dir <= 0);
+                } else {
+                    go = !(f_dist * f_ndotl <= 0);
+                }
+                if (go) {
+                    float vis = inv_shadow(a.bvh, SP + SN * kShadowOffset, Lpos, L.radius, a.err, nq, nv);
+                    traced = 1;
+                    kv = L.type == 2 ? f_dist * f_ndotl * f_dir * vis : f_dist * f_ndotl * vis;
+                    float fac = L.type == 2 ? f_dist * f_dir * vis * f_ndotl * brightness(Lcol)
+                                            : f_dist * vis * f_ndotl * brightness(Lcol);
+                    if (fac > 0) nd = st4(s2l * fac, 1.0f);
+                }
+            } else if (L.type == 3) {
+                float f_ndotl = fmax_(0.0f, dot(Ldir, SN));
+                float vis = inv_shadow(a.bvh, SP + SN * kShadowOffset, SP + Ldir * L.range, L.radius, a.err, nq, nv);
+                traced = 1;
+                kv = f_ndotl * vis;
+                float fac = vis * f_ndotl * brightness(Lcol);
+                if (fac > 0) nd = st4(Ldir * fac, 1.0f);
+            }
+        }
+        a.kval[w] = kv;
+        if (a.ndir) a.ndir[w] = (inst == 0) ? make_float4(0, 0, 0, 0) : nd;
+        c_traced += traced;
+        c_nq += nq;
+        c_nv += nv;
+    }
+    if (a.counters) {
+        warp_add(&a.counters->shadow_evals, c_traced);
+        warp_add(&a.counters->distance_queries, c_nq);
+        warp_add(&a.counters->node_visits, c_nv);
+    }
+}
+
+// Per sample, ambient plus every light's term in light order (lighter.cpp:504, 542, 589).
+__global__ void k_accumulate(u32 n_samples, int n_lights, const DLight* __restrict__ lights, const float* __restrict__ kval,
+                             float amb_r, float amb_g, float amb_b, float4* __restrict__ lm)
+{
+    u32 s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_samples) return;
+    V3 c = mk(amb_r, amb_g, amb_b);
+    for (int l = 0; l < n_lights; ++l) {
+        float k = kval[(size_t) l * n_samples + s];
+        if (k != 0.0f) c += mk(lights[l].color[0], lights[l].color[1], lights[l].color[2]) * k;
+    }
+    lm[s] = st4(c, 0.0f);
+}
+
+// ----------------------------------------------------------------------------- ambient occlusion
+
+__device__ __forceinline__ V3 spiral_dir(V3 dir, float randoff, int i, int count)
+{
+    float q = (i + 0.5f) / count;
+    float cos_side = sqrtf(q);
+    float sin_side = sinf(acosf(cos_side));
+    float angle = (i + randoff) * (137.508f / 180.0f * 3.14159265358979323846f);
+    float ca = cosf(angle), sa = sinf(angle);
+    V3 diffvec = mk(dir.y, -dir.z, dir.x);
+    V3 up = normalized(cross(dir, diffvec));
+    V3 rt = cross(dir, up);
+    return ca * sin_side * rt + sa * sin_side * up + cos_side * dir;
+}
+
+struct AoArgs {
+    BvhView bvh;
+    ErrFlag err;
+    u32 n_samples;
+    const float4* spos;
+    const float4* snrm;
+    const float* randoff;
+    float4* lm;
+    float dist, falloff, mult, effect;
+    int ns;
+    float aoc[3];
+    Counters* counters;
+};
+
+// Job_AORender_Inner (lighter.cpp:799-841): one warp per sample, one lane per
+// ray; the hit fractions are summed in ray order like the reference loop.
+__global__ void k_ao(AoArgs a)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned long long warp = (blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nwarps = ((unsigned long long) gridDim.x * blockDim.x) >> 5;
+    for (unsigned long long s = warp; s < a.n_samples; s += nwarps) {
+        V3 SP = ld3(a.spos[s]), SN = ld3(a.snrm[s]);
+        V3 ro = SP + SN * (kSmall * 2);
+        float ro_off = a.randoff[s];
+        float f = 0;
+        for (int c = 0; c < a.ns; c += 32) {
+            int r = c + lane;
+            float hit = kNoHit;
+            if (r < a.ns) {
+                V3 rd = spiral_dir(SN, ro_off, r, a.ns) * a.dist;
+                V3 B = ro + rd;
+                V3 dn = normalized(B - ro);
+                hit = bvh_closest(a.bvh, ro + dn * kSmall, B - dn * kSmall, a.err, nullptr);
+            }
+            int m = min(32, a.ns - c);
+            for (int k = 0; k < m; ++k) {
+                float v = __shfl_sync(0xffffffffu, hit, k);
+                if (v < 1.0f) f += 1.0f - v;
+            }
+        }
+        if (lane == 0) {
+            f /= a.ns;
+            f = fmin_(f * a.mult, 1.0f);
+            if (a.falloff) f = powf(f, a.falloff);
+            V3 out = ld3(a.lm[s]);
+            V3 aoc = mk(a.aoc[0], a.aoc[1], a.aoc[2]);
+            if (a.effect >= 0) out = out * (1 - f * (1 - a.effect)) + aoc * f;
+            else out = lerp3(out, lerp3(aoc, aoc * out, -a.effect), f);
+            a.lm[s] = st4(out, 0.0f);
+            if (a.counters) atomicAdd(&a.counters->ao_rays, (unsigned long long) a.ns);
+        }
+    }
+}
+
+// ----------------------------------------------------------------------------- finalize
+
+__device__ __forceinline__ int find_inst(const unsigned long long* off, int n_inst, unsigned long long g)
+{
+    int lo = 1, hi = n_inst - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= g) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_scatter(u32 n_probe, u32 n_samples, const u32* __restrict__ sloc, const u32* __restrict__ sinst,
+                          const float4* __restrict__ lm, const unsigned long long* __restrict__ tex_off,
+                          float* __restrict__ img, unsigned char* __restrict__ mask)
+{
+    u32 s = n_probe + blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_samples) return;
+    unsigned long long g = tex_off[sinst[s]] + sloc[s];
+    float4 c = lm[s];
+    img[3 * g + 0] = c.x;
+    img[3 * g + 1] = c.y;
+    img[3 * g + 2] = c.z;
+    mask[g] = 1;
+}
+
+// One extrapolating dilation sweep (lighter.cpp:884-943): `old` is the mask
+// before the sweep, `next` receives newly set texels; colours of texels set
+// in `old` are never written during the sweep, so reading them is race-free.
+__global__ void k_dilate(unsigned long long ntex, int n_inst, const unsigned long long* __restrict__ tex_off,
+                         const u32* __restrict__ inst_w, const u32* __restrict__ inst_h,
+                         const unsigned char* __restrict__ old, unsigned char* __restrict__ next, float* img)
+{
+    for (unsigned long long g = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; g < ntex;
+         g += (unsigned long long) gridDim.x * blockDim.x) {
+        if (old[g]) continue;
+        int inst = find_inst(tex_off, n_inst, g);
+        unsigned long long base = tex_off[inst];
+        u32 w = inst_w[inst], h = inst_h[inst];
+        unsigned long long local = g - base;
+        u32 x = (u32) (local % w), y = (u32) (local / w);
+        auto isset = [&](u32 xx, u32 yy) { return xx < w && yy < h && old[base + xx + (unsigned long long) yy * w]; };
+        auto col = [&](u32 xx, u32 yy) {
+            const float* p = img + 3 * (base + xx + (unsigned long long) yy * w);
+            return mk(p[0], p[1], p[2]);
+        };
+        V3 c = mk(0, 0, 0);
+        int cnt = 0;
+        if (isset(x - 1, y)) { c += isset(x - 2, y) ? lerp3(col(x - 2, y), col(x - 1, y), 2.0f) : col(x - 1, y); cnt++; }
+        if (isset(x + 1, y)) { c += isset(x + 2, y) ? lerp3(col(x + 2, y), col(x + 1, y), 2.0f) : col(x + 1, y); cnt++; }
+        if (isset(x, y - 1)) { c += isset(x, y - 2) ? lerp3(col(x, y - 2), col(x, y - 1), 2.0f) : col(x, y - 1); cnt++; }
+        if (isset(x, y + 1)) { c += isset(x, y + 2) ? lerp3(col(x, y + 2), col(x, y + 1), 2.0f) : col(x, y + 1); cnt++; }
+        if (cnt) {
+            c = c / (float) cnt;
+            float* p = img + 3 * g;
+            p[0] = fmax_(c.x, 0.0f);
+            p[1] = fmax_(c.y, 0.0f);
+            p[2] = fmax_(c.z, 0.0f);
+            next[g] = 1;
+        }
+    }
+}
+
+// Row convolution with clamp-to-edge taps, written transposed
+// (Convolve_Transpose, lighter_math.cpp:367-398). `transposed` selects the
+// second pass, whose input rows are the instance's columns.
+__global__ void k_conv_t(unsigned long long ntex, int n_inst, const unsigned long long* __restrict__ tex_off,
+                         const u32* __restrict__ inst_w, const u32* __restrict__ inst_h, int transposed, int ext,
+                         const float* __restrict__ kern, const float* __restrict__ src, float* __restrict__ dst)
+{
+    for (unsigned long long g = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; g < ntex;
+         g += (unsigned long long) gridDim.x * blockDim.x) {
+        int inst = find_inst(tex_off, n_inst, g);
+        unsigned long long base = tex_off[inst];
+        u32 W = transposed ? inst_h[inst] : inst_w[inst];
+        u32 H = transposed ? inst_w[inst] : inst_h[inst];
+        unsigned long long local = g - base;
+        u32 x = (u32) (local % W), y = (u32) (local / W);
+        const float* row = src + 3 * (base + (unsigned long long) y * W);
+        float s0 = 0, s1 = 0, s2 = 0;
+        for (int i = -ext; i <= ext; ++i) {
+            int xx = (int) x + i;
+            xx = xx < 0 ? 0 : (xx >= (int) W ? (int) W - 1 : xx);
+            float kq = kern[i + ext];
+            s0 += row[3 * xx + 0] * kq;
+            s1 += row[3 * xx + 1] * kq;
+            s2 += row[3 * xx + 2] * kq;
+        }
+        float* o = dst + 3 * (base + y + (unsigned long long) H * x);
+        o[0] = s0; o[1] = s1; o[2] = s2;
+    }
+}
+
+// Downsample2X (lighter_math.cpp:400-424) into a separate per-instance layout.
+__global__ void k_ds2x(unsigned long long nout, int n_inst, const unsigned long long* __restrict__ out_off,
+                       const unsigned long long* __restrict__ tex_off, const u32* __restrict__ inst_w,
+                       const u32* __restrict__ inst_h, const float* __restrict__ src, float* __restrict__ dst)
+{
+    for (unsigned long long g = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; g < nout;
+         g += (unsigned long long) gridDim.x * blockDim.x) {
+        int inst = find_inst(out_off, n_inst, g);
+        u32 w = inst_w[inst], h = inst_h[inst];
+        u32 hw = max(w / 2, 1u);
+        unsigned long long local = g - out_off[inst];
+        u32 x = (u32) (local % hw), y = (u32) (local / hw);
+        u32 sx0 = (x * 2) % w, sy0 = (y * 2) % h, sx1 = (x * 2 + 1) % w, sy1 = (y * 2 + 1) % h;
+        const float* b = src + 3 * tex_off[inst];
+        auto col = [&](u32 xx, u32 yy) { const float* p = b + 3 * (xx + (unsigned long long) yy * w); return mk(p[0], p[1], p[2]); };
+        V3 avg = (col(sx0, sy0) + col(sx1, sy0) + col(sx0, sy1) + col(sx1, sy1)) * 0.25f;
+        float* o = dst + 3 * g;
+        o[0] = avg.x; o[1] = avg.y; o[2] = avg.z;
+    }
+}
+
+// Normal/"focus" data per sample (lighter.cpp:977-1027): ambient-weighted
+// normal plus the recorded light directions in light order, then the product
+// of the per-light agreement terms.
+__global__ void k_normals(u32 n_probe, u32 n_samples, int n_lights, const float4* __restrict__ ndir,
+                          const float4* __restrict__ snrm, const u32* __restrict__ sloc, const u32* __restrict__ sinst,
+                          const unsigned long long* __restrict__ nout_off, const u32* __restrict__ cap, float amb,
+                          float* __restrict__ out)
+{
+    u32 s = n_probe + blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_samples) return;
+    V3 n = ld3(snrm[s]) * amb;
+    int cnt = 1;
+    for (int l = 0; l < n_lights; ++l) {
+        float4 c = ndir[(size_t) l * n_samples + s];
+        if (c.w != 0.0f) { n += ld3(c); cnt++; }
+    }
+    n = n / (float) cnt;
+    float mindot = 1;
+    for (int l = 0; l < n_lights; ++l) {
+        float4 c = ndir[(size_t) l * n_samples + s];
+        if (c.w == 0.0f) continue;
+        V3 cn = ld3(c);
+        float d = fmax_(dot(normalized(n), normalized(cn)), 0.0f);
+        float t = fmin_(len(cn) / len(n), 1.0f);
+        d = 1.0f * (1.0f - t) + d * t;
+        mindot *= d;
+    }
+    u32 inst = sinst[s];
+    if (sloc[s] >= cap[inst]) return;   // ds2x shrinks the image but keeps full-size texel ids
+    V3 N = normalized(n);
+    float* o = out + 4 * (nout_off[inst] + sloc[s]);
+    o[0] = N.x; o[1] = N.y; o[2] = N.z; o[3] = mindot;
+}
+
+// ----------------------------------------------------------------------------- host helpers
+
+// Device arena: every buffer of one bake, freed (stream-ordered) at the end.
+struct Arena {
+    cudaStream_t st = nullptr;
+    std::vector<void*> ptrs;
+    size_t bytes = 0;
+    template <class T> T* alloc(size_t n)
+    {
+        void* p = nullptr;
+        size_t b = (n ? n : 1) * sizeof(T);
+        CK(cudaMallocAsync(&p, b, st));
+        ptrs.push_back(p);
+        bytes += b;
+        return (T*) p;
+    }
+    template <class T> T* upload(const std::vector<T>& v)
+    {
+        T* d = alloc<T>(v.size());
+        if (!v.empty()) CK(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+        return d;
+    }
+    template <class T> T* zeros(size_t n)
+    {
+        T* d = alloc<T>(n);
+        CK(cudaMemsetAsync(d, 0, (n ? n : 1) * sizeof(T), st));
+        return d;
+    }
+    void release()
+    {
+        for (void* p : ptrs) cudaFreeAsync(p, st);
+        ptrs.clear();
+    }
+    ~Arena()
+    {
+        release();
+        if (st) {
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
+    }
+};
+
+struct StageClock {
+    cudaStream_t st;
+    std::vector<cudaEvent_t> evs;
+    cudaEvent_t mark()
+    {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        CK(cudaEventRecord(e, st));
+        evs.push_back(e);
+        return e;
+    }
+    static double ms(cudaEvent_t a, cudaEvent_t b)
+    {
+        float m = 0;
+        cudaEventElapsedTime(&m, a, b);
+        return m;
+    }
+    ~StageClock()
+    {
+        for (auto e : evs) cudaEventDestroy(e);
+    }
+};
+
+inline float randf_host() { return (float) rand() / (float) RAND_MAX; }   // lighter_int.hpp:271
+
+void check_abort(ltr_Scene* s)
+{
+    if (s->abort_flag.load()) throw std::runtime_error("aborted by ltr_Abort");
+}
+
+// Row-vector transform and normal matrix of Job_PreXForm_Inner (lighter.cpp:292-341,
+// lighter_int.hpp:511-545). The 2x2 minors keep the operand order of the
+// 4x4 cofactor expansion of Mat4::InvertTo applied to [R 0; 0 1].
+void prexform(ltr_Scene* S, HostInst* mi)
+{
+    const float* m = mi->matrix;   // m[r*4+c]
+    ltr_Mesh* me = mi->mesh;
+    size_t nv = me->pos.size();
+    mi->vpos.resize(nv); mi->vnrm.resize(nv); mi->vtex.resize(nv); mi->ltex.resize(nv);
+    const float a0 = m[0], a1 = m[1], a2 = m[2], a4 = m[4], a5 = m[5], a6 = m[6], a8 = m[8], a9 = m[9], a10 = m[10];
+    float c[16] = {0};
+    c[0] = a5 * a10 - a9 * a6;
+    c[4] = -(a4 * a10) + a8 * a6;
+    c[8] = a4 * a9 - a8 * a5;
+    c[1] = -(a1 * a10) + a9 * a2;
+    c[5] = a0 * a10 - a8 * a2;
+    c[9] = -(a0 * a9) + a8 * a1;
+    c[2] = a1 * a6 - a5 * a2;
+    c[6] = -(a0 * a6) + a4 * a2;
+    c[10] = a0 * a5 - a4 * a1;
+    float det = a0 * c[0] + a1 * c[4] + a2 * c[8];
+    float inv[16];
+    if (det == 0) {
+        for (int i = 0; i < 16; ++i) inv[i] = 0;
+        inv[0] = a0; inv[1] = a1; inv[2] = a2; inv[4] = a4; inv[5] = a5; inv[6] = a6; inv[8] = a8; inv[9] = a9;
+        inv[10] = a10;
+    } else {
+        float d = 1.0f / det;
+        for (int i = 0; i < 16; ++i) inv[i] = c[i] * d;
+    }
+    // normal matrix N[r][k] = inv[k*4+r]; transform of (n, 0) by rows
+    for (size_t i = 0; i < nv; ++i) {
+        V3 v = me->pos[i];
+        mi->vpos[i] = mk(v.x * m[0] + v.y * m[4] + v.z * m[8] + m[12] * 1.0f,
+                         v.x * m[1] + v.y * m[5] + v.z * m[9] + m[13] * 1.0f,
+                         v.x * m[2] + v.y * m[6] + v.z * m[10] + m[14] * 1.0f);
+        V3 n = me->nrm[i];
+        mi->vnrm[i] = normalized(mk(n.x * inv[0] + n.y * inv[1] + n.z * inv[2] + inv[3] * 0.0f,
+                                    n.x * inv[4] + n.y * inv[5] + n.z * inv[6] + inv[7] * 0.0f,
+                                    n.x * inv[8] + n.y * inv[9] + n.z * inv[10] + inv[11] * 0.0f));
+    }
+    float area = 0.0f;
+    for (const HostPart& p : me->parts) {
+        const V3* vb = &mi->vpos[p.voff];
+        const u32* ib = &me->idx[p.ioff];
+        for (u32 t = 0; t < p.icount; t += 3) area += tri_area3(vb[ib[t]], vb[ib[t + 1]], vb[ib[t + 2]]);
+    }
+    u32 size[2] = {S->cfg.default_width, S->cfg.default_height};
+    if (!S->cfg.size_fn || !S->cfg.size_fn(&S->cfg, me->ident.c_str(), me->ident.size(), mi->ident.c_str(),
+                                           mi->ident.size(), area, mi->importance, size)) {
+        size[0] = S->cfg.default_width;
+        size[1] = S->cfg.default_height;
+    }
+    mi->w = size[0];
+    mi->h = size[1];
+    float fw = (float) mi->w, fh = (float) mi->h;
+    for (size_t i = 0; i < nv; ++i) {
+        mi->vtex[i] = me->tex1[i];
+        mi->ltex[i] = mk2(me->tex2[i].x * fw - 0.5f, me->tex2[i].y * fh - 0.5f);
+    }
+}
+
+// Gaussian taps (Generate_Gaussian_Kernel, lighter_math.cpp:357-365), on the
+// host so the weights are the reference's glibc values.
+std::vector<float> gauss_taps(int ext, float radius)
+{
+    std::vector<float> k(ext * 2 + 1);
+    float sum = 0.0f;
+    float mc = 1.0f / sqrtf(2.0f * 3.14159265358979323846f * radius * radius);
+    for (int i = -ext; i <= ext; ++i) sum += k[i + ext] = expf(-0.5f * powf((float) i / radius, 2.0f)) * mc;
+    for (int i = -ext; i <= ext; ++i) k[i + ext] /= sum;
+    return k;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------------- the bake
+
+void run_bake(ltr_Scene* S)
+{
+    const ltr_Config& cfg = S->cfg;
+    memset(&S->stats, 0, sizeof(S->stats));
+    S->rad_links = 0;
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw std::runtime_error("no CUDA device available");
+    if (S->opt.device >= ndev) throw std::runtime_error("ltrg_Options.device out of range");
+    CK(cudaSetDevice(S->opt.device));
+
+    Arena A;
+    CK(cudaStreamCreateWithFlags(&A.st, cudaStreamNonBlocking));
+    StageClock clock{A.st};
+    cudaStream_t st = A.st;
+
+    // ---- host: transform + lightmap sizing (Job_PreXForm)
+    S->stage = "transforming spatial data";
+    const int n_inst = (int) S->insts.size();
+    for (int i = 1; i < n_inst; ++i) prexform(S, S->insts[i]);
+    check_abort(S);
+
+    // ---- host: triangle soup of shadow parts (Job_ColInfo) + instance boxes
+    S->stage = "generating data structures";
+    std::vector<float> tri_xyz;
+    std::vector<u32> tri_meta, tri_local;
+    std::vector<float> inst_box(6 * n_inst);
+    float smin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, smax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int i = 0; i < n_inst; ++i) {
+        HostInst* mi = S->insts[i];
+        V3 bmn = splat(FLT_MAX), bmx = splat(-FLT_MAX);
+        u32 local = 0;
+        if (!mi->container) {
+            ltr_Mesh* me = mi->mesh;
+            for (const HostPart& p : me->parts) {
+                if (!p.shadow) continue;
+                const V3* vb = &mi->vpos[p.voff];
+                const u32* ib = &me->idx[p.ioff];
+                for (u32 t = 0; t < p.icount; t += 3) {
+                    V3 P1 = vb[ib[t]], P2 = vb[ib[t + 1]], P3 = vb[ib[t + 2]];
+                    if (near_zero(cross(P2 - P1, P3 - P1))) continue;   // Triangle::CheckIsUseful
+                    const V3 ps[3] = {P1, P2, P3};
+                    for (const V3& q : ps) {
+                        tri_xyz.push_back(q.x); tri_xyz.push_back(q.y); tri_xyz.push_back(q.z);
+                        bmn = vmin(bmn, q); bmx = vmax(bmx, q);
+                    }
+                    float cx = (P1.x + P2.x + P3.x) * (1.0f / 3.0f), cy = (P1.y + P2.y + P3.y) * (1.0f / 3.0f),
+                          cz = (P1.z + P2.z + P3.z) * (1.0f / 3.0f);
+                    smin[0] = fminf(smin[0], cx); smin[1] = fminf(smin[1], cy); smin[2] = fminf(smin[2], cz);
+                    smax[0] = fmaxf(smax[0], cx); smax[1] = fmaxf(smax[1], cy); smax[2] = fmaxf(smax[2], cz);
+                    tri_meta.push_back((u32) i | (mi->shadow ? kOccluderBit : 0u));
+                    tri_local.push_back(local++);
+                }
+            }
+        }
+        inst_box[6 * i + 0] = bmn.x; inst_box[6 * i + 1] = bmn.y; inst_box[6 * i + 2] = bmn.z;
+        inst_box[6 * i + 3] = bmx.x; inst_box[6 * i + 4] = bmx.y; inst_box[6 * i + 5] = bmx.z;
+    }
+    const int n_tris = (int) tri_meta.size();
+    S->stats.triangles = (uint64_t) n_tris;
+
+    // reference-shaped per-instance trees for the sample-offset pass
+    std::vector<int> inst_tri_off(n_inst + 1, 0);
+    for (int t = 0; t < n_tris; ++t) inst_tri_off[(tri_meta[t] & kInstMask) + 1]++;
+    for (int i = 0; i < n_inst; ++i) inst_tri_off[i + 1] += inst_tri_off[i];
+    std::vector<RefTree> rtrees(n_inst);
+    {
+        std::vector<std::thread> pool;
+        std::atomic<int> next(1);
+        int nth = std::max(1, std::min(8, (int) std::thread::hardware_concurrency()));
+        for (int t = 0; t < nth; ++t)
+            pool.emplace_back([&]() {
+                for (int i = next++; i < n_inst; i = next++)
+                    build_ref_tree(tri_xyz.data() + 9 * (size_t) inst_tri_off[i],
+                                   (size_t) (inst_tri_off[i + 1] - inst_tri_off[i]), rtrees[i]);
+            });
+        for (auto& th : pool) th.join();
+    }
+    std::vector<float4> ref_nodes;
+    std::vector<int> ref_items;
+    std::vector<int4> ref_inst(n_inst, make_int4(0, 0, 0, 0));
+    for (int i = 1; i < n_inst; ++i) {
+        const RefTree& rt_i = rtrees[i];
+        if (inst_tri_off[i + 1] == inst_tri_off[i]) continue;
+        ref_inst[i] = make_int4((int) (ref_nodes.size() / 2), (int) ref_items.size(), inst_tri_off[i],
+                                (int) rt_i.nodes.size());
+        for (const RefNode& nd : rt_i.nodes) {
+            float chf, idof;
+            memcpy(&chf, &nd.ch, 4);
+            memcpy(&idof, &nd.ido, 4);
+            ref_nodes.push_back(make_float4(nd.mn[0], nd.mn[1], nd.mn[2], nd.mx[0]));
+            ref_nodes.push_back(make_float4(nd.mx[1], nd.mx[2], chf, idof));
+        }
+        ref_items.insert(ref_items.end(), rt_i.items.begin(), rt_i.items.end());
+    }
+
+    // Light culling against instance boxes (ltr_Light::QueryMeshInsts,
+    // lighter.cpp:80-98, 1079-1093): point/spot lights reach instances whose
+    // box meets [pos - range, pos + range]; directional lights reach every
+    // instance with a box; the probe container (instance 0) is always lit.
+    const int n_lights = (int) S->lights.size();
+    std::vector<unsigned char> lit((size_t) n_lights * n_inst, 0);
+    std::vector<DLight> dl(n_lights);
+    for (int l = 0; l < n_lights; ++l) {
+        const HostLight& L = S->lights[l];
+        DLight& d = dl[l];
+        d.type = (int) L.type;
+        d.pos[0] = L.pos.x; d.pos[1] = L.pos.y; d.pos[2] = L.pos.z;
+        d.dir[0] = L.dir.x; d.dir[1] = L.dir.y; d.dir[2] = L.dir.z;
+        d.color[0] = L.color.x; d.color[1] = L.color.y; d.color[2] = L.color.z;
+        d.range = L.range; d.power = L.power; d.radius = L.radius; d.curve = L.curve;
+        d.out_rad = 0; d.diff = 0;
+        if (L.type == 2) {   // lighter.cpp:641-644
+            float out_rad = L.out / 180.0f * 3.14159265358979323846f, in_rad = L.in / 180.0f * 3.14159265358979323846f;
+            if (in_rad == out_rad) in_rad -= kSmall;
+            d.out_rad = out_rad;
+            d.diff = in_rad - out_rad;
+        }
+        lit[(size_t) l * n_inst + 0] = 1;
+        for (int i = 1; i < n_inst; ++i) {
+            const float* b = &inst_box[6 * i];
+            bool valid = b[0] <= b[3] && b[1] <= b[4] && b[2] <= b[5];
+            if (!valid) continue;
+            if (L.type == 1 || L.type == 2) {
+                V3 r3 = splat(L.range);
+                V3 qmn = L.pos - r3, qmx = L.pos + r3;
+                bool ov = !(qmn.x > b[3] || qmx.x < b[0] || qmn.y > b[4] || qmx.y < b[1] || qmn.z > b[5] || qmx.z < b[2]);
+                lit[(size_t) l * n_inst + i] = ov ? 1 : 0;
+            } else if (L.type == 3) {
+                lit[(size_t) l * n_inst + i] = 1;
+            }
+        }
+    }
+
+    // Raster records and per-pass bounding boxes (RasterizeInstance /
+    // RasterizeTriangle2D_x2_ex set-up, lighter.cpp:32-66, lighter_math.cpp:251-267).
+    std::vector<float> rt;
+    std::vector<u32> rinst;
+    std::vector<unsigned long long> tex_off(n_inst + 1, 0);
+    std::vector<u32> inst_w(n_inst, 0), inst_h(n_inst, 0);
+    unsigned long long ntex = 0;
+    for (int i = 0; i < n_inst; ++i) {
+        HostInst* mi = S->insts[i];
+        tex_off[i] = ntex;
+        if (mi->container) continue;
+        inst_w[i] = mi->w;
+        inst_h[i] = mi->h;
+        ntex += (unsigned long long) mi->w * mi->h;
+        ltr_Mesh* me = mi->mesh;
+        for (u32 part = 0; part < me->parts.size(); ++part) {
+            const HostPart& p = me->parts[part];
+            const u32* ib = &me->idx[p.ioff];
+            for (u32 t = 0; t + 2 < p.icount; t += 3) {
+                u32 i1 = p.voff + ib[t], i2 = p.voff + ib[t + 1], i3 = p.voff + ib[t + 2];
+                float lmarea = tri_area2(mi->ltex[i1], mi->ltex[i2], mi->ltex[i3]);
+                float coarea = tri_area3(mi->vpos[i1], mi->vpos[i2], mi->vpos[i3]);
+                float sa = lmarea > 0 ? coarea / lmarea : 0;
+                const u32 ids[3] = {i1, i2, i3};
+                for (u32 v : ids) { rt.push_back(mi->ltex[v].x); rt.push_back(mi->ltex[v].y); }
+                for (u32 v : ids) { rt.push_back(mi->vpos[v].x); rt.push_back(mi->vpos[v].y); rt.push_back(mi->vpos[v].z); }
+                for (u32 v : ids) { rt.push_back(mi->vnrm[v].x); rt.push_back(mi->vnrm[v].y); rt.push_back(mi->vnrm[v].z); }
+                for (u32 v : ids) { rt.push_back(mi->vtex[v].x); rt.push_back(mi->vtex[v].y); }
+                rt.push_back((float) part);
+                rt.push_back(sa);
+                rinst.push_back((u32) i);
+            }
+        }
+    }
+    tex_off[n_inst] = ntex;
+    const int n_rt = (int) rinst.size();
+    if (n_rt >= (1 << 30) - 1) throw std::runtime_error("too many triangles for the raster keys");
+    S->stats.texels = ntex;
+    std::vector<int4> bbox[2];
+    std::vector<unsigned long long> woff[2];
+    const float margins[2] = {0.5f + kSmall, 0.0f};
+    for (int pass = 0; pass < 2; ++pass) {
+        bbox[pass].resize(n_rt);
+        woff[pass].resize(n_rt + 1);
+        unsigned long long acc = 0;
+        for (int k = 0; k < n_rt; ++k) {
+            const float* r = &rt[(size_t) k * kRT];
+            u32 inst = rinst[k];
+            int w = (int) inst_w[inst], h = (int) inst_h[inst];
+            float mg = margins[pass];
+            int maxX = (int) (fmax_(r[0], fmax_(r[2], r[4])) + mg);
+            int minX = (int) (fmin_(r[0], fmin_(r[2], r[4])) - mg);
+            int maxY = (int) (fmax_(r[1], fmax_(r[3], r[5])) + mg);
+            int minY = (int) (fmin_(r[1], fmin_(r[3], r[5])) - mg);
+            bool empty = maxX < 0 || minX >= w || maxY < 0 || minY >= h;
+            if (minX < 0) minX = 0;
+            if (maxX >= w) maxX = w - 1;
+            if (minY < 0) minY = 0;
+            if (maxY >= h) maxY = h - 1;
+            V2 p1 = mk2(r[0], r[1]), p2 = mk2(r[2], r[3]), p3 = mk2(r[4], r[5]);
+            if (cross2(p2 - p1, p3 - p1) == 0) empty = true;
+            if (maxX < minX || maxY < minY) empty = true;
+            woff[pass][k] = acc;
+            if (empty) {
+                bbox[pass][k] = make_int4(0, 0, 1, 0);
+            } else {
+                bbox[pass][k] = make_int4(minX, minY, maxX - minX + 1, maxY - minY + 1);
+                acc += (unsigned long long) (maxX - minX + 1) * (unsigned long long) (maxY - minY + 1);
+            }
+        }
+        woff[pass][n_rt] = acc;
+    }
+
+    // ---- upload
+    cudaEvent_t e_up0 = clock.mark();
+    const u32 n_probe = (u32) S->samples.size();
+    float* d_tri_xyz = A.upload(tri_xyz);
+    u32* d_tri_meta = A.upload(tri_meta);
+    u32* d_tri_local = A.upload(tri_local);
+    float4* d_ref_nodes = A.upload(ref_nodes);
+    int* d_ref_items = A.upload(ref_items);
+    int4* d_ref_inst = A.upload(ref_inst);
+    unsigned char* d_lit = A.upload(lit);
+    DLight* d_lights = A.upload(dl);
+    float* d_rt = A.upload(rt);
+    u32* d_rinst = A.upload(rinst);
+    unsigned long long* d_tex_off = A.upload(tex_off);
+    u32* d_inst_w = A.upload(inst_w);
+    u32* d_inst_h = A.upload(inst_h);
+    int4* d_bbox[2];
+    unsigned long long* d_woff[2];
+    for (int p = 0; p < 2; ++p) { d_bbox[p] = A.upload(bbox[p]); d_woff[p] = A.upload(woff[p]); }
+    // one error word per stage kernel: 0 fixup, 1 direct, 2 radiosity, 3 AO
+    u32* d_err = A.zeros<u32>(8);
+    Counters* d_cnt = A.zeros<Counters>(1);
+    ErrFlag err_fix{d_err + 0}, err_direct{d_err + 1}, err_rad{d_err + 2}, err_ao{d_err + 3};
+    cudaEvent_t e_up1 = clock.mark();
+    check_abort(S);
+
+    // ---- BVH
+    BvhStorage bvh;
+    BvhBuildInput bin;
+    bin.tri_xyz = d_tri_xyz;
+    bin.tri_meta = d_tri_meta;
+    bin.tri_local = d_tri_local;
+    bin.n = n_tris;
+    for (int c = 0; c < 3; ++c) { bin.scene_min[c] = n_tris ? smin[c] : 0; bin.scene_max[c] = n_tris ? smax[c] : 0; }
+    bvh_build(bin, bvh, st);
+    struct BvhGuard { BvhStorage* b; cudaStream_t s; ~BvhGuard() { bvh_free(*b, s); } } bvh_guard{&bvh, st};
+    BvhView bv = bvh.view();
+    cudaEvent_t e_bvh = clock.mark();
+    // LTRG_VALIDATE=1: re-check the BVH topology after every stage
+    const bool validate = getenv("LTRG_VALIDATE") && getenv("LTRG_VALIDATE")[0] == '1';
+    auto checkpoint = [&](const char* where) {
+        if (!validate) return;
+        CK(cudaStreamSynchronize(st));
+        std::string e = bvh_validate(bvh, st);
+        if (!e.empty()) throw std::runtime_error(std::string("BVH corrupted after ") + where + ": " + e);
+    };
+    checkpoint("build");
+
+    // ---- samples (Job_Samples)
+    S->stage = "generating samples";
+    u32* d_keys = A.zeros<u32>(ntex);
+    for (int pass = 0; pass < 2; ++pass) {
+        unsigned long long nw = woff[pass][n_rt];
+        if (nw == 0) continue;
+        k_raster_mark<<<blocks_for(nw), kThreads, 0, st>>>(pass, margins[pass], d_rt, d_rinst, d_bbox[pass],
+                                                           d_woff[pass], n_rt, nw, d_tex_off, d_inst_w, d_keys);
+        CK(cudaGetLastError());
+        checkpoint("raster mark");
+    }
+    float4* d_R1 = A.alloc<float4>(ntex);
+    float4* d_R2 = A.alloc<float4>(ntex);
+    float4* d_R3 = A.alloc<float4>(ntex);
+    u32* d_flags = A.alloc<u32>(ntex + 1);
+    u32* d_scan = A.alloc<u32>(ntex + 1);
+    CK(cudaMemsetAsync(d_flags + ntex, 0, sizeof(u32), st));
+    if (ntex) {
+        k_raster_resolve<<<blocks_for(ntex), kThreads, 0, st>>>(ntex, d_keys, d_rt, d_rinst, d_tex_off, d_inst_w,
+                                                                d_R1, d_R2, d_R3, d_flags);
+        CK(cudaGetLastError());
+        checkpoint("raster resolve");
+    }
+    {
+        size_t tb = 0;
+        CK(cub::DeviceScan::ExclusiveSum(nullptr, tb, d_flags, d_scan, (int64_t) (ntex + 1), st));
+        void* tmp = A.alloc<char>(tb);
+        CK(cub::DeviceScan::ExclusiveSum(tmp, tb, d_flags, d_scan, (int64_t) (ntex + 1), st));
+    }
+    // per-instance sample starts = scan at each instance's first texel
+    std::vector<u32> inst_sbeg(n_inst + 1, 0);
+    for (int i = 1; i <= n_inst; ++i)
+        CK(cudaMemcpyAsync(&inst_sbeg[i], d_scan + tex_off[i == n_inst ? n_inst : i], sizeof(u32),
+                           cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const u32 n_cov = inst_sbeg[n_inst];
+    const u32 n_samples = n_probe + n_cov;
+    S->stats.samples = n_samples;
+    // sample ranges: instance 0 = probes [0, n_probe); instance i = n_probe + [scan(tex_off[i]), scan(tex_off[i+1]))
+    std::vector<u32> sbeg(n_inst + 1), scount(n_inst);
+    sbeg[0] = 0;
+    scount[0] = n_probe;
+    for (int i = 1; i < n_inst; ++i) {
+        u32 b = n_probe + inst_sbeg[i];
+        u32 e = n_probe + (i + 1 < n_inst ? inst_sbeg[i + 1] : n_cov);
+        sbeg[i] = b;
+        scount[i] = e - b;
+    }
+
+    float4* d_spos = A.alloc<float4>(n_samples);
+    float4* d_snrm = A.alloc<float4>(n_samples);
+    float4* d_srad = A.zeros<float4>(n_samples);
+    u32* d_sloc = A.alloc<u32>(n_samples);
+    u32* d_sinst = A.alloc<u32>(n_samples);
+    if (n_probe) {
+        std::vector<float4> pp(n_probe), pn(n_probe);
+        std::vector<u32> pl(n_probe, kNoLoc), pi(n_probe, 0);
+        for (u32 i = 0; i < n_probe; ++i) {
+            const ltr_SampleInfo& si = S->samples[i];
+            pp[i] = make_float4(si.position[0], si.position[1], si.position[2], 0);
+            pn[i] = make_float4(si.normal[0], si.normal[1], si.normal[2], 0);
+        }
+        CK(cudaMemcpyAsync(d_spos, pp.data(), n_probe * sizeof(float4), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(d_snrm, pn.data(), n_probe * sizeof(float4), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(d_sloc, pl.data(), n_probe * sizeof(u32), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(d_sinst, pi.data(), n_probe * sizeof(u32), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    if (ntex) {
+        k_compact<<<blocks_for(ntex), kThreads, 0, st>>>(ntex, d_flags, d_scan, d_R1, d_R2, d_R3, d_tex_off, n_inst,
+                                                         n_probe, d_spos, d_snrm, d_srad, d_sloc, d_sinst);
+        CK(cudaGetLastError());
+        checkpoint("compaction");
+    }
+    if (n_cov) {
+        FixupArgs fa;
+        fa.bvh = bv;
+        fa.err = err_fix;
+        fa.ref_nodes = d_ref_nodes;
+        fa.ref_items = d_ref_items;
+        fa.ref_inst = d_ref_inst;
+        fa.tri_xyz = d_tri_xyz;
+        fa.n_inst = n_inst;
+        fa.n_probe = n_probe;
+        fa.n_samples = n_samples;
+        fa.max_correct_dist = cfg.max_correct_dist;
+        fa.corr_min_dot = cosf(cfg.max_correct_angle / 180.0f * 3.14159265358979323846f);
+        fa.spos = d_spos;
+        fa.snrm = d_snrm;
+        fa.srad = d_srad;
+        k_fixup<<<(n_cov + 127) / 128, 128, 0, st>>>(fa);
+        CK(cudaGetLastError());
+        checkpoint("sample fixup");
+    }
+    cudaEvent_t e_samples = clock.mark();
+    check_abort(S);
+
+    // ---- direct light (Int_LMRender per light)
+    float4* d_lm = A.alloc<float4>(n_samples);
+    float* d_kval = nullptr;
+    float4* d_ndir = nullptr;
+    S->stage = "rendering lightmaps";
+    const bool want_normals = cfg.generate_normalmap_data != 0;
+    if (n_lights && n_samples) {
+        d_kval = A.alloc<float>((size_t) n_lights * n_samples);
+        if (want_normals) d_ndir = A.alloc<float4>((size_t) n_lights * n_samples);
+        DirectArgs da;
+        da.bvh = bv;
+        da.err = err_direct;
+        da.lights = d_lights;
+        da.n_lights = n_lights;
+        da.n_inst = n_inst;
+        da.lit = d_lit;
+        da.n_samples = n_samples;
+        da.spos = d_spos;
+        da.snrm = d_snrm;
+        da.sinst = d_sinst;
+        da.kval = d_kval;
+        da.ndir = d_ndir;
+        da.counters = d_cnt;
+        unsigned long long items = (unsigned long long) n_lights * n_samples;
+        k_direct<<<blocks_for(items, 128, 152ull * 256), 128, 0, st>>>(da);
+        CK(cudaGetLastError());
+    }
+    if (n_samples) {
+        k_accumulate<<<(n_samples + kThreads - 1) / kThreads, kThreads, 0, st>>>(
+            n_samples, n_lights, d_lights, d_kval, cfg.ambient_color[0], cfg.ambient_color[1], cfg.ambient_color[2], d_lm);
+        CK(cudaGetLastError());
+    }
+    cudaEvent_t e_direct = clock.mark();
+    check_abort(S);
+
+    // ---- radiosity (Int_RDGenLinks + Int_RDBounce)
+    cudaEvent_t e_rad_links = e_direct, e_rad_bounce = e_direct;
+    if (cfg.bounce_count && n_samples) {
+        S->stage = "calculating radiosity";
+        // host side of the sample gathering: sample_fn per sample, in order
+        std::vector<float4> hpos(n_samples), hnrm(n_samples), hrad(n_samples), hlm(n_samples);
+        std::vector<u32> hloc(n_samples);
+        CK(cudaMemcpyAsync(hpos.data(), d_spos, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hnrm.data(), d_snrm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hrad.data(), d_srad, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hlm.data(), d_lm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hloc.data(), d_sloc, n_samples * sizeof(u32), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        RadInputs ri;
+        ri.n = n_samples;
+        ri.pos.resize(n_samples);
+        ri.nrm.resize(n_samples);
+        ri.diff_area.resize(n_samples);
+        ri.emit.resize(n_samples);
+        for (int i = 0; i < n_inst; ++i) {
+            HostInst* mi = S->insts[i];
+            for (u32 k = 0; k < scount[i]; ++k) {
+                u32 s = sbeg[i] + k;
+                V3 P = mk(hpos[s].x, hpos[s].y, hpos[s].z);
+                V3 N = normalized(mk(hnrm[s].x, hnrm[s].y, hnrm[s].z));
+                V3 diff = mk(1, 1, 1);
+                V3 emit = mk(hlm[s].x, hlm[s].y, hlm[s].z);
+                float area = mi->container ? 0 : hrad[s].w;
+                if (mi->container) {
+                    diff = mk(0, 0, 0);
+                } else if (cfg.sample_fn) {   // lighter.cpp:692-714
+                    u32 L = hloc[s];
+                    int lx = (int) (L % mi->w), ly = (int) (L / mi->w);
+                    ltr_SampleRequest req;
+                    req.position[0] = P.x; req.position[1] = P.y; req.position[2] = P.z;
+                    req.normal[0] = N.x; req.normal[1] = N.y; req.normal[2] = N.z;
+                    req.tex0u = hrad[s].x; req.tex0v = hrad[s].y;
+                    req.tex1u = (lx + 0.5f) / mi->w; req.tex1v = (ly + 0.5f) / mi->h;
+                    req.part_id = (uint32_t) hrad[s].z;
+                    req.mesh_ident = mi->mesh->ident.c_str(); req.mesh_ident_size = mi->mesh->ident.size();
+                    req.inst_ident = mi->ident.c_str(); req.inst_ident_size = mi->ident.size();
+                    req.out_diffuse_color[0] = req.out_diffuse_color[1] = req.out_diffuse_color[2] = 1;
+                    req.out_emissive_color[0] = req.out_emissive_color[1] = req.out_emissive_color[2] = 0;
+                    if (cfg.sample_fn(const_cast<ltr_Config*>(&cfg), &req)) {
+                        diff = mk(req.out_diffuse_color[0], req.out_diffuse_color[1], req.out_diffuse_color[2]);
+                        emit += mk(req.out_emissive_color[0], req.out_emissive_color[1], req.out_emissive_color[2]);
+                    }
+                }
+                ri.pos[s] = make_float4(P.x, P.y, P.z, 0);
+                ri.nrm[s] = make_float4(N.x, N.y, N.z, 0);
+                ri.diff_area[s] = make_float4(diff.x, diff.y, diff.z, area);
+                ri.emit[s] = make_float4(emit.x, emit.y, emit.z, 0);
+            }
+        }
+        RadSettings rs;
+        rs.links = S->opt.radiosity_links;
+        rs.precision = S->opt.radiosity_precision;
+        rs.refine_steps = S->opt.refine_steps;
+        rs.bounces = cfg.bounce_count;
+        RadResult rr = radiosity_solve(ri, rs, bv, err_rad, st, d_lm, &S->abort_flag);
+        S->rad_links = (u32) rr.links;
+        S->stats.rad_pairs = rr.pairs;
+        S->stats.rad_vis_rays = rr.vis_rays;
+        S->stats.ms_rad_links = rr.ms_links;
+        S->stats.ms_rad_bounce = rr.ms_bounce;
+        S->stage = "committing radiosity";
+        e_rad_links = e_rad_bounce = clock.mark();
+    }
+    check_abort(S);
+
+    // ---- ambient occlusion (Job_AORender)
+    cudaEvent_t e_ao0 = clock.mark();
+    if (cfg.ao_distance && n_samples) {
+        S->stage = "rendering ambient occlusion";
+        std::vector<float> ro(n_samples);
+        for (u32 s = 0; s < n_samples; ++s) ro[s] = randf_host();   // instance order, sample order
+        float* d_ro = A.upload(ro);
+        AoArgs aa;
+        aa.bvh = bv;
+        aa.err = err_ao;
+        aa.n_samples = n_samples;
+        aa.spos = d_spos;
+        aa.snrm = d_snrm;
+        aa.randoff = d_ro;
+        aa.lm = d_lm;
+        aa.dist = cfg.ao_distance;
+        aa.falloff = cfg.ao_falloff;
+        aa.mult = cfg.ao_multiplier;
+        aa.effect = cfg.ao_effect;
+        aa.ns = cfg.ao_num_samples;
+        for (int c = 0; c < 3; ++c) aa.aoc[c] = cfg.ao_color_rgb[c];
+        aa.counters = d_cnt;
+        if (aa.ns > 0) {
+            k_ao<<<blocks_for((size_t) n_samples * 32, 256, 152ull * 64), 256, 0, st>>>(aa);
+            CK(cudaGetLastError());
+        }
+    }
+    cudaEvent_t e_ao1 = clock.mark();
+    check_abort(S);
+
+    // ---- finalize (Int_Finalize)
+    S->stage = "exporting lightmaps";
+    float* d_img = A.zeros<float>(3 * ntex);
+    unsigned char* d_maskA = A.zeros<unsigned char>(ntex);
+    unsigned char* d_maskB = A.alloc<unsigned char>(ntex);
+    if (n_cov) {
+        k_scatter<<<(n_cov + kThreads - 1) / kThreads, kThreads, 0, st>>>(n_probe, n_samples, d_sloc, d_sinst, d_lm,
+                                                                          d_tex_off, d_img, d_maskA);
+        CK(cudaGetLastError());
+    }
+    if (ntex) {
+        for (int it = 0; it < 3; ++it) {
+            CK(cudaMemcpyAsync(d_maskB, d_maskA, ntex, cudaMemcpyDeviceToDevice, st));
+            k_dilate<<<blocks_for(ntex), kThreads, 0, st>>>(ntex, n_inst, d_tex_off, d_inst_w, d_inst_h, d_maskA,
+                                                            d_maskB, d_img);
+            CK(cudaGetLastError());
+            std::swap(d_maskA, d_maskB);
+        }
+    }
+    if (cfg.blur_size && ntex) {
+        int ext = (int) ceilf(cfg.blur_size);
+        std::vector<float> taps = gauss_taps(ext, cfg.blur_size);
+        float* d_taps = A.upload(taps);
+        float* d_tmp = A.alloc<float>(3 * ntex);
+        k_conv_t<<<blocks_for(ntex), kThreads, 0, st>>>(ntex, n_inst, d_tex_off, d_inst_w, d_inst_h, 0, ext, d_taps,
+                                                        d_img, d_tmp);
+        CK(cudaGetLastError());
+        k_conv_t<<<blocks_for(ntex), kThreads, 0, st>>>(ntex, n_inst, d_tex_off, d_inst_w, d_inst_h, 1, ext, d_taps,
+                                                        d_tmp, d_img);
+        CK(cudaGetLastError());
+    }
+    // output layout (after optional ds2x)
+    std::vector<unsigned long long> out_off(n_inst + 1, 0);
+    std::vector<u32> out_w(n_inst, 0), out_h(n_inst, 0);
+    unsigned long long nout = 0;
+    for (int i = 0; i < n_inst; ++i) {
+        out_off[i] = nout;
+        if (S->insts[i]->container) continue;
+        u32 w = inst_w[i], h = inst_h[i];
+        if (cfg.ds2x) { w = std::max(w / 2, 1u); h = std::max(h / 2, 1u); }
+        out_w[i] = w;
+        out_h[i] = h;
+        nout += (unsigned long long) w * h;
+    }
+    out_off[n_inst] = nout;
+    float* d_out = d_img;
+    if (cfg.ds2x && nout) {
+        unsigned long long* d_out_off = A.upload(out_off);
+        d_out = A.alloc<float>(3 * nout);
+        k_ds2x<<<blocks_for(nout), kThreads, 0, st>>>(nout, n_inst, d_out_off, d_tex_off, d_inst_w, d_inst_h, d_img, d_out);
+        CK(cudaGetLastError());
+    }
+    float* d_nimg = nullptr;
+    if (want_normals && nout) {
+        std::vector<u32> cap(n_inst);
+        for (int i = 0; i < n_inst; ++i) cap[i] = out_w[i] * out_h[i];
+        unsigned long long* d_nout_off = A.upload(out_off);
+        u32* d_cap = A.upload(cap);
+        d_nimg = A.zeros<float>(4 * nout);
+        float amb = brightness(mk(cfg.ambient_color[0], cfg.ambient_color[1], cfg.ambient_color[2]));
+        if (n_cov && d_ndir) {
+            k_normals<<<(n_cov + kThreads - 1) / kThreads, kThreads, 0, st>>>(n_probe, n_samples, n_lights, d_ndir, d_snrm,
+                                                                              d_sloc, d_sinst, d_nout_off, d_cap, amb, d_nimg);
+            CK(cudaGetLastError());
+        } else if (n_cov) {
+            float4* d_zero = A.zeros<float4>(1);
+            k_normals<<<(n_cov + kThreads - 1) / kThreads, kThreads, 0, st>>>(n_probe, n_samples, 0, d_zero, d_snrm,
+                                                                              d_sloc, d_sinst, d_nout_off, d_cap, amb, d_nimg);
+            CK(cudaGetLastError());
+        }
+    }
+    cudaEvent_t e_fin = clock.mark();
+
+    // ---- readback
+    u32 err_words[8] = {0};
+    Counters cnt;
+    CK(cudaMemcpyAsync(err_words, d_err, sizeof(err_words), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&cnt, d_cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    std::vector<float> himg(3 * nout), hnimg(d_nimg ? 4 * nout : 0);
+    if (nout) CK(cudaMemcpyAsync(himg.data(), d_out, himg.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (d_nimg) CK(cudaMemcpyAsync(hnimg.data(), d_nimg, hnimg.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+    std::vector<float4> probe_lm(n_probe);
+    if (n_probe) CK(cudaMemcpyAsync(probe_lm.data(), d_lm, n_probe * sizeof(float4), cudaMemcpyDeviceToHost, st));
+    std::vector<float4> dpos, dnrm, drad, dlm;
+    std::vector<u32> dloc;
+    if (S->opt.keep_samples && n_samples) {
+        dpos.resize(n_samples); dnrm.resize(n_samples); drad.resize(n_samples); dlm.resize(n_samples); dloc.resize(n_samples);
+        CK(cudaMemcpyAsync(dpos.data(), d_spos, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(dnrm.data(), d_snrm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(drad.data(), d_srad, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(dlm.data(), d_lm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(dloc.data(), d_sloc, n_samples * sizeof(u32), cudaMemcpyDeviceToHost, st));
+    }
+    cudaEvent_t e_down = clock.mark();
+    CK(cudaStreamSynchronize(st));
+    static const char* kStageName[4] = {"sample fixup", "direct light", "radiosity", "ambient occlusion"};
+    for (int k = 0; k < 4; ++k) {
+        if (!err_words[k]) continue;
+        char msg[160];
+        snprintf(msg, sizeof(msg), "%s kernel reported error word 0x%08x (bit 0: traversal stack overflow)", kStageName[k], err_words[k]);
+        throw std::runtime_error(msg);
+    }
+
+    // ---- outputs (scene-owned, lighter.cpp:1029-1042)
+    for (u32 i = 0; i < n_probe; ++i) {
+        S->samples[i].out_color[0] = probe_lm[i].x;
+        S->samples[i].out_color[1] = probe_lm[i].y;
+        S->samples[i].out_color[2] = probe_lm[i].z;
+    }
+    for (int i = 0; i < n_inst; ++i) {
+        HostInst* mi = S->insts[i];
+        if (mi->container) continue;
+        size_t n = (size_t) out_w[i] * out_h[i];
+        float* img = new float[n * 3];
+        memcpy(img, himg.data() + 3 * out_off[i], n * 3 * sizeof(float));
+        float* nimg = nullptr;
+        if (d_nimg) {
+            nimg = new float[n * 4];
+            memcpy(nimg, hnimg.data() + 4 * out_off[i], n * 4 * sizeof(float));
+        }
+        if (cfg.ds2x) { mi->w = out_w[i]; mi->h = out_h[i]; }
+        ltr_WorkOutput wo = {(u32) i, mi->mesh->ident.c_str(), mi->mesh->ident.size(), mi->ident.c_str(),
+                             mi->ident.size(), img, nimg, out_w[i], out_h[i]};
+        S->outputs.push_back(wo);
+    }
+    if (S->opt.keep_samples) {
+        S->dump.assign(n_inst, SampleDump());
+        for (int i = 0; i < n_inst && n_samples; ++i) {
+            SampleDump& d = S->dump[i];
+            for (u32 k = 0; k < scount[i]; ++k) {
+                u32 s = sbeg[i] + k;
+                d.pos.insert(d.pos.end(), {dpos[s].x, dpos[s].y, dpos[s].z});
+                d.nrm.insert(d.nrm.end(), {dnrm[s].x, dnrm[s].y, dnrm[s].z});
+                d.radinfo.insert(d.radinfo.end(), {drad[s].x, drad[s].y, drad[s].z, drad[s].w});
+                d.color.insert(d.color.end(), {dlm[s].x, dlm[s].y, dlm[s].z});
+                d.loc.push_back(dloc[s]);
+            }
+        }
+    }
+
+    S->stats.ms_upload = StageClock::ms(e_up0, e_up1);
+    S->stats.ms_bvh = StageClock::ms(e_up1, e_bvh);
+    S->stats.ms_samples = StageClock::ms(e_bvh, e_samples);
+    S->stats.ms_direct = StageClock::ms(e_samples, e_direct);
+    S->stats.ms_ao = StageClock::ms(e_ao0, e_ao1);
+    S->stats.ms_finalize = StageClock::ms(e_ao1, e_fin);
+    S->stats.ms_download = StageClock::ms(e_fin, e_down);
+    S->stats.shadow_evals = cnt.shadow_evals;
+    S->stats.distance_queries = cnt.distance_queries;
+    S->stats.ao_rays = cnt.ao_rays;
+    S->stats.node_visits = cnt.node_visits;
+    (void) e_rad_links;
+    (void) e_rad_bounce;
+}
+
+}  // namespace lg

@@ -1,0 +1,280 @@
+// GPU build of the flat scene BVH (layout in bvh.cuh).
+//
+// Replaces the reference's per-instance top-down AABBTree build
+// (AABBTree::SetAABBs/_MakeNode, lighter_math.cpp:674-781) and its instance
+// tree (lighter.cpp:1060-1069) with one linear BVH over all world-space
+// shadow-casting triangles, built in five passes on the GPU:
+//   1. 30-bit Morton code of each triangle centroid inside the scene bounds;
+//   2. radix sort of (code, triangle) pairs;
+//   3. Karras' (HPG 2012) top-down-by-prefix hierarchy, one thread per
+//      internal node, ties between equal codes broken by index;
+//   4. bottom-up box refit, one thread per leaf, second arrival at a node
+//      computes its box (atomic arrival counters);
+//   5. packing into 64-byte nodes that hold both child boxes, and
+//      triangles reordered into leaf order.
+#include <cuda_runtime.h>
+#include <cub/cub.cuh>
+
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "bvh.cuh"
+
+namespace lg {
+namespace {
+
+#define BVH_CHECK(x)                                                                                  \
+    do {                                                                                              \
+        cudaError_t e_ = (x);                                                                         \
+        if (e_ != cudaSuccess) throw std::runtime_error(std::string("bvh: ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+__device__ __forceinline__ u32 spread10(u32 v)
+{
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+__global__ void k_morton(const float* xyz, int n, float3 mn, float3 inv_ext, u32* codes, u32* ids)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* p = xyz + 9 * (size_t) i;
+    float cx = (p[0] + p[3] + p[6]) * (1.0f / 3.0f);
+    float cy = (p[1] + p[4] + p[7]) * (1.0f / 3.0f);
+    float cz = (p[2] + p[5] + p[8]) * (1.0f / 3.0f);
+    float qx = fminf(fmaxf((cx - mn.x) * inv_ext.x * 1024.0f, 0.0f), 1023.0f);
+    float qy = fminf(fmaxf((cy - mn.y) * inv_ext.y * 1024.0f, 0.0f), 1023.0f);
+    float qz = fminf(fmaxf((cz - mn.z) * inv_ext.z * 1024.0f, 0.0f), 1023.0f);
+    codes[i] = (spread10((u32) qx) << 2) | (spread10((u32) qy) << 1) | spread10((u32) qz);
+    ids[i] = (u32) i;
+}
+
+__device__ __forceinline__ int prefix(const u32* codes, int n, int i, int j)
+{
+    if (j < 0 || j >= n) return -1;
+    u32 a = codes[i], b = codes[j];
+    if (a == b) return 32 + __clz((u32) i ^ (u32) j);
+    return __clz(a ^ b);
+}
+
+__global__ void k_hierarchy(const u32* codes, int n, int* left, int* right, int* parent_int, int* parent_leaf)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int d = (prefix(codes, n, i, i + 1) - prefix(codes, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = prefix(codes, n, i, i - d);
+    int lmax = 2;
+    while (prefix(codes, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (prefix(codes, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = prefix(codes, n, i, j);
+    int s = 0;
+    for (int div = 2;; div <<= 1) {
+        int t = (l + div - 1) / div;
+        if (prefix(codes, n, i, i + (s + t) * d) > dnode) s += t;
+        if (t <= 1) break;
+    }
+    int gamma = i + s * d + min(d, 0);
+    int lc = (min(i, j) == gamma) ? ~gamma : gamma;
+    int rc = (max(i, j) == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+    left[i] = lc;
+    right[i] = rc;
+    if (lc < 0) parent_leaf[~lc] = i; else parent_int[lc] = i;
+    if (rc < 0) parent_leaf[~rc] = i; else parent_int[rc] = i;
+}
+
+// Conservative box of a triangle: a few tens of ulps of slack absorb the
+// rounding of the exact hit and distance tests.
+__device__ __forceinline__ void tri_box(const float* p, float* b)
+{
+    float mnx = fminf(p[0], fminf(p[3], p[6])), mny = fminf(p[1], fminf(p[4], p[7])), mnz = fminf(p[2], fminf(p[5], p[8]));
+    float mxx = fmaxf(p[0], fmaxf(p[3], p[6])), mxy = fmaxf(p[1], fmaxf(p[4], p[7])), mxz = fmaxf(p[2], fmaxf(p[5], p[8]));
+    float m = fmaxf(fmaxf(fmaxf(fabsf(mnx), fabsf(mxx)), fmaxf(fabsf(mny), fabsf(mxy))), fmaxf(fabsf(mnz), fabsf(mxz)));
+    float e = m * 2e-5f + 1e-6f;
+    b[0] = mnx - e; b[1] = mny - e; b[2] = mnz - e;
+    b[3] = mxx + e; b[4] = mxy + e; b[5] = mxz + e;
+}
+
+__device__ __forceinline__ void read_box(const float* boxes, int k, float* b)
+{
+    for (int c = 0; c < 6; ++c) b[c] = __ldcg(boxes + 6 * (size_t) k + c);
+}
+
+__global__ void k_refit(const float* xyz, const u32* ids, int n, const int* parent_leaf, const int* parent_int,
+                        const int* left, const int* right, float* leaf_box, float* int_box, u32* arrivals)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float b[6];
+    tri_box(xyz + 9 * (size_t) ids[i], b);
+    for (int c = 0; c < 6; ++c) leaf_box[6 * (size_t) i + c] = b[c];
+    __threadfence();
+    int p = n > 1 ? parent_leaf[i] : -1;
+    while (p >= 0) {
+        if (atomicAdd(&arrivals[p], 1u) == 0u) return;
+        __threadfence();
+        float bl[6], br[6];
+        int l = left[p], r = right[p];
+        if (l < 0) read_box(leaf_box, ~l, bl); else read_box(int_box, l, bl);
+        if (r < 0) read_box(leaf_box, ~r, br); else read_box(int_box, r, br);
+        for (int c = 0; c < 3; ++c) {
+            int_box[6 * (size_t) p + c] = fminf(bl[c], br[c]);
+            int_box[6 * (size_t) p + 3 + c] = fmaxf(bl[3 + c], br[3 + c]);
+        }
+        __threadfence();
+        p = parent_int[p];
+    }
+}
+
+__global__ void k_pack_nodes(int n_int, const int* left, const int* right, const float* leaf_box, const float* int_box,
+                             float4* nodes)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_int) return;
+    int l = left[i], r = right[i];
+    const float* L = l < 0 ? leaf_box + 6 * (size_t) (~l) : int_box + 6 * (size_t) l;
+    const float* R = r < 0 ? leaf_box + 6 * (size_t) (~r) : int_box + 6 * (size_t) r;
+    float4* o = nodes + 4 * (size_t) i;
+    o[0] = make_float4(L[0], L[1], L[2], L[3]);
+    o[1] = make_float4(L[4], L[5], R[0], R[1]);
+    o[2] = make_float4(R[2], R[3], R[4], R[5]);
+    o[3] = make_float4(__int_as_float(l), __int_as_float(r), 0.0f, 0.0f);
+}
+
+__global__ void k_pack_tris(int n, const u32* ids, const float* xyz, const u32* meta, const u32* local, float4* tris)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    u32 s = ids[i];
+    const float* p = xyz + 9 * (size_t) s;
+    tris[3 * (size_t) i + 0] = make_float4(p[0], p[1], p[2], __uint_as_float(meta[s]));
+    tris[3 * (size_t) i + 1] = make_float4(p[3], p[4], p[5], __uint_as_float(local[s]));
+    tris[3 * (size_t) i + 2] = make_float4(p[6], p[7], p[8], __uint_as_float(s));
+}
+
+template <class T>
+T* alloc(size_t count, cudaStream_t st, size_t& bytes)
+{
+    void* p = nullptr;
+    if (count == 0) count = 1;
+    BVH_CHECK(cudaMallocAsync(&p, count * sizeof(T), st));
+    bytes += count * sizeof(T);
+    return (T*) p;
+}
+
+}  // namespace
+
+void bvh_build(const BvhBuildInput& in, BvhStorage& out, void* stream)
+{
+    cudaStream_t st = (cudaStream_t) stream;
+    const int n = in.n;
+    out.n_tris = n;
+    out.bytes = 0;
+    if (n <= 0) { out.root = 0; return; }
+    const int n_int = n > 1 ? n - 1 : 0;
+    out.root = n > 1 ? 0 : ~0;
+
+    size_t scratch_bytes = 0;
+    u32* codes = alloc<u32>(n, st, scratch_bytes);
+    u32* codes2 = alloc<u32>(n, st, scratch_bytes);
+    u32* ids = alloc<u32>(n, st, scratch_bytes);
+    u32* ids2 = alloc<u32>(n, st, scratch_bytes);
+    int* left = alloc<int>(n_int, st, scratch_bytes);
+    int* right = alloc<int>(n_int, st, scratch_bytes);
+    int* parent_int = alloc<int>(n_int, st, scratch_bytes);
+    int* parent_leaf = alloc<int>(n, st, scratch_bytes);
+    float* leaf_box = alloc<float>(6 * (size_t) n, st, scratch_bytes);
+    float* int_box = alloc<float>(6 * (size_t) n_int, st, scratch_bytes);
+    u32* arrivals = alloc<u32>(n_int, st, scratch_bytes);
+
+    const int B = 256;
+    float3 mn = make_float3(in.scene_min[0], in.scene_min[1], in.scene_min[2]);
+    float ex = in.scene_max[0] - in.scene_min[0], ey = in.scene_max[1] - in.scene_min[1], ez = in.scene_max[2] - in.scene_min[2];
+    float3 inv_ext = make_float3(ex > 0 ? 1.0f / ex : 0.0f, ey > 0 ? 1.0f / ey : 0.0f, ez > 0 ? 1.0f / ez : 0.0f);
+    k_morton<<<(n + B - 1) / B, B, 0, st>>>(in.tri_xyz, n, mn, inv_ext, codes, ids);
+    BVH_CHECK(cudaGetLastError());
+
+    size_t temp_bytes = 0;
+    BVH_CHECK(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, codes, codes2, ids, ids2, n, 0, 30, st));
+    void* temp = alloc<char>(temp_bytes, st, scratch_bytes);
+    BVH_CHECK(cub::DeviceRadixSort::SortPairs(temp, temp_bytes, codes, codes2, ids, ids2, n, 0, 30, st));
+
+    if (n_int > 0) {
+        BVH_CHECK(cudaMemsetAsync(parent_int, 0xff, sizeof(int) * n_int, st));
+        BVH_CHECK(cudaMemsetAsync(arrivals, 0, sizeof(u32) * n_int, st));
+        k_hierarchy<<<(n_int + B - 1) / B, B, 0, st>>>(codes2, n, left, right, parent_int, parent_leaf);
+        BVH_CHECK(cudaGetLastError());
+    }
+    k_refit<<<(n + B - 1) / B, B, 0, st>>>(in.tri_xyz, ids2, n, parent_leaf, parent_int, left, right, leaf_box, int_box,
+                                            arrivals);
+    BVH_CHECK(cudaGetLastError());
+
+    out.nodes = alloc<float4>(4 * (size_t) (n_int > 0 ? n_int : 1), st, out.bytes);
+    out.tris = alloc<float4>(3 * (size_t) n, st, out.bytes);
+    if (n_int > 0) {
+        k_pack_nodes<<<(n_int + B - 1) / B, B, 0, st>>>(n_int, left, right, leaf_box, int_box, out.nodes);
+        BVH_CHECK(cudaGetLastError());
+    }
+    k_pack_tris<<<(n + B - 1) / B, B, 0, st>>>(n, ids2, in.tri_xyz, in.tri_meta, in.tri_local, out.tris);
+    BVH_CHECK(cudaGetLastError());
+
+    void* ptrs[] = {codes, codes2, ids, ids2, left, right, parent_int, parent_leaf, leaf_box, int_box, arrivals, temp};
+    for (void* p : ptrs) BVH_CHECK(cudaFreeAsync(p, st));
+}
+
+// Copies the topology back and checks that a walk from the root reaches every
+// internal node and every leaf exactly once; returns an empty string when the
+// tree is sound. Used by the LTRG_VALIDATE=1 debug mode of the bake.
+std::string bvh_validate(const BvhStorage& s, void* stream)
+{
+    if (s.n_tris <= 1) return "";
+    const int n = s.n_tris, n_int = n - 1;
+    std::vector<float4> nodes(4 * (size_t) n_int);
+    BVH_CHECK(cudaMemcpyAsync(nodes.data(), s.nodes, nodes.size() * sizeof(float4), cudaMemcpyDeviceToHost,
+                              (cudaStream_t) stream));
+    BVH_CHECK(cudaStreamSynchronize((cudaStream_t) stream));
+    std::vector<int> seen_int(n_int, 0), seen_leaf(n, 0);
+    std::vector<int> stack(1, s.root);
+    while (!stack.empty()) {
+        int c = stack.back();
+        stack.pop_back();
+        if (c < 0) {
+            if (~c >= n) return "leaf index out of range: " + std::to_string(~c);
+            if (seen_leaf[~c]++) return "leaf reached twice: " + std::to_string(~c);
+            continue;
+        }
+        if (c >= n_int) return "node index out of range: " + std::to_string(c);
+        if (seen_int[c]++) return "node reached twice: " + std::to_string(c);
+        float4 n3 = nodes[4 * (size_t) c + 3];
+        int l, r;
+        memcpy(&l, &n3.x, 4);
+        memcpy(&r, &n3.y, 4);
+        stack.push_back(l);
+        stack.push_back(r);
+    }
+    for (int i = 0; i < n_int; ++i)
+        if (!seen_int[i]) return "node unreachable: " + std::to_string(i);
+    for (int i = 0; i < n; ++i)
+        if (!seen_leaf[i]) return "leaf unreachable: " + std::to_string(i);
+    return "";
+}
+
+void bvh_free(BvhStorage& s, void* stream)
+{
+    cudaStream_t st = (cudaStream_t) stream;
+    if (s.nodes) cudaFreeAsync(s.nodes, st);
+    if (s.tris) cudaFreeAsync(s.tris, st);
+    s.nodes = nullptr;
+    s.tris = nullptr;
+    s.n_tris = 0;
+}
+
+}  // namespace lg

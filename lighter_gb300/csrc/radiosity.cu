@@ -1,0 +1,220 @@
+// Dense radiosity of the bake (see radiosity.cuh).
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+
+#include <stdexcept>
+#include <string>
+
+#include "radiosity.cuh"
+
+namespace lg {
+namespace {
+
+void rck(cudaError_t e, const char* what, int line)
+{
+    if (e != cudaSuccess)
+        throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(e) + " at radiosity.cu:" +
+                                 std::to_string(line) + " (" + what + ")");
+}
+#define RCK(x) rck((x), #x, __LINE__)
+
+template <class T> __device__ __forceinline__ T to_store(float f);
+template <> __device__ __forceinline__ float to_store<float>(float f) { return f; }
+template <> __device__ __forceinline__ __half to_store<__half>(float f) { return __float2half_rn(f); }
+template <> __device__ __forceinline__ __nv_bfloat16 to_store<__nv_bfloat16>(float f) { return __float2bfloat16_rn(f); }
+
+__device__ __forceinline__ float to_f(float v) { return v; }
+__device__ __forceinline__ float to_f(__half v) { return __half2float(v); }
+__device__ __forceinline__ float to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+// Link factor of the pair (i, j), i < j (lighter.cpp:733-757): facing tests on
+// the unnormalised offset, f = dotA dotB / (|d|^4 pi) >= SMALL_FLOAT, then the
+// predicate on the segment between the two samples.
+__device__ __forceinline__ float pair_factor(const BvhView& bvh, ErrFlag err, int links, V3 AP, V3 AN, V3 BP, V3 BN,
+                                             unsigned& vis)
+{
+    V3 pd = BP - AP;
+    float dA = dot(AN, pd), dB = dot(BN, -pd);
+    if (dA <= kSmall || dB <= kSmall) return 0.0f;
+    float l2 = lensq(pd);
+    float f = dA * dB / (l2 * l2 * 3.14159265358979323846f);
+    if (f < kSmall) return 0.0f;
+    ++vis;
+    // ltr_Scene::VisibilityTest (lighter.cpp:138-147): segment shrunk by
+    // SMALL_FLOAT at both ends, any occluder hit
+    V3 dn = normalized(BP - AP);
+    bool occluded = bvh_any_hit(bvh, AP + dn * kSmall, BP - dn * kSmall, err);
+    bool keep = links == 0 ? occluded : !occluded;
+    return keep ? f : 0.0f;
+}
+
+// 32x32 tile of F per block (upper-triangle tiles only); entries written to
+// both (i, j) and (j, i) through a shared-memory transpose.
+template <class T>
+__global__ void k_form_factors(u32 n, const float4* __restrict__ pos, const float4* __restrict__ nrm, BvhView bvh,
+                               ErrFlag err, int links, T* __restrict__ F, unsigned long long* counts)
+{
+    __shared__ float tile[32][33];
+    const u32 bi = blockIdx.y, bj = blockIdx.x;
+    if (bj < bi) return;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    unsigned nlinks = 0, nvis = 0;
+    for (int k = 0; k < 4; ++k) {
+        int r = ty + 8 * k;
+        u32 i = bi * 32 + r, j = bj * 32 + tx;
+        float f = 0.0f;
+        if (i < j && j < n) {
+            f = pair_factor(bvh, err, links, ld3(pos[i]), ld3(nrm[i]), ld3(pos[j]), ld3(nrm[j]), nvis);
+            nlinks += f != 0.0f;
+        }
+        tile[r][tx] = f;
+    }
+    __syncthreads();
+    for (int k = 0; k < 4; ++k) {
+        int r = ty + 8 * k;
+        if (bi == bj) {
+            u32 i = bi * 32 + r, j = bj * 32 + tx;
+            if (i < n && j < n) F[(size_t) i * n + j] = to_store<T>(tile[r][tx] + tile[tx][r]);
+        } else {
+            u32 i = bi * 32 + r, j = bj * 32 + tx;
+            if (i < n && j < n) F[(size_t) i * n + j] = to_store<T>(tile[r][tx]);
+            u32 i2 = bj * 32 + r, j2 = bi * 32 + tx;
+            if (i2 < n && j2 < n) F[(size_t) i2 * n + j2] = to_store<T>(tile[tx][r]);
+        }
+    }
+    // block totals
+    for (int o = 16; o > 0; o >>= 1) {
+        nlinks += __shfl_down_sync(0xffffffffu, nlinks, o);
+        nvis += __shfl_down_sync(0xffffffffu, nvis, o);
+    }
+    if (tx == 0) {
+        atomicAdd(&counts[0], (unsigned long long) nlinks);
+        atomicAdd(&counts[1], (unsigned long long) nvis);
+    }
+}
+
+// X_j = (out_j * diffuse_j) * area_j (lighter.cpp:781-782 without the factor).
+__global__ void k_rad_x(u32 n, const float4* __restrict__ out, const float4* __restrict__ da, float4* __restrict__ X)
+{
+    u32 j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    float4 o = out[j], d = da[j];
+    V3 x = (mk(o.x, o.y, o.z) * mk(d.x, d.y, d.z)) * d.w;
+    X[j] = st4(x, 0.0f);
+}
+
+// Y = F X, one warp per row; F streamed once per bounce (HBM-bound).
+template <class T>
+__global__ void k_rad_gemv(u32 n, const T* __restrict__ F, const float4* __restrict__ X, float4* __restrict__ Y)
+{
+    const int lane = threadIdx.x & 31;
+    u32 row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (row >= n) return;
+    const T* fr = F + (size_t) row * n;
+    float ax = 0, ay = 0, az = 0;
+    for (u32 j = lane; j < n; j += 32) {
+        float f = to_f(fr[j]);
+        if (f != 0.0f) {
+            float4 x = __ldg(&X[j]);
+            ax += x.x * f; ay += x.y * f; az += x.z * f;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ax += __shfl_down_sync(0xffffffffu, ax, o);
+        ay += __shfl_down_sync(0xffffffffu, ay, o);
+        az += __shfl_down_sync(0xffffffffu, az, o);
+    }
+    if (lane == 0) Y[row] = make_float4(ax, ay, az, 0.0f);
+}
+
+// total += Y, out = Y (lighter.cpp:784-796).
+__global__ void k_rad_update(u32 n, const float4* __restrict__ Y, float4* __restrict__ total, float4* __restrict__ out)
+{
+    u32 j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    float4 y = Y[j], t = total[j];
+    total[j] = make_float4(t.x + y.x, t.y + y.y, t.z + y.z, 0.0f);
+    out[j] = y;
+}
+
+template <class T>
+RadResult solve_t(const RadInputs& in, const RadSettings& rs, const BvhView& bvh, ErrFlag err, cudaStream_t st,
+                  float4* lm_out, std::atomic<bool>* abort_flag)
+{
+    RadResult rr;
+    const u32 n = in.n;
+    size_t free_b = 0, total_b = 0;
+    RCK(cudaMemGetInfo(&free_b, &total_b));
+    size_t fbytes = (size_t) n * n * sizeof(T);
+    if (fbytes > free_b / 10 * 9)
+        throw std::runtime_error("radiosity: dense form factors for " + std::to_string(n) + " samples need " +
+                                 std::to_string(fbytes >> 20) + " MiB, more than the free device memory");
+    T* F = nullptr;
+    float4 *pos, *nrm, *da, *out, *total, *X, *Y;
+    unsigned long long* counts;
+    RCK(cudaMallocAsync(&F, fbytes ? fbytes : 1, st));
+    RCK(cudaMallocAsync(&pos, n * sizeof(float4), st));
+    RCK(cudaMallocAsync(&nrm, n * sizeof(float4), st));
+    RCK(cudaMallocAsync(&da, n * sizeof(float4), st));
+    RCK(cudaMallocAsync(&out, n * sizeof(float4), st));
+    RCK(cudaMallocAsync(&total, n * sizeof(float4), st));
+    RCK(cudaMallocAsync(&X, n * sizeof(float4), st));
+    RCK(cudaMallocAsync(&Y, n * sizeof(float4), st));
+    RCK(cudaMallocAsync(&counts, 2 * sizeof(unsigned long long), st));
+    struct Free {
+        cudaStream_t st; void* p[9];
+        ~Free() { for (void* q : p) if (q) cudaFreeAsync(q, st); }
+    } guard{st, {F, pos, nrm, da, out, total, X, Y, counts}};
+    RCK(cudaMemcpyAsync(pos, in.pos.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st));
+    RCK(cudaMemcpyAsync(nrm, in.nrm.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st));
+    RCK(cudaMemcpyAsync(da, in.diff_area.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st));
+    RCK(cudaMemcpyAsync(out, in.emit.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st));
+    RCK(cudaMemcpyAsync(total, in.emit.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st));
+    RCK(cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned long long), st));
+
+    cudaEvent_t e0, e1, e2;
+    RCK(cudaEventCreate(&e0)); RCK(cudaEventCreate(&e1)); RCK(cudaEventCreate(&e2));
+    RCK(cudaEventRecord(e0, st));
+    u32 nb = (n + 31) / 32;
+    if (nb > 65535) throw std::runtime_error("radiosity: too many samples for the tile grid");
+    dim3 grid(nb, nb), block(32, 8);
+    k_form_factors<T><<<grid, block, 0, st>>>(n, pos, nrm, bvh, err, rs.links, F, counts);
+    RCK(cudaGetLastError());
+    RCK(cudaEventRecord(e1, st));
+    for (int b = 0; b < rs.bounces; ++b) {
+        if (abort_flag && abort_flag->load()) break;
+        k_rad_x<<<(n + 255) / 256, 256, 0, st>>>(n, out, da, X);
+        k_rad_gemv<T><<<(unsigned) (((size_t) n * 32 + 255) / 256), 256, 0, st>>>(n, F, X, Y);
+        k_rad_update<<<(n + 255) / 256, 256, 0, st>>>(n, Y, total, out);
+        RCK(cudaGetLastError());
+    }
+    RCK(cudaEventRecord(e2, st));
+    RCK(cudaMemcpyAsync(lm_out, total, n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    unsigned long long hc[2];
+    RCK(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    RCK(cudaStreamSynchronize(st));
+    float m1 = 0, m2 = 0;
+    cudaEventElapsedTime(&m1, e0, e1);
+    cudaEventElapsedTime(&m2, e1, e2);
+    cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
+    rr.links = hc[0];
+    rr.vis_rays = hc[1];
+    rr.pairs = (uint64_t) n * (n - 1) / 2;
+    rr.ms_links = m1;
+    rr.ms_bounce = m2;
+    return rr;
+}
+
+}  // namespace
+
+RadResult radiosity_solve(const RadInputs& in, const RadSettings& rs, const BvhView& bvh, ErrFlag err, cudaStream_t st,
+                          float4* lm_out, std::atomic<bool>* abort_flag)
+{
+    if (in.n == 0) return RadResult();
+    if (rs.precision == 1) return solve_t<__half>(in, rs, bvh, err, st, lm_out, abort_flag);
+    if (rs.precision == 2) return solve_t<__nv_bfloat16>(in, rs, bvh, err, st, lm_out, abort_flag);
+    return solve_t<float>(in, rs, bvh, err, st, lm_out, abort_flag);
+}
+
+}  // namespace lg

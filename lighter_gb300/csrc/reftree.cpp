@@ -1,0 +1,98 @@
+// Host build of the reference-shaped per-instance trees (see reftree.hpp).
+#include "reftree.hpp"
+
+#include <algorithm>
+#include <cfloat>
+
+namespace lg {
+namespace {
+
+struct Box { V3 mn, mx; };
+
+inline float volume(const Box& b) { return (b.mx.x - b.mn.x) * (b.mx.y - b.mn.y) * (b.mx.z - b.mn.z); }
+inline V3 centre(const Box& b) { return (b.mn + b.mx) * 0.5f; }
+
+struct Builder {
+    const Box* boxes;
+    RefTree* t;
+
+    void emit(int32_t node, const int32_t* ids, size_t n)
+    {
+        t->nodes[node].ido = (int32_t) t->items.size();
+        t->items.push_back((int32_t) n);
+        t->items.insert(t->items.end(), ids, ids + n);
+    }
+
+    void make(int32_t node, const int32_t* ids, size_t n, int depth)
+    {
+        V3 mn = splat(FLT_MAX), mx = splat(-FLT_MAX);
+        for (size_t i = 0; i < n; ++i) { mn = vmin(mn, boxes[ids[i]].mn); mx = vmax(mx, boxes[ids[i]].mx); }
+        RefNode& N = t->nodes[node];
+        N.mn[0] = mn.x; N.mn[1] = mn.y; N.mn[2] = mn.z;
+        N.mx[0] = mx.x; N.mx[1] = mx.y; N.mx[2] = mx.z;
+        N.ch = -1;
+        N.ido = -1;
+        Box nb = {mn, mx};
+        float nvol = volume(nb);
+        if (n > 4 && depth < 16) {
+            int nsplit = 0;
+            V3 smn = splat(FLT_MAX), smx = splat(-FLT_MAX);
+            for (size_t i = 0; i < n; ++i) {
+                const Box& b = boxes[ids[i]];
+                if (volume(b) * 3 < nvol) { nsplit++; smn = vmin(smn, b.mn); smx = vmax(smx, b.mx); }
+            }
+            V3 ss = smx - smn;
+            V3 axis = mk(0, 0, 1);
+            if (ss.x > ss.y && ss.x > ss.z) axis = mk(1, 0, 0);
+            else if (ss.y > ss.x && ss.y > ss.z) axis = mk(0, 1, 0);
+            if (nsplit >= 4) {
+                std::vector<int32_t> self, split;
+                for (size_t i = 0; i < n; ++i) {
+                    if (volume(boxes[ids[i]]) * 3 < nvol) split.push_back(ids[i]);
+                    else self.push_back(ids[i]);
+                }
+                if (!self.empty()) emit(node, self.data(), self.size());
+                const Box* bx = boxes;
+                std::sort(split.begin(), split.end(), [bx, axis](int32_t a, int32_t b) {
+                    return dot(axis, centre(bx[a])) < dot(axis, centre(bx[b]));
+                });
+                size_t mid = split.size() / 2;
+                t->nodes.push_back(RefNode());
+                make((int32_t) t->nodes.size() - 1, split.data(), mid, depth + 1);
+                t->nodes[node].ch = (int32_t) t->nodes.size();
+                t->nodes.push_back(RefNode());
+                make((int32_t) t->nodes.size() - 1, split.data() + mid, split.size() - mid, depth + 1);
+                return;
+            }
+        }
+        emit(node, ids, n);
+    }
+};
+
+}  // namespace
+
+void build_ref_tree(const float* xyz, size_t n, RefTree& out)
+{
+    out.nodes.assign(1, RefNode());
+    out.items.clear();
+    RefNode& root = out.nodes[0];
+    for (int c = 0; c < 3; ++c) { root.mn[c] = FLT_MAX; root.mx[c] = -FLT_MAX; }
+    root.ch = -1;
+    root.ido = -1;
+    if (n == 0) return;
+    std::vector<Box> boxes(n);
+    std::vector<int32_t> ids;
+    ids.reserve(n);
+    for (size_t i = 0; i < n; ++i) {
+        const float* p = xyz + 9 * i;
+        V3 a = mk(p[0], p[1], p[2]), b = mk(p[3], p[4], p[5]), c = mk(p[6], p[7], p[8]);
+        boxes[i].mn = vmin(a, vmin(b, c));
+        boxes[i].mx = vmax(a, vmax(b, c));
+        const Box& bb = boxes[i];
+        if (bb.mn.x <= bb.mx.x && bb.mn.y <= bb.mx.y && bb.mn.z <= bb.mx.z) ids.push_back((int32_t) i);
+    }
+    Builder bld{boxes.data(), &out};
+    bld.make(0, ids.data(), ids.size(), 0);
+}
+
+}  // namespace lg

@@ -1,0 +1,83 @@
+// Host-side scene model behind the ltr_* API (replaces ltr_Scene/ltr_Mesh/
+// ltr_MeshInstance/ltr_Light of lighter_int.hpp:837-1051). Ingest copies the
+// caller's data here; ltr_Start hands the scene to the bake thread
+// (bake.cu), which uploads it as structure-of-arrays device buffers.
+#pragma once
+
+#include <atomic>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/lighter_gb300.h"
+#include "common.cuh"
+
+namespace lg {
+
+struct HostPart { u32 vcount, voff, icount, ioff; int shadow; };
+
+struct HostInst {
+    ltr_Mesh* mesh = nullptr;
+    std::string ident;
+    float importance = 0;
+    float matrix[16];
+    bool shadow = false;
+    bool container = false;
+    u32 w = 128, h = 128;      // lightmap size (lighter.cpp:1277-1278 default)
+    // filled by the bake (world space, lightmap texel space)
+    std::vector<V3> vpos, vnrm;
+    std::vector<V2> vtex, ltex;
+};
+
+struct HostLight {
+    u32 type;
+    V3 pos, dir, up, color;
+    float range, power, radius;
+    int nsamples;
+    float out, in, curve;
+};
+
+// Per-instance copies of the sample arrays, kept when keep_samples is set.
+struct SampleDump {
+    std::vector<float> pos, nrm, radinfo, color;
+    std::vector<u32> loc;
+};
+
+}  // namespace lg
+
+struct ltr_Mesh {
+    ltr_Scene* scene;
+    std::string ident;
+    std::vector<lg::V3> pos, nrm;
+    std::vector<lg::V2> tex1, tex2;
+    std::vector<lg::u32> idx;
+    std::vector<lg::HostPart> parts;
+};
+
+struct ltr_Scene {
+    ltr_Config cfg;
+    ltrg_Options opt;
+    std::vector<ltr_Mesh*> meshes;
+    std::vector<lg::HostInst*> insts;   // [0] = probe-sample container
+    std::vector<lg::HostLight> lights;
+    std::vector<ltr_SampleInfo> samples;
+    std::vector<ltr_WorkOutput> outputs;
+    std::vector<lg::SampleDump> dump;
+    lg::u32 rad_links = 0;
+    ltrg_Stats stats;
+    std::string error;
+    std::atomic<const char*> stage{"not started"};
+    std::atomic<float> completion{0};
+    std::atomic<bool> abort_flag{false};
+    std::atomic<bool> running{false};
+    std::thread worker;
+
+    ltr_Scene();
+    ~ltr_Scene();
+    void clear_outputs();
+};
+
+namespace lg {
+// Runs the whole bake on the calling thread; throws std::runtime_error.
+void run_bake(ltr_Scene* s);
+}

@@ -1,0 +1,56 @@
+"""ctypes mirror of include/lighter_gb300.h (the GPU extensions)."""
+import ctypes as C
+
+from .abi import Config, SampleRequest, u32
+
+LTRG_LINKS_REFERENCE = 0
+LTRG_LINKS_VISIBLE = 1
+LTRG_F_FP32 = 0
+LTRG_F_FP16 = 1
+LTRG_F_BF16 = 2
+
+
+class Options(C.Structure):
+    _fields_ = [
+        ("device", C.c_int),
+        ("keep_samples", C.c_int),
+        ("radiosity_links", C.c_int),
+        ("radiosity_precision", C.c_int),
+        ("refine_steps", C.c_int),
+        ("reserved", u32 * 11),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "ms_total", "ms_upload", "ms_bvh", "ms_samples", "ms_direct", "ms_rad_links", "ms_rad_bounce", "ms_ao",
+        "ms_finalize", "ms_download")] + [(n, C.c_uint64) for n in (
+            "texels", "samples", "triangles", "shadow_evals", "distance_queries", "ao_rays", "rad_pairs",
+            "rad_vis_rays", "node_visits")] + [("reserved", C.c_uint64 * 7)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
+
+
+EXT_API = {
+    "ltrg_GetOptions": (None, [C.c_void_p, C.POINTER(Options)]),
+    "ltrg_SetOptions": (C.c_int, [C.c_void_p, C.POINTER(Options)]),
+    "ltrg_GetStats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "ltrg_LastError": (C.c_char_p, [C.c_void_p]),
+    "ltrg_Wait": (C.c_int, [C.c_void_p]),
+}
+
+
+def set_options(lib, scene, **kw):
+    o = Options()
+    lib.ltrg_GetOptions(scene, C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    if not lib.ltrg_SetOptions(scene, C.byref(o)):
+        raise ValueError(f"ltrg_SetOptions rejected {kw}")
+
+
+def get_stats(lib, scene) -> dict:
+    s = Stats()
+    lib.ltrg_GetStats(scene, C.byref(s))
+    return s.as_dict()

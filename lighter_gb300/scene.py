@@ -104,8 +104,20 @@ def _vec3(v):
     return abi.VEC3(*[float(x) for x in v])
 
 
+def _has(lib, name):
+    try:
+        getattr(lib, name)
+        return True
+    except AttributeError:
+        return False
+
+
 def bake(lib, desc: SceneDesc, threads: int = 1, debug: bool = True, poll_s: float = 0.001,
-         timeout_s: float = 3600.0, before_start: Optional[Callable] = None) -> BakeResult:
+         timeout_s: float = 3600.0, before_start: Optional[Callable] = None, gpu_options: Optional[dict] = None,
+         stats: Optional[dict] = None) -> BakeResult:
+    """Replay `desc` through `lib`'s C API and return its outputs. For the GPU
+    library, `gpu_options` are ltrg_Options fields and `stats` (a dict) receives
+    ltrg_GetStats; a bake that ends in an error raises RuntimeError."""
     keep = []
     scene = lib.ltr_CreateScene()
     if not scene:
@@ -216,6 +228,14 @@ def bake(lib, desc: SceneDesc, threads: int = 1, debug: bool = True, poll_s: flo
             si.normal = _vec3(nrm)
             lib.ltr_SampleAdd(scene, C.byref(si))
 
+        is_gpu = _has(lib, "ltrg_SetOptions")
+        if is_gpu:
+            from .ext import set_options
+            opts = dict(gpu_options or {})
+            if debug:
+                opts.setdefault("keep_samples", 1)
+            if opts:
+                set_options(lib, scene, **opts)
         if before_start is not None:
             before_start(scene)
         stages = []
@@ -231,6 +251,13 @@ def bake(lib, desc: SceneDesc, threads: int = 1, debug: bool = True, poll_s: flo
             time.sleep(poll_s)
         wall = time.perf_counter() - t0
         final = st.stage.decode() if st.stage else ""
+        if is_gpu:
+            if final != "finished":
+                msg = lib.ltrg_LastError(scene)
+                raise RuntimeError(f"bake {desc.name} ended with '{final}': {msg.decode() if msg else ''}")
+            if stats is not None:
+                from .ext import get_stats
+                stats.update(get_stats(lib, scene))
 
         info = abi.WorkOutputInfo()
         lib.ltr_GetWorkOutputInfo(scene, C.byref(info))
