@@ -1,0 +1,309 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 lightmap bake on the mid-size seeded scene.
+
+One step = one complete bake (ltr_Start .. finished) of the mid scene:
+200x200 m ground, 400 boxes (0.5-8 m, random yaw) and 50 icospheres of 320
+triangles (~21k triangles), four 1024^2 lightmaps, 8 point + 2 spot lights,
+32 AO rays of radius 2 m and 2 radiosity bounces over 16k patches, FP32.
+
+  value  rays/s with the scene resident on the device: rays counted by the
+         library (shadow evaluations + AO rays + radiosity visibility rays)
+         over the device time of the bake (CUDA events from the first kernel
+         after the upload to the end of finalize), summed over ranks.
+  e2e    the same rays over the host wall time of ltr_Start .. outputs on the
+         host, i.e. through the C API with the upload and readback inside.
+  roofline  the direct-light kernel (sphere-traced shadows), the dominant one:
+         algorithmic bytes = BVH node visits x 64 B + triangle tests x 48 B.
+  cpu_baseline  the CPU oracle port (all host threads) on a bounded sample.
+
+--impl reference times the reference's CPU bake on the host cores instead
+(the oracle port: the reference's own sources are not present on this machine).
+Multi-GPU runs are replicas (each rank bakes its own copy); the bake has no
+exchange step, so there is no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "rays/s & s/radiosity bounce: batched FP16-F vs plain FP32 GPU @1e-3 rel err"
+WORKLOAD = ("mid: 200x200 m ground + 400 boxes + 50 icospheres (320 tris), ~21k tris, 4 x 1024^2 lightmaps, "
+            "8 point + 2 spot lights, AO 32 rays r=2 m, radiosity 2 bounces over 16k patches, FP32")
+CPU_SAMPLE = ("same mid scene (geometry, lights, AO) at 256^2 lightmaps = 1/16 of the texels, "
+              "radiosity off (texel-level radiosity of the reference is not runnable at this size)")
+NODE_BYTES = 64
+TRI_BYTES = 48
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic_from_profile():
+    """dram bytes per launch of the direct-light kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_direct_mid.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch_full:"):
+                    return float(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        return world, rank, local, dist
+    return 1, 0, 0, None
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def _allreduce(dist, vals, op):
+    if dist is None:
+        return vals
+    import torch
+    t = torch.tensor(vals, dtype=torch.float64)
+    dist.all_reduce(t, op=op)
+    return t.tolist()
+
+
+def _oracle_bake(desc, threads):
+    """One bake of `desc` on the CPU oracle port; returns (rays, seconds, counters)."""
+    import ctypes as C
+    from lighter_gb300 import load_library
+    from lighter_gb300.scene import bake
+    orc = load_library(os.path.join(ROOT, "oracle", "liblighter_oracle.so"),
+                       extra={"orc_GetCounters": (None, [C.c_void_p])})
+    t0 = time.perf_counter()
+    bake(orc, desc, threads=threads, debug=False)
+    dt = time.perf_counter() - t0
+    cnt = (C.c_ulonglong * 4)()
+    orc.orc_GetCounters(C.cast(cnt, C.c_void_p))
+    rays = cnt[0] + cnt[2] + cnt[3]
+    return rays, dt, list(cnt)
+
+
+def run_reference(args, world, rank, dist):
+    from lighter_gb300 import scenes
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    desc = scenes.mid(seed=1, lm=args.cpu_lm, bounces=0)
+    for _ in range(args.warmup):
+        _oracle_bake(desc, threads)
+    rays_tot, t_tot = 0, 0.0
+    for _ in range(args.steps):
+        r, dt, _ = _oracle_bake(desc, threads)
+        rays_tot += r
+        t_tot += dt
+    v = rays_tot / t_tot
+    line = {
+        "metric": METRIC, "value": v, "unit": "rays/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * t_tot / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "impl": "reference",
+        "config": {"workload": WORKLOAD, "sample": CPU_SAMPLE, "parallelism": "host threads"},
+        "cpu_baseline": {"value": v, "unit": "rays/s", "cores": threads, "kind": "port", "sample": CPU_SAMPLE},
+        "e2e": {"value": v, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, world, rank, local, dist):
+    from lighter_gb300 import library, scenes
+    from lighter_gb300.ext import get_stats
+
+    lib = library()
+    desc = scenes.mid(seed=1, lm=args.lm)
+    gpu_opts = {"device": local, "radiosity_patches": args.patches, "radiosity_links": 1}
+    # ingest once through the C API; every step is ltr_Start .. finished
+    from lighter_gb300.scene import ingest
+    scene, keep = ingest(lib, desc, gpu_options=gpu_opts)
+    try:
+        for _ in range(args.warmup):
+            _bake_once(lib, scene)
+        _barrier(dist)
+        sampler = ClockSampler(local)
+        sampler.start()
+        stats = []
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            _bake_once(lib, scene)
+            stats.append(get_stats(lib, scene))
+        wall = time.perf_counter() - t0
+        clocks = sampler.stop()
+        _barrier(dist)
+    finally:
+        lib.ltr_DestroyScene(scene)
+        del keep
+    rays = sum(s["shadow_evals"] + s["ao_rays"] + s["rad_vis_rays"] for s in stats)
+    dev_ms = sum(s["ms_device"] for s in stats)
+    launches = sum(s["kernel_launches"] for s in stats)
+    return rays, dev_ms, wall, stats, clocks, stats[-1]["bytes_h2d"], stats[-1]["bytes_d2h"], launches
+
+
+def _bake_once(lib, scene):
+    lib.ltr_Start(scene)
+    if not lib.ltrg_Wait(scene):
+        msg = lib.ltrg_LastError(scene)
+        raise RuntimeError("bake failed: " + (msg.decode() if msg else "unknown"))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--lm", type=int, default=1024, help="lightmap side of the mid scene")
+    ap.add_argument("--patches", type=int, default=16384)
+    ap.add_argument("--cpu-lm", type=int, default=256, help="lightmap side of the CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local, dist = _dist()
+    if args.impl == "reference":
+        return run_reference(args, world, rank, dist)
+
+    rays, dev_ms, wall, stats, clocks, h2d, d2h, launches = run_ours(args, world, rank, local, dist)
+    if dist is not None:
+        import torch.distributed as td
+        rays_all, = _allreduce(dist, [float(rays)], td.ReduceOp.SUM)
+        dev_ms_max, wall_max = _allreduce(dist, [dev_ms, wall], td.ReduceOp.MAX)
+    else:
+        rays_all, dev_ms_max, wall_max = float(rays), dev_ms, wall
+    if rank != 0:
+        return 0
+
+    s0 = stats[-1]
+    peak, peak_kind = _peaks()
+    direct_bytes = s0["node_visits"] * NODE_BYTES + s0["tri_tests"] * TRI_BYTES
+    achieved = direct_bytes / (s0["ms_direct"] / 1000.0) / 1e9 if s0["ms_direct"] > 0 else 0.0
+    bounces = 2
+    line = {
+        "metric": METRIC,
+        "value": rays_all / (dev_ms_max / 1000.0),
+        "unit": "rays/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dev_ms_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded procedural scene, seed 1)",
+        "config": {
+            "workload": WORKLOAD,
+            "lightmap": args.lm,
+            "radiosity_patches": args.patches,
+            "radiosity_links": "visible pairs (patch mode)",
+            "l2": "inputs larger than L2: per-bake sample buffers of %.0f MB, scene re-uploaded every step"
+                  % (s0["samples"] * 84 / 1e6),
+            "parallelism": "replicas" if world > 1 else "single GPU",
+        },
+        "e2e": {"value": rays_all / wall_max, "unit": "rays/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "k_direct (sphere-traced shadows)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": _traffic_from_profile(),
+                     "algorithmic_bytes_per_launch": direct_bytes},
+        "clocks": clocks,
+        "s_per_bounce": s0["ms_rad_bounce"] / bounces / 1000.0,
+        "texels_per_s": s0["samples"] / (s0["ms_device"] / 1000.0),
+        "rays_per_step": {"shadow": s0["shadow_evals"], "ao": s0["ao_rays"], "radiosity_visibility": s0["rad_vis_rays"]},
+        "distance_queries_per_s": s0["distance_queries"] / (s0["ms_device"] / 1000.0),
+        "stages_ms": {k: round(s0[k], 3) for k in ("ms_upload", "ms_bvh", "ms_samples", "ms_direct", "ms_rad_links",
+                                                    "ms_rad_bounce", "ms_ao", "ms_finalize", "ms_download",
+                                                    "ms_device", "ms_total")},
+    }
+    if not args.no_cpu_baseline:
+        from lighter_gb300 import scenes
+        threads = os.cpu_count() or 1
+        r, dt, cnt = _oracle_bake(scenes.mid(seed=1, lm=args.cpu_lm, bounces=0), threads)
+        line["cpu_baseline"] = {"value": r / dt, "unit": "rays/s", "cores": threads, "kind": "port",
+                                "sample": CPU_SAMPLE, "seconds": dt}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

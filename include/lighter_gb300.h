@@ -32,7 +32,11 @@ typedef struct ltrg_Options {
     int radiosity_links;      /* LTRG_LINKS_*, default LTRG_LINKS_REFERENCE */
     int radiosity_precision;  /* LTRG_F_*, default LTRG_F_FP32 */
     int refine_steps;         /* FP32 residual-refinement sweeps for FP16/BF16 F, default 1 */
-    uint32_t reserved[11];
+    uint32_t radiosity_patches; /* 0: one radiosity element per sample (reference, lighter.cpp:673-719);
+                                   N > 0: group samples into about N patches by (instance, lightmap
+                                   tile, dominant normal axis); each texel then receives its patch's
+                                   gathered (bounced) light on top of its own direct light */
+    uint32_t reserved[10];
 } ltrg_Options;
 
 /* Per-stage device times (CUDA events on the bake stream) and work counters
@@ -57,7 +61,13 @@ typedef struct ltrg_Stats {
     uint64_t rad_pairs;       /* radiosity pairs i<j examined */
     uint64_t rad_vis_rays;    /* pairs that passed the facing/form-factor tests */
     uint64_t node_visits;     /* BVH internal nodes visited by the direct-light queries */
-    uint64_t reserved[7];
+    uint64_t tri_tests;       /* point/triangle distance tests of the direct-light queries */
+    uint64_t rad_elements;    /* radiosity elements: samples, or patches in patch mode */
+    uint64_t kernel_launches; /* CUDA kernels this library launched for the bake */
+    uint64_t bytes_h2d;       /* host->device bytes copied for the bake */
+    uint64_t bytes_d2h;       /* device->host bytes copied for the bake */
+    double ms_device;         /* device time from the first kernel to the last (CUDA events) */
+    uint64_t reserved[1];
 } ltrg_Stats;
 
 /* Options are read at ltr_Start; returns 0 on an invalid value. */

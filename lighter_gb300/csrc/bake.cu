@@ -17,6 +17,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
+#include <unordered_map>
 #include <chrono>
 #include <thread>
 #include <cstring>
@@ -30,6 +32,12 @@
 #include "scene.hpp"
 
 namespace lg {
+
+HostCounters& host_counters()
+{
+    static thread_local HostCounters c;
+    return c;
+}
 
 namespace {
 
@@ -65,7 +73,7 @@ struct DLight {
 constexpr int kRT = 32;
 
 struct Counters {
-    unsigned long long shadow_evals, distance_queries, ao_rays, rad_pairs, rad_vis_rays, node_visits, links, pad;
+    unsigned long long shadow_evals, distance_queries, ao_rays, rad_pairs, rad_vis_rays, node_visits, tri_tests, pad;
 };
 
 // Warp total of a per-thread count, added once per warp; every lane of the
@@ -289,13 +297,14 @@ __global__ void k_fixup(FixupArgs a)
 // ----------------------------------------------------------------------------- direct light
 
 // Sphere-traced soft-shadow factor (ltr_Scene::CalcInvShadowFactor, lighter.cpp:190-207).
-__device__ __forceinline__ float inv_shadow(const BvhView& bvh, V3 from, V3 to, float k, ErrFlag err, u32& nq, u32& nv)
+__device__ __forceinline__ float inv_shadow(const BvhView& bvh, V3 from, V3 to, float k, ErrFlag err, u32& nq, u32& nv,
+                                            u32& nt)
 {
     V3 rd = normalized(to - from);
     float maxt = len(to - from);
     float res = 1.0f;
     for (float t = 0.001f; t < maxt;) {
-        float h = bvh_distance(bvh, from + rd * t, kMaxPenumbraSize, err, &nv);
+        float h = bvh_distance(bvh, from + rd * t, kMaxPenumbraSize, err, &nv, &nt);
         ++nq;
         if (h < 0.001f) return 0.0f;
         res = fmin_(res, h / fmin_(t * k, kMaxPenumbraSize));
@@ -324,7 +333,7 @@ struct DirectArgs {
 __global__ void k_direct(DirectArgs a)
 {
     unsigned long long total = (unsigned long long) a.n_lights * a.n_samples;
-    unsigned long long c_traced = 0, c_nq = 0, c_nv = 0;
+    unsigned long long c_traced = 0, c_nq = 0, c_nv = 0, c_nt = 0;
     for (unsigned long long w = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; w < total;
          w += (unsigned long long) gridDim.x * blockDim.x) {
         int l = (int) (w / a.n_samples);
@@ -333,7 +342,7 @@ __global__ void k_direct(DirectArgs a)
         u32 inst = a.sinst[s];
         float kv = 0.0f;
         float4 nd = make_float4(0, 0, 0, 0);
-        u32 nq = 0, nv = 0, traced = 0;
+        u32 nq = 0, nv = 0, nt = 0, traced = 0;
         if (a.lit[(size_t) l * a.n_inst + inst]) {
             V3 SP = ld3(a.spos[s]), SN = ld3(a.snrm[s]);
             V3 Lpos = mk(L.pos[0], L.pos[1], L.pos[2]);
@@ -356,7 +365,7 @@ __global__ void k_direct(DirectArgs a)
                     go = !(f_dist * f_ndotl <= 0);
                 }
                 if (go) {
-                    float vis = inv_shadow(a.bvh, SP + SN * kShadowOffset, Lpos, L.radius, a.err, nq, nv);
+                    float vis = inv_shadow(a.bvh, SP + SN * kShadowOffset, Lpos, L.radius, a.err, nq, nv, nt);
                     traced = 1;
                     kv = L.type == 2 ? f_dist * f_ndotl * f_dir * vis : f_dist * f_ndotl * vis;
                     float fac = L.type == 2 ? f_dist * f_dir * vis * f_ndotl * brightness(Lcol)
@@ -365,7 +374,7 @@ __global__ void k_direct(DirectArgs a)
                 }
             } else if (L.type == 3) {
                 float f_ndotl = fmax_(0.0f, dot(Ldir, SN));
-                float vis = inv_shadow(a.bvh, SP + SN * kShadowOffset, SP + Ldir * L.range, L.radius, a.err, nq, nv);
+                float vis = inv_shadow(a.bvh, SP + SN * kShadowOffset, SP + Ldir * L.range, L.radius, a.err, nq, nv, nt);
                 traced = 1;
                 kv = f_ndotl * vis;
                 float fac = vis * f_ndotl * brightness(Lcol);
@@ -377,11 +386,13 @@ __global__ void k_direct(DirectArgs a)
         c_traced += traced;
         c_nq += nq;
         c_nv += nv;
+        c_nt += nt;
     }
     if (a.counters) {
         warp_add(&a.counters->shadow_evals, c_traced);
         warp_add(&a.counters->distance_queries, c_nq);
         warp_add(&a.counters->node_visits, c_nv);
+        warp_add(&a.counters->tri_tests, c_nt);
     }
 }
 
@@ -637,6 +648,7 @@ struct Arena {
     {
         T* d = alloc<T>(v.size());
         if (!v.empty()) CK(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+        note_h2d(v.size() * sizeof(T));
         return d;
     }
     template <class T> T* zeros(size_t n)
@@ -772,6 +784,7 @@ void run_bake(ltr_Scene* S)
 {
     const ltr_Config& cfg = S->cfg;
     memset(&S->stats, 0, sizeof(S->stats));
+    host_counters() = HostCounters();
     S->rad_links = 0;
 
     int ndev = 0;
@@ -1030,7 +1043,7 @@ void run_bake(ltr_Scene* S)
         unsigned long long nw = woff[pass][n_rt];
         if (nw == 0) continue;
         k_raster_mark<<<blocks_for(nw), kThreads, 0, st>>>(pass, margins[pass], d_rt, d_rinst, d_bbox[pass],
-                                                           d_woff[pass], n_rt, nw, d_tex_off, d_inst_w, d_keys);
+                                                           d_woff[pass], n_rt, nw, d_tex_off, d_inst_w, d_keys); note_launch();
         CK(cudaGetLastError());
         checkpoint("raster mark");
     }
@@ -1042,7 +1055,7 @@ void run_bake(ltr_Scene* S)
     CK(cudaMemsetAsync(d_flags + ntex, 0, sizeof(u32), st));
     if (ntex) {
         k_raster_resolve<<<blocks_for(ntex), kThreads, 0, st>>>(ntex, d_keys, d_rt, d_rinst, d_tex_off, d_inst_w,
-                                                                d_R1, d_R2, d_R3, d_flags);
+                                                                d_R1, d_R2, d_R3, d_flags); note_launch();
         CK(cudaGetLastError());
         checkpoint("raster resolve");
     }
@@ -1085,15 +1098,15 @@ void run_bake(ltr_Scene* S)
             pp[i] = make_float4(si.position[0], si.position[1], si.position[2], 0);
             pn[i] = make_float4(si.normal[0], si.normal[1], si.normal[2], 0);
         }
-        CK(cudaMemcpyAsync(d_spos, pp.data(), n_probe * sizeof(float4), cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(d_snrm, pn.data(), n_probe * sizeof(float4), cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(d_sloc, pl.data(), n_probe * sizeof(u32), cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(d_sinst, pi.data(), n_probe * sizeof(u32), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(d_spos, pp.data(), n_probe * sizeof(float4), cudaMemcpyHostToDevice, st)); note_h2d(n_probe * sizeof(float4));
+        CK(cudaMemcpyAsync(d_snrm, pn.data(), n_probe * sizeof(float4), cudaMemcpyHostToDevice, st)); note_h2d(n_probe * sizeof(float4));
+        CK(cudaMemcpyAsync(d_sloc, pl.data(), n_probe * sizeof(u32), cudaMemcpyHostToDevice, st)); note_h2d(n_probe * sizeof(u32));
+        CK(cudaMemcpyAsync(d_sinst, pi.data(), n_probe * sizeof(u32), cudaMemcpyHostToDevice, st)); note_h2d(n_probe * sizeof(u32));
         CK(cudaStreamSynchronize(st));
     }
     if (ntex) {
         k_compact<<<blocks_for(ntex), kThreads, 0, st>>>(ntex, d_flags, d_scan, d_R1, d_R2, d_R3, d_tex_off, n_inst,
-                                                         n_probe, d_spos, d_snrm, d_srad, d_sloc, d_sinst);
+                                                         n_probe, d_spos, d_snrm, d_srad, d_sloc, d_sinst); note_launch();
         CK(cudaGetLastError());
         checkpoint("compaction");
     }
@@ -1113,7 +1126,7 @@ void run_bake(ltr_Scene* S)
         fa.spos = d_spos;
         fa.snrm = d_snrm;
         fa.srad = d_srad;
-        k_fixup<<<(n_cov + 127) / 128, 128, 0, st>>>(fa);
+        k_fixup<<<(n_cov + 127) / 128, 128, 0, st>>>(fa); note_launch();
         CK(cudaGetLastError());
         checkpoint("sample fixup");
     }
@@ -1144,12 +1157,12 @@ void run_bake(ltr_Scene* S)
         da.ndir = d_ndir;
         da.counters = d_cnt;
         unsigned long long items = (unsigned long long) n_lights * n_samples;
-        k_direct<<<blocks_for(items, 128, 152ull * 256), 128, 0, st>>>(da);
+        k_direct<<<blocks_for(items, 128, 152ull * 256), 128, 0, st>>>(da); note_launch();
         CK(cudaGetLastError());
     }
     if (n_samples) {
         k_accumulate<<<(n_samples + kThreads - 1) / kThreads, kThreads, 0, st>>>(
-            n_samples, n_lights, d_lights, d_kval, cfg.ambient_color[0], cfg.ambient_color[1], cfg.ambient_color[2], d_lm);
+            n_samples, n_lights, d_lights, d_kval, cfg.ambient_color[0], cfg.ambient_color[1], cfg.ambient_color[2], d_lm); note_launch();
         CK(cudaGetLastError());
     }
     cudaEvent_t e_direct = clock.mark();
@@ -1162,11 +1175,11 @@ void run_bake(ltr_Scene* S)
         // host side of the sample gathering: sample_fn per sample, in order
         std::vector<float4> hpos(n_samples), hnrm(n_samples), hrad(n_samples), hlm(n_samples);
         std::vector<u32> hloc(n_samples);
-        CK(cudaMemcpyAsync(hpos.data(), d_spos, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(hnrm.data(), d_snrm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(hrad.data(), d_srad, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(hlm.data(), d_lm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(hloc.data(), d_sloc, n_samples * sizeof(u32), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hpos.data(), d_spos, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(float4));
+        CK(cudaMemcpyAsync(hnrm.data(), d_snrm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(float4));
+        CK(cudaMemcpyAsync(hrad.data(), d_srad, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(float4));
+        CK(cudaMemcpyAsync(hlm.data(), d_lm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(float4));
+        CK(cudaMemcpyAsync(hloc.data(), d_sloc, n_samples * sizeof(u32), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(u32));
         CK(cudaStreamSynchronize(st));
         RadInputs ri;
         ri.n = n_samples;
@@ -1214,7 +1227,83 @@ void run_bake(ltr_Scene* S)
         rs.precision = S->opt.radiosity_precision;
         rs.refine_steps = S->opt.refine_steps;
         rs.bounces = cfg.bounce_count;
-        RadResult rr = radiosity_solve(ri, rs, bv, err_rad, st, d_lm, &S->abort_flag);
+        RadResult rr;
+        if (S->opt.radiosity_patches == 0) {
+            rr = radiosity_solve(ri, rs, bv, err_rad, st, d_lm, &S->abort_flag);
+            S->stats.rad_elements = n_samples;
+        } else {
+            // Patch mode: group samples by (instance, lightmap tile, dominant
+            // normal axis); a patch carries the area-weighted mean position,
+            // normal, albedo and emission of its samples and their total area.
+            u32 target = S->opt.radiosity_patches;
+            double per = std::max(1.0, (double) n_cov / (double) target);
+            u32 tile = (u32) std::max(1.0, std::floor(std::sqrt(per) + 0.5));
+            std::vector<int> patch_of(n_samples, -1);
+            std::unordered_map<uint64_t, int> key_to_patch;
+            std::vector<double> acc;   // per patch: area, pos3, nrm3, diff3, emit3 (area-weighted)
+            for (int i = 1; i < n_inst; ++i) {
+                HostInst* mi = S->insts[i];
+                for (u32 k = 0; k < scount[i]; ++k) {
+                    u32 s = sbeg[i] + k;
+                    u32 L = hloc[s];
+                    u32 tx = (L % mi->w) / tile, ty = (L / mi->w) / tile;
+                    float4 n = ri.nrm[s];
+                    float ax = fabsf(n.x), ay = fabsf(n.y), az = fabsf(n.z);
+                    u32 axis = (ax >= ay && ax >= az) ? (n.x >= 0 ? 0 : 1) : (ay >= az ? (n.y >= 0 ? 2 : 3) : (n.z >= 0 ? 4 : 5));
+                    uint64_t key = ((uint64_t) i << 40) ^ ((uint64_t) ty << 21) ^ ((uint64_t) tx << 3) ^ axis;
+                    auto it = key_to_patch.find(key);
+                    int p;
+                    if (it == key_to_patch.end()) {
+                        p = (int) key_to_patch.size();
+                        key_to_patch.emplace(key, p);
+                        acc.resize(acc.size() + 13, 0.0);
+                    } else {
+                        p = it->second;
+                    }
+                    patch_of[s] = p;
+                    double a = ri.diff_area[s].w;
+                    double* q = &acc[13 * (size_t) p];
+                    q[0] += a;
+                    q[1] += a * ri.pos[s].x; q[2] += a * ri.pos[s].y; q[3] += a * ri.pos[s].z;
+                    q[4] += a * n.x; q[5] += a * n.y; q[6] += a * n.z;
+                    q[7] += a * ri.diff_area[s].x; q[8] += a * ri.diff_area[s].y; q[9] += a * ri.diff_area[s].z;
+                    q[10] += a * ri.emit[s].x; q[11] += a * ri.emit[s].y; q[12] += a * ri.emit[s].z;
+                }
+            }
+            const u32 np = (u32) key_to_patch.size();
+            RadInputs pi;
+            pi.n = np;
+            pi.pos.resize(np); pi.nrm.resize(np); pi.diff_area.resize(np); pi.emit.resize(np);
+            for (u32 p = 0; p < np; ++p) {
+                const double* q = &acc[13 * (size_t) p];
+                double a = q[0] > 0 ? q[0] : 1.0;
+                V3 nn = normalized(mk((float) (q[4] / a), (float) (q[5] / a), (float) (q[6] / a)));
+                pi.pos[p] = make_float4((float) (q[1] / a), (float) (q[2] / a), (float) (q[3] / a), 0);
+                pi.nrm[p] = make_float4(nn.x, nn.y, nn.z, 0);
+                pi.diff_area[p] = make_float4((float) (q[7] / a), (float) (q[8] / a), (float) (q[9] / a), (float) q[0]);
+                pi.emit[p] = make_float4((float) (q[10] / a), (float) (q[11] / a), (float) (q[12] / a), 0);
+            }
+            float4* d_ptot = A.alloc<float4>(np);
+            rr = radiosity_solve(pi, rs, bv, err_rad, st, d_ptot, &S->abort_flag);
+            std::vector<float4> ptot(np);
+            CK(cudaMemcpyAsync(ptot.data(), d_ptot, np * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(np * sizeof(float4));
+            CK(cudaStreamSynchronize(st));
+            // texel = own emission + its patch's gathered light
+            std::vector<float4> out(n_samples);
+            for (u32 s = 0; s < n_samples; ++s) {
+                float4 e = ri.emit[s];
+                int p = patch_of[s];
+                if (p >= 0) {
+                    e.x += ptot[p].x - pi.emit[p].x;
+                    e.y += ptot[p].y - pi.emit[p].y;
+                    e.z += ptot[p].z - pi.emit[p].z;
+                }
+                out[s] = e;
+            }
+            CK(cudaMemcpyAsync(d_lm, out.data(), n_samples * sizeof(float4), cudaMemcpyHostToDevice, st)); note_h2d(n_samples * sizeof(float4));
+            CK(cudaStreamSynchronize(st));
+            S->stats.rad_elements = np;
+        }
         S->rad_links = (u32) rr.links;
         S->stats.rad_pairs = rr.pairs;
         S->stats.rad_vis_rays = rr.vis_rays;
@@ -1248,7 +1337,7 @@ void run_bake(ltr_Scene* S)
         for (int c = 0; c < 3; ++c) aa.aoc[c] = cfg.ao_color_rgb[c];
         aa.counters = d_cnt;
         if (aa.ns > 0) {
-            k_ao<<<blocks_for((size_t) n_samples * 32, 256, 152ull * 64), 256, 0, st>>>(aa);
+            k_ao<<<blocks_for((size_t) n_samples * 32, 256, 152ull * 64), 256, 0, st>>>(aa); note_launch();
             CK(cudaGetLastError());
         }
     }
@@ -1262,14 +1351,14 @@ void run_bake(ltr_Scene* S)
     unsigned char* d_maskB = A.alloc<unsigned char>(ntex);
     if (n_cov) {
         k_scatter<<<(n_cov + kThreads - 1) / kThreads, kThreads, 0, st>>>(n_probe, n_samples, d_sloc, d_sinst, d_lm,
-                                                                          d_tex_off, d_img, d_maskA);
+                                                                          d_tex_off, d_img, d_maskA); note_launch();
         CK(cudaGetLastError());
     }
     if (ntex) {
         for (int it = 0; it < 3; ++it) {
             CK(cudaMemcpyAsync(d_maskB, d_maskA, ntex, cudaMemcpyDeviceToDevice, st));
             k_dilate<<<blocks_for(ntex), kThreads, 0, st>>>(ntex, n_inst, d_tex_off, d_inst_w, d_inst_h, d_maskA,
-                                                            d_maskB, d_img);
+                                                            d_maskB, d_img); note_launch();
             CK(cudaGetLastError());
             std::swap(d_maskA, d_maskB);
         }
@@ -1280,10 +1369,10 @@ void run_bake(ltr_Scene* S)
         float* d_taps = A.upload(taps);
         float* d_tmp = A.alloc<float>(3 * ntex);
         k_conv_t<<<blocks_for(ntex), kThreads, 0, st>>>(ntex, n_inst, d_tex_off, d_inst_w, d_inst_h, 0, ext, d_taps,
-                                                        d_img, d_tmp);
+                                                        d_img, d_tmp); note_launch();
         CK(cudaGetLastError());
         k_conv_t<<<blocks_for(ntex), kThreads, 0, st>>>(ntex, n_inst, d_tex_off, d_inst_w, d_inst_h, 1, ext, d_taps,
-                                                        d_tmp, d_img);
+                                                        d_tmp, d_img); note_launch();
         CK(cudaGetLastError());
     }
     // output layout (after optional ds2x)
@@ -1304,7 +1393,7 @@ void run_bake(ltr_Scene* S)
     if (cfg.ds2x && nout) {
         unsigned long long* d_out_off = A.upload(out_off);
         d_out = A.alloc<float>(3 * nout);
-        k_ds2x<<<blocks_for(nout), kThreads, 0, st>>>(nout, n_inst, d_out_off, d_tex_off, d_inst_w, d_inst_h, d_img, d_out);
+        k_ds2x<<<blocks_for(nout), kThreads, 0, st>>>(nout, n_inst, d_out_off, d_tex_off, d_inst_w, d_inst_h, d_img, d_out); note_launch();
         CK(cudaGetLastError());
     }
     float* d_nimg = nullptr;
@@ -1317,12 +1406,12 @@ void run_bake(ltr_Scene* S)
         float amb = brightness(mk(cfg.ambient_color[0], cfg.ambient_color[1], cfg.ambient_color[2]));
         if (n_cov && d_ndir) {
             k_normals<<<(n_cov + kThreads - 1) / kThreads, kThreads, 0, st>>>(n_probe, n_samples, n_lights, d_ndir, d_snrm,
-                                                                              d_sloc, d_sinst, d_nout_off, d_cap, amb, d_nimg);
+                                                                              d_sloc, d_sinst, d_nout_off, d_cap, amb, d_nimg); note_launch();
             CK(cudaGetLastError());
         } else if (n_cov) {
             float4* d_zero = A.zeros<float4>(1);
             k_normals<<<(n_cov + kThreads - 1) / kThreads, kThreads, 0, st>>>(n_probe, n_samples, 0, d_zero, d_snrm,
-                                                                              d_sloc, d_sinst, d_nout_off, d_cap, amb, d_nimg);
+                                                                              d_sloc, d_sinst, d_nout_off, d_cap, amb, d_nimg); note_launch();
             CK(cudaGetLastError());
         }
     }
@@ -1331,22 +1420,22 @@ void run_bake(ltr_Scene* S)
     // ---- readback
     u32 err_words[8] = {0};
     Counters cnt;
-    CK(cudaMemcpyAsync(err_words, d_err, sizeof(err_words), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(&cnt, d_cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(err_words, d_err, sizeof(err_words), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(err_words));
+    CK(cudaMemcpyAsync(&cnt, d_cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(Counters));
     std::vector<float> himg(3 * nout), hnimg(d_nimg ? 4 * nout : 0);
-    if (nout) CK(cudaMemcpyAsync(himg.data(), d_out, himg.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
-    if (d_nimg) CK(cudaMemcpyAsync(hnimg.data(), d_nimg, hnimg.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (nout) CK(cudaMemcpyAsync(himg.data(), d_out, himg.size() * sizeof(float), cudaMemcpyDeviceToHost, st)); note_d2h(himg.size() * sizeof(float));
+    if (d_nimg) CK(cudaMemcpyAsync(hnimg.data(), d_nimg, hnimg.size() * sizeof(float), cudaMemcpyDeviceToHost, st)); note_d2h(hnimg.size() * sizeof(float));
     std::vector<float4> probe_lm(n_probe);
-    if (n_probe) CK(cudaMemcpyAsync(probe_lm.data(), d_lm, n_probe * sizeof(float4), cudaMemcpyDeviceToHost, st));
+    if (n_probe) CK(cudaMemcpyAsync(probe_lm.data(), d_lm, n_probe * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_probe * sizeof(float4));
     std::vector<float4> dpos, dnrm, drad, dlm;
     std::vector<u32> dloc;
     if (S->opt.keep_samples && n_samples) {
         dpos.resize(n_samples); dnrm.resize(n_samples); drad.resize(n_samples); dlm.resize(n_samples); dloc.resize(n_samples);
-        CK(cudaMemcpyAsync(dpos.data(), d_spos, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(dnrm.data(), d_snrm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(drad.data(), d_srad, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(dlm.data(), d_lm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(dloc.data(), d_sloc, n_samples * sizeof(u32), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(dpos.data(), d_spos, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(float4));
+        CK(cudaMemcpyAsync(dnrm.data(), d_snrm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(float4));
+        CK(cudaMemcpyAsync(drad.data(), d_srad, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(float4));
+        CK(cudaMemcpyAsync(dlm.data(), d_lm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(float4));
+        CK(cudaMemcpyAsync(dloc.data(), d_sloc, n_samples * sizeof(u32), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(u32));
     }
     cudaEvent_t e_down = clock.mark();
     CK(cudaStreamSynchronize(st));
@@ -1406,6 +1495,11 @@ void run_bake(ltr_Scene* S)
     S->stats.distance_queries = cnt.distance_queries;
     S->stats.ao_rays = cnt.ao_rays;
     S->stats.node_visits = cnt.node_visits;
+    S->stats.tri_tests = cnt.tri_tests;
+    S->stats.kernel_launches = host_counters().launches;
+    S->stats.bytes_h2d = host_counters().h2d;
+    S->stats.bytes_d2h = host_counters().d2h;
+    S->stats.ms_device = StageClock::ms(e_up1, e_fin);
     (void) e_rad_links;
     (void) e_rad_bounce;
 }

@@ -199,7 +199,7 @@ void bvh_build(const BvhBuildInput& in, BvhStorage& out, void* stream)
     float3 mn = make_float3(in.scene_min[0], in.scene_min[1], in.scene_min[2]);
     float ex = in.scene_max[0] - in.scene_min[0], ey = in.scene_max[1] - in.scene_min[1], ez = in.scene_max[2] - in.scene_min[2];
     float3 inv_ext = make_float3(ex > 0 ? 1.0f / ex : 0.0f, ey > 0 ? 1.0f / ey : 0.0f, ez > 0 ? 1.0f / ez : 0.0f);
-    k_morton<<<(n + B - 1) / B, B, 0, st>>>(in.tri_xyz, n, mn, inv_ext, codes, ids);
+    k_morton<<<(n + B - 1) / B, B, 0, st>>>(in.tri_xyz, n, mn, inv_ext, codes, ids); note_launch();
     BVH_CHECK(cudaGetLastError());
 
     size_t temp_bytes = 0;
@@ -210,20 +210,20 @@ void bvh_build(const BvhBuildInput& in, BvhStorage& out, void* stream)
     if (n_int > 0) {
         BVH_CHECK(cudaMemsetAsync(parent_int, 0xff, sizeof(int) * n_int, st));
         BVH_CHECK(cudaMemsetAsync(arrivals, 0, sizeof(u32) * n_int, st));
-        k_hierarchy<<<(n_int + B - 1) / B, B, 0, st>>>(codes2, n, left, right, parent_int, parent_leaf);
+        k_hierarchy<<<(n_int + B - 1) / B, B, 0, st>>>(codes2, n, left, right, parent_int, parent_leaf); note_launch();
         BVH_CHECK(cudaGetLastError());
     }
     k_refit<<<(n + B - 1) / B, B, 0, st>>>(in.tri_xyz, ids2, n, parent_leaf, parent_int, left, right, leaf_box, int_box,
-                                            arrivals);
+                                            arrivals); note_launch();
     BVH_CHECK(cudaGetLastError());
 
     out.nodes = alloc<float4>(4 * (size_t) (n_int > 0 ? n_int : 1), st, out.bytes);
     out.tris = alloc<float4>(3 * (size_t) n, st, out.bytes);
     if (n_int > 0) {
-        k_pack_nodes<<<(n_int + B - 1) / B, B, 0, st>>>(n_int, left, right, leaf_box, int_box, out.nodes);
+        k_pack_nodes<<<(n_int + B - 1) / B, B, 0, st>>>(n_int, left, right, leaf_box, int_box, out.nodes); note_launch();
         BVH_CHECK(cudaGetLastError());
     }
-    k_pack_tris<<<(n + B - 1) / B, B, 0, st>>>(n, ids2, in.tri_xyz, in.tri_meta, in.tri_local, out.tris);
+    k_pack_tris<<<(n + B - 1) / B, B, 0, st>>>(n, ids2, in.tri_xyz, in.tri_meta, in.tri_local, out.tris); note_launch();
     BVH_CHECK(cudaGetLastError());
 
     void* ptrs[] = {codes, codes2, ids, ids2, left, right, parent_int, parent_leaf, leaf_box, int_box, arrivals, temp};

@@ -203,8 +203,10 @@ __device__ __forceinline__ float bvh_closest_inst(const BvhView& b, V3 o, V3 e, 
 // (ltr_Scene::Distance + TriTree::GetDistance, lighter.cpp:150-188,
 // lighter_math.cpp:954-989). The reference shrinks a query cube; a sphere
 // test against the child boxes prunes the same triangles.
-__device__ __forceinline__ float bvh_distance(const BvhView& b, V3 p, float d0, ErrFlag err, u32* visits = nullptr)
+__device__ __forceinline__ float bvh_distance(const BvhView& b, V3 p, float d0, ErrFlag err, u32* visits = nullptr,
+                                              u32* tests = nullptr)
 {
+    u32 nt = 0;
     float dist = d0;
     if (b.n_tris <= 0) return dist;
     int stack[kStack];
@@ -234,6 +236,7 @@ __device__ __forceinline__ float bvh_distance(const BvhView& b, V3 p, float d0, 
             load_tri(b, ~cur, P1, P2, P3, meta, local);
             if (meta & kOccluderBit) {
                 float nd = point_tri_dist(p, P1, P2, P3);
+                ++nt;
                 if (nd < dist) dist = nd;
             }
         }
@@ -247,6 +250,7 @@ __device__ __forceinline__ float bvh_distance(const BvhView& b, V3 p, float d0, 
         cur = stack[sp];
     }
     if (visits) *visits += nv;
+    if (tests) *tests += nt;
     return dist;
 }
 

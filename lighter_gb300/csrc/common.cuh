@@ -159,4 +159,14 @@ HD bool point_proj_on_tri(V3 pt, V3 t0, V3 t1, V3 t2)
 // Reverse-winding unit normal, Triangle::GetNormal (lighter_int.hpp:614-617).
 HD V3 tri_normal_rev(V3 P1, V3 P2, V3 P3) { return normalized(cross(P3 - P1, P2 - P1)); }
 
+// Host-side bookkeeping of one bake (the calling thread's): kernels this
+// library launched and bytes it copied between host and device.
+struct HostCounters {
+    uint64_t launches = 0, h2d = 0, d2h = 0;
+};
+HostCounters& host_counters();
+inline void note_launch() { host_counters().launches++; }
+inline void note_h2d(size_t b) { host_counters().h2d += b; }
+inline void note_d2h(size_t b) { host_counters().d2h += b; }
+
 }  // namespace lg

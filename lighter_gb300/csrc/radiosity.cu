@@ -166,11 +166,11 @@ RadResult solve_t(const RadInputs& in, const RadSettings& rs, const BvhView& bvh
         cudaStream_t st; void* p[9];
         ~Free() { for (void* q : p) if (q) cudaFreeAsync(q, st); }
     } guard{st, {F, pos, nrm, da, out, total, X, Y, counts}};
-    RCK(cudaMemcpyAsync(pos, in.pos.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st));
-    RCK(cudaMemcpyAsync(nrm, in.nrm.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st));
-    RCK(cudaMemcpyAsync(da, in.diff_area.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st));
-    RCK(cudaMemcpyAsync(out, in.emit.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st));
-    RCK(cudaMemcpyAsync(total, in.emit.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st));
+    RCK(cudaMemcpyAsync(pos, in.pos.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st)); note_h2d(n * sizeof(float4));
+    RCK(cudaMemcpyAsync(nrm, in.nrm.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st)); note_h2d(n * sizeof(float4));
+    RCK(cudaMemcpyAsync(da, in.diff_area.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st)); note_h2d(n * sizeof(float4));
+    RCK(cudaMemcpyAsync(out, in.emit.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st)); note_h2d(n * sizeof(float4));
+    RCK(cudaMemcpyAsync(total, in.emit.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st)); note_h2d(n * sizeof(float4));
     RCK(cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned long long), st));
 
     cudaEvent_t e0, e1, e2;
@@ -179,20 +179,20 @@ RadResult solve_t(const RadInputs& in, const RadSettings& rs, const BvhView& bvh
     u32 nb = (n + 31) / 32;
     if (nb > 65535) throw std::runtime_error("radiosity: too many samples for the tile grid");
     dim3 grid(nb, nb), block(32, 8);
-    k_form_factors<T><<<grid, block, 0, st>>>(n, pos, nrm, bvh, err, rs.links, F, counts);
+    k_form_factors<T><<<grid, block, 0, st>>>(n, pos, nrm, bvh, err, rs.links, F, counts); note_launch();
     RCK(cudaGetLastError());
     RCK(cudaEventRecord(e1, st));
     for (int b = 0; b < rs.bounces; ++b) {
         if (abort_flag && abort_flag->load()) break;
-        k_rad_x<<<(n + 255) / 256, 256, 0, st>>>(n, out, da, X);
-        k_rad_gemv<T><<<(unsigned) (((size_t) n * 32 + 255) / 256), 256, 0, st>>>(n, F, X, Y);
-        k_rad_update<<<(n + 255) / 256, 256, 0, st>>>(n, Y, total, out);
+        k_rad_x<<<(n + 255) / 256, 256, 0, st>>>(n, out, da, X); note_launch();
+        k_rad_gemv<T><<<(unsigned) (((size_t) n * 32 + 255) / 256), 256, 0, st>>>(n, F, X, Y); note_launch();
+        k_rad_update<<<(n + 255) / 256, 256, 0, st>>>(n, Y, total, out); note_launch();
         RCK(cudaGetLastError());
     }
     RCK(cudaEventRecord(e2, st));
     RCK(cudaMemcpyAsync(lm_out, total, n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
     unsigned long long hc[2];
-    RCK(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    RCK(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(hc));
     RCK(cudaStreamSynchronize(st));
     float m1 = 0, m2 = 0;
     cudaEventElapsedTime(&m1, e0, e1);

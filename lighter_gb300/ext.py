@@ -17,7 +17,8 @@ class Options(C.Structure):
         ("radiosity_links", C.c_int),
         ("radiosity_precision", C.c_int),
         ("refine_steps", C.c_int),
-        ("reserved", u32 * 11),
+        ("radiosity_patches", u32),
+        ("reserved", u32 * 10),
     ]
 
 
@@ -26,7 +27,8 @@ class Stats(C.Structure):
         "ms_total", "ms_upload", "ms_bvh", "ms_samples", "ms_direct", "ms_rad_links", "ms_rad_bounce", "ms_ao",
         "ms_finalize", "ms_download")] + [(n, C.c_uint64) for n in (
             "texels", "samples", "triangles", "shadow_evals", "distance_queries", "ao_rays", "rad_pairs",
-            "rad_vis_rays", "node_visits")] + [("reserved", C.c_uint64 * 7)]
+            "rad_vis_rays", "node_visits", "tri_tests", "rad_elements", "kernel_launches", "bytes_h2d",
+            "bytes_d2h")] + [("ms_device", C.c_double), ("reserved", C.c_uint64 * 1)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}

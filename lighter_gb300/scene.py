@@ -112,130 +112,148 @@ def _has(lib, name):
         return False
 
 
-def bake(lib, desc: SceneDesc, threads: int = 1, debug: bool = True, poll_s: float = 0.001,
-         timeout_s: float = 3600.0, before_start: Optional[Callable] = None, gpu_options: Optional[dict] = None,
-         stats: Optional[dict] = None) -> BakeResult:
-    """Replay `desc` through `lib`'s C API and return its outputs. For the GPU
-    library, `gpu_options` are ltrg_Options fields and `stats` (a dict) receives
-    ltrg_GetStats; a bake that ends in an error raises RuntimeError."""
+def _populate(lib, scene, desc: SceneDesc, threads: int, keep: list) -> None:
+    """Config, meshes, instances, lights (after srand) and probes of `desc`."""
+    cfg = abi.Config()
+    lib.ltr_GetConfig(C.byref(cfg), scene)
+    for k, v in desc.config.items():
+        if isinstance(v, (tuple, list)):
+            setattr(cfg, k, _vec3(v))
+        else:
+            setattr(cfg, k, v)
+    cfg.max_num_threads = threads
+    if desc.fixed_lm_size is not None:
+        w, h = desc.fixed_lm_size
+
+        def _size(cfgp, mi, mis, ii, iis, area, imp, out):
+            out[0] = w
+            out[1] = h
+            return 1
+        cb = abi.SIZE_FN(_size)
+        keep.append(cb)
+        cfg.size_fn = C.cast(cb, C.c_void_p).value
+    if desc.sample_table is not None:
+        dif, emi = desc.sample_table
+        dif = np.ascontiguousarray(dif, dtype=np.float32)
+        keep.append(dif)
+        tab = abi.SampleTable()
+        tab.count = dif.shape[0]
+        tab.diffuse_rgb = dif.ctypes.data_as(C.POINTER(C.c_float))
+        if emi is not None:
+            emi = np.ascontiguousarray(emi, dtype=np.float32)
+            keep.append(emi)
+            tab.emissive_rgb = emi.ctypes.data_as(C.POINTER(C.c_float))
+        keep.append(tab)
+        cfg.userdata = C.cast(C.pointer(tab), C.c_void_p).value
+        cfg.sample_fn = C.cast(lib.ltrg_TableSampleFn, C.c_void_p).value
+    elif desc.sample_fn_py is not None:
+        fn = desc.sample_fn_py
+
+        def _sample(cfgp, reqp):
+            return 1 if fn(reqp.contents) else 0
+        cb = abi.SAMPLE_FN(_sample)
+        keep.append(cb)
+        cfg.sample_fn = C.cast(cb, C.c_void_p).value
+    lib.ltr_SetConfig(scene, C.byref(cfg))
+
+    mesh_handles = []
+    for m in desc.meshes:
+        ident = m.ident.encode()
+        mh = lib.ltr_CreateMesh(scene, ident, len(ident))
+        mesh_handles.append(mh)
+        for p in m.parts:
+            pos = np.ascontiguousarray(p.positions, dtype=np.float32)
+            nrm = np.ascontiguousarray(p.normals, dtype=np.float32)
+            t1 = np.ascontiguousarray(p.uv1, dtype=np.float32)
+            t2 = np.ascontiguousarray(p.uv2, dtype=np.float32)
+            idx = np.ascontiguousarray(p.indices, dtype=np.uint32)
+            info = abi.MeshPartInfo()
+            info.positions_f3 = pos.ctypes.data
+            info.normals_f3 = nrm.ctypes.data
+            info.texcoords1_f2 = t1.ctypes.data
+            info.texcoords2_f2 = t2.ctypes.data
+            info.stride_positions = 12
+            info.stride_normals = 12
+            info.stride_texcoords1 = 8
+            info.stride_texcoords2 = 8
+            info.indices = idx.ctypes.data_as(C.POINTER(abi.u32))
+            info.vertex_count = pos.shape[0]
+            info.index_count = idx.shape[0]
+            info.shadow = int(p.shadow)
+            if not lib.ltr_MeshAddPart(mh, C.byref(info)):
+                raise RuntimeError(f"ltr_MeshAddPart rejected a part of {m.ident}")
+    for inst in desc.instances:
+        ii = abi.MeshInstanceInfo()
+        mat = np.asarray(inst.matrix, dtype=np.float32).reshape(4, 4)
+        for r in range(4):
+            for c in range(4):
+                ii.matrix[r][c] = float(mat[r, c])
+        ii.importance = inst.importance
+        ii.shadow = inst.shadow
+        ident = inst.ident.encode()
+        keep.append(ident)
+        ii.ident = ident
+        ii.ident_size = len(ident)
+        lib.ltr_MeshAddInstance(mesh_handles[inst.mesh], C.byref(ii))
+
+    srand(desc.seed)
+    for L in desc.lights:
+        li = abi.LightInfo()
+        li.type = L.type
+        li.position = _vec3(L.position)
+        li.direction = _vec3(L.direction)
+        li.up_direction = _vec3(L.up)
+        li.color_rgb = _vec3(L.color)
+        li.range = L.range
+        li.power = L.power
+        li.light_radius = L.light_radius
+        li.shadow_sample_count = L.shadow_sample_count
+        li.spot_angle_out = L.spot_angle_out
+        li.spot_angle_in = L.spot_angle_in
+        li.spot_curve = L.spot_curve
+        lib.ltr_LightAdd(scene, C.byref(li))
+    for (sid, pos, nrm) in desc.probes:
+        si = abi.SampleInfo()
+        si.id = sid
+        si.position = _vec3(pos)
+        si.normal = _vec3(nrm)
+        lib.ltr_SampleAdd(scene, C.byref(si))
+
+
+
+def ingest(lib, desc: SceneDesc, threads: int = 1, gpu_options: Optional[dict] = None, debug: bool = False):
+    """Create a scene and feed `desc` through the C API without starting the
+    bake. Returns (scene handle, keep-alive list); the caller keeps the list
+    alive while the scene exists (it holds ctypes callbacks and buffers) and
+    destroys the scene with ltr_DestroyScene."""
     keep = []
     scene = lib.ltr_CreateScene()
     if not scene:
         raise RuntimeError("ltr_CreateScene returned NULL")
     try:
-        cfg = abi.Config()
-        lib.ltr_GetConfig(C.byref(cfg), scene)
-        for k, v in desc.config.items():
-            if isinstance(v, (tuple, list)):
-                setattr(cfg, k, _vec3(v))
-            else:
-                setattr(cfg, k, v)
-        cfg.max_num_threads = threads
-        if desc.fixed_lm_size is not None:
-            w, h = desc.fixed_lm_size
-
-            def _size(cfgp, mi, mis, ii, iis, area, imp, out):
-                out[0] = w
-                out[1] = h
-                return 1
-            cb = abi.SIZE_FN(_size)
-            keep.append(cb)
-            cfg.size_fn = C.cast(cb, C.c_void_p).value
-        if desc.sample_table is not None:
-            dif, emi = desc.sample_table
-            dif = np.ascontiguousarray(dif, dtype=np.float32)
-            keep.append(dif)
-            tab = abi.SampleTable()
-            tab.count = dif.shape[0]
-            tab.diffuse_rgb = dif.ctypes.data_as(C.POINTER(C.c_float))
-            if emi is not None:
-                emi = np.ascontiguousarray(emi, dtype=np.float32)
-                keep.append(emi)
-                tab.emissive_rgb = emi.ctypes.data_as(C.POINTER(C.c_float))
-            keep.append(tab)
-            cfg.userdata = C.cast(C.pointer(tab), C.c_void_p).value
-            cfg.sample_fn = C.cast(lib.ltrg_TableSampleFn, C.c_void_p).value
-        elif desc.sample_fn_py is not None:
-            fn = desc.sample_fn_py
-
-            def _sample(cfgp, reqp):
-                return 1 if fn(reqp.contents) else 0
-            cb = abi.SAMPLE_FN(_sample)
-            keep.append(cb)
-            cfg.sample_fn = C.cast(cb, C.c_void_p).value
-        lib.ltr_SetConfig(scene, C.byref(cfg))
-
-        mesh_handles = []
-        for m in desc.meshes:
-            ident = m.ident.encode()
-            mh = lib.ltr_CreateMesh(scene, ident, len(ident))
-            mesh_handles.append(mh)
-            for p in m.parts:
-                pos = np.ascontiguousarray(p.positions, dtype=np.float32)
-                nrm = np.ascontiguousarray(p.normals, dtype=np.float32)
-                t1 = np.ascontiguousarray(p.uv1, dtype=np.float32)
-                t2 = np.ascontiguousarray(p.uv2, dtype=np.float32)
-                idx = np.ascontiguousarray(p.indices, dtype=np.uint32)
-                info = abi.MeshPartInfo()
-                info.positions_f3 = pos.ctypes.data
-                info.normals_f3 = nrm.ctypes.data
-                info.texcoords1_f2 = t1.ctypes.data
-                info.texcoords2_f2 = t2.ctypes.data
-                info.stride_positions = 12
-                info.stride_normals = 12
-                info.stride_texcoords1 = 8
-                info.stride_texcoords2 = 8
-                info.indices = idx.ctypes.data_as(C.POINTER(abi.u32))
-                info.vertex_count = pos.shape[0]
-                info.index_count = idx.shape[0]
-                info.shadow = int(p.shadow)
-                if not lib.ltr_MeshAddPart(mh, C.byref(info)):
-                    raise RuntimeError(f"ltr_MeshAddPart rejected a part of {m.ident}")
-        for inst in desc.instances:
-            ii = abi.MeshInstanceInfo()
-            mat = np.asarray(inst.matrix, dtype=np.float32).reshape(4, 4)
-            for r in range(4):
-                for c in range(4):
-                    ii.matrix[r][c] = float(mat[r, c])
-            ii.importance = inst.importance
-            ii.shadow = inst.shadow
-            ident = inst.ident.encode()
-            keep.append(ident)
-            ii.ident = ident
-            ii.ident_size = len(ident)
-            lib.ltr_MeshAddInstance(mesh_handles[inst.mesh], C.byref(ii))
-
-        srand(desc.seed)
-        for L in desc.lights:
-            li = abi.LightInfo()
-            li.type = L.type
-            li.position = _vec3(L.position)
-            li.direction = _vec3(L.direction)
-            li.up_direction = _vec3(L.up)
-            li.color_rgb = _vec3(L.color)
-            li.range = L.range
-            li.power = L.power
-            li.light_radius = L.light_radius
-            li.shadow_sample_count = L.shadow_sample_count
-            li.spot_angle_out = L.spot_angle_out
-            li.spot_angle_in = L.spot_angle_in
-            li.spot_curve = L.spot_curve
-            lib.ltr_LightAdd(scene, C.byref(li))
-        for (sid, pos, nrm) in desc.probes:
-            si = abi.SampleInfo()
-            si.id = sid
-            si.position = _vec3(pos)
-            si.normal = _vec3(nrm)
-            lib.ltr_SampleAdd(scene, C.byref(si))
-
-        is_gpu = _has(lib, "ltrg_SetOptions")
-        if is_gpu:
+        _populate(lib, scene, desc, threads, keep)
+        if _has(lib, "ltrg_SetOptions"):
             from .ext import set_options
             opts = dict(gpu_options or {})
             if debug:
                 opts.setdefault("keep_samples", 1)
             if opts:
                 set_options(lib, scene, **opts)
+    except BaseException:
+        lib.ltr_DestroyScene(scene)
+        raise
+    return scene, keep
+
+
+def bake(lib, desc: SceneDesc, threads: int = 1, debug: bool = True, poll_s: float = 0.001,
+         timeout_s: float = 3600.0, before_start: Optional[Callable] = None, gpu_options: Optional[dict] = None,
+         stats: Optional[dict] = None) -> BakeResult:
+    """Replay `desc` through `lib`'s C API and return its outputs. For the GPU
+    library, `gpu_options` are ltrg_Options fields and `stats` (a dict) receives
+    ltrg_GetStats; a bake that ends in an error raises RuntimeError."""
+    scene, keep = ingest(lib, desc, threads, gpu_options, debug)
+    try:
+        is_gpu = _has(lib, "ltrg_SetOptions")
         if before_start is not None:
             before_start(scene)
         stages = []

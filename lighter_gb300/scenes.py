@@ -82,7 +82,8 @@ def pack_faces(faces, lm_size: int, pad_texels: float = 2.0):
     cell minus `pad_texels` of margin. Returns one (k,2) UV array per face."""
     g = max(1, int(math.ceil(math.sqrt(len(faces)))))
     cell = 1.0 / g
-    pad = pad_texels / lm_size
+    # the margin shrinks to a quarter of the cell when cells get small
+    pad = min(pad_texels, 0.25 * cell * lm_size) / lm_size
     inner = cell - 2 * pad
     if inner <= 0:
         raise ValueError(f"{len(faces)} faces do not fit a {lm_size}^2 lightmap")

@@ -32,6 +32,11 @@ typedef int32_t i32;
 
 namespace orc {
 
+// Work counters of the last bake (shadow evaluations traced, sphere-trace
+// steps, AO segment queries, radiosity visibility tests), for the CPU
+// baseline's rays/s.
+static std::atomic<unsigned long long> g_shadow_evals{0}, g_distance_queries{0}, g_ao_rays{0}, g_rad_vis{0};
+
 // ---------------------------------------------------------------- math (lighter_int.hpp:261-557)
 static const float kSmall = 0.001f;            // SMALL_FLOAT lighter_int.hpp:261
 static const float kMaxPenumbraSize = 2.0f;    // lighter_int.hpp:964
@@ -732,11 +737,13 @@ struct ltr_Scene {
     }
     float inv_shadow(V3 from, V3 to, float k) const   // lighter.cpp:190-207
     {
+        g_shadow_evals.fetch_add(1, std::memory_order_relaxed);
         V3 rd = normalized(to - from);
         float maxt = len(to - from);
         float res = 1.0f;
         for (float t = 0.001f; t < maxt;) {
             float h = distance(from + rd * t);
+            g_distance_queries.fetch_add(1, std::memory_order_relaxed);
             if (h < 0.001f) return 0.0f;
             res = fmin_(res, h / fmin_(t * k, kMaxPenumbraSize));
             h = fmin_(h, kMaxPenumbraStep);
@@ -1069,6 +1076,7 @@ void ltr_Scene::rad_links()
             float l2 = lensq(pd);
             float f = dA * dB / (l2 * l2 * (float) M_PI);
             if (f < kSmall) continue;
+            g_rad_vis.fetch_add(1, std::memory_order_relaxed);
             if (occluded(AP, BP) == false) continue;
             RadLink rl = {(u32) j, f};
             links.push_back(rl);
@@ -1110,6 +1118,7 @@ void ltr_Scene::ao(OInst* mi, const std::vector<float>& randoff)
         for (int s = 0; s < ns; ++s) {
             V3 rd = spiral_dir(SN, randoff[i], s, ns) * dist;
             float hit = closest_tree(ro, ro + rd);
+            g_ao_rays.fetch_add(1, std::memory_order_relaxed);
             if (hit < 1.0f) f += 1.0f - hit;
         }
         f /= ns;
@@ -1369,6 +1378,7 @@ API void ltr_DestroyScene(ltr_Scene* s) { delete s; }
 
 API void ltr_Start(ltr_Scene* s)
 {
+    g_shadow_evals = 0; g_distance_queries = 0; g_ao_rays = 0; g_rad_vis = 0;
     s->stage = "starting";
     s->worker = std::thread([s]() { s->run(); });
 }
@@ -1484,6 +1494,12 @@ API int ltrdbg_GetSamples(ltr_Scene* s, u32 inst, float* pos3, float* nrm3, u32*
     return 1;
 }
 API u32 ltrdbg_RadLinkCount(ltr_Scene* s) { return (u32) s->links.size(); }
+
+// out[0..3] = shadow evaluations, sphere-trace steps, AO rays, radiosity visibility tests
+API void orc_GetCounters(unsigned long long* out)
+{
+    out[0] = g_shadow_evals; out[1] = g_distance_queries; out[2] = g_ao_rays; out[3] = g_rad_vis;
+}
 
 struct ltrg_SampleTable { u32 count; const float* diffuse_rgb; const float* emissive_rgb; };
 API int ltrg_TableSampleFn(ltr_Config* cfg, ltr_SampleRequest* req)
