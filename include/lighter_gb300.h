@@ -89,6 +89,33 @@ typedef struct ltrg_SampleTable {
 } ltrg_SampleTable;
 LTRAPI LTRBOOL ltrg_TableSampleFn(ltr_Config* config, ltr_SampleRequest* req);
 
+/* Lightmap finishing that allocates no device memory. No counterpart in the
+ * reference: it exposes the bake's finalize step (three extrapolating dilation
+ * sweeps, then the separable Gaussian blur; lighter.cpp:880-961) for callers
+ * that cannot call cudaMalloc where they finish a lightmap -- code running
+ * inside a CUDA stream capture, plugins whose host owns all device memory,
+ * per-frame callbacks that must not synchronise the device.
+ *   rgb    device, width*height*3 floats: the scattered sample colours
+ *   mask   device, width*height bytes: nonzero where a sample was written
+ *   out    device, width*height*3 floats: the finished lightmap (may equal rgb)
+ *   stream cudaStream_t to enqueue on (NULL = default stream); the call does
+ *          not wait for the GPU
+ * Limits: width*height <= LTRG_NOALLOC_MAX_TEXELS (1024 x 1024) and
+ * ceil(blur_size) <= 16. The scratch is one static device array of
+ * LTRG_NOALLOC_SCRATCH_BYTES held by every GPU that loads the library until
+ * exit; the first call on a device looks up its address (make that call
+ * before any stream capture). Calls share the scratch: calls that overlap on
+ * the GPU race and must be serialised by the caller.
+ * Returns LTRG_NOALLOC_OK or a negative LTRG_NOALLOC_E* code. */
+#define LTRG_NOALLOC_MAX_TEXELS (1u << 20)
+#define LTRG_NOALLOC_SCRATCH_BYTES (2u * LTRG_NOALLOC_MAX_TEXELS + 12u * LTRG_NOALLOC_MAX_TEXELS)
+#define LTRG_NOALLOC_OK 0
+#define LTRG_NOALLOC_EINVAL (-1)   /* null pointer, zero size or blur_size out of range */
+#define LTRG_NOALLOC_ETOOBIG (-2)  /* width*height above LTRG_NOALLOC_MAX_TEXELS */
+#define LTRG_NOALLOC_ECUDA (-3)    /* no current device, symbol lookup or launch failed */
+LTRAPI int ltrg_FinalizeLightmapNoAlloc(const float* rgb, const unsigned char* mask, float* out, u32 width,
+                                        u32 height, float blur_size, void* stream);
+
 /* Read-only introspection of a finished bake (requires keep_samples = 1).
  * Instance 0 is the probe-sample container of ltr_SampleAdd, as in the
  * reference (lighter_int.hpp:975-980). */

@@ -56,3 +56,9 @@ def get_stats(lib, scene) -> dict:
     s = Stats()
     lib.ltrg_GetStats(scene, C.byref(s))
     return s.as_dict()
+
+# Finalize without device allocation (include/lighter_gb300.h).
+NOALLOC_MAX_TEXELS = 1 << 20
+NOALLOC_OK, NOALLOC_EINVAL, NOALLOC_ETOOBIG, NOALLOC_ECUDA = 0, -1, -2, -3
+EXT_API["ltrg_FinalizeLightmapNoAlloc"] = (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, u32, u32, C.c_float,
+                                                     C.c_void_p])
