@@ -303,13 +303,26 @@ __device__ __forceinline__ float inv_shadow(const BvhView& bvh, V3 from, V3 to, 
     V3 rd = normalized(to - from);
     float maxt = len(to - from);
     float res = 1.0f;
+    // Warm start: the nearest triangle of the previous point lies within
+    // h_prev + step of the next one, so the query starts with that radius
+    // (plus slack for rounding) instead of MAX_PENUMBRA_SIZE. If nothing lies
+    // inside it, the query is repeated with the full radius, so the result is
+    // the reference's min(MAX_PENUMBRA_SIZE, nearest distance) either way.
+    float reach = kMaxPenumbraSize;
     for (float t = 0.001f; t < maxt;) {
-        float h = bvh_distance(bvh, from + rd * t, kMaxPenumbraSize, err, &nv, &nt);
+        V3 p = from + rd * t;
+        float r0 = fminf(kMaxPenumbraSize, reach * 1.0001f + 1e-5f);
+        float h = bvh_distance(bvh, p, r0, err, &nv, &nt);
         ++nq;
+        if (!(h < r0) && r0 < kMaxPenumbraSize) {
+            h = bvh_distance(bvh, p, kMaxPenumbraSize, err, &nv, &nt);
+            ++nq;
+        }
         if (h < 0.001f) return 0.0f;
         res = fmin_(res, h / fmin_(t * k, kMaxPenumbraSize));
-        h = fmin_(h, kMaxPenumbraStep);
-        t += h;
+        float step = fmin_(h, kMaxPenumbraStep);
+        reach = h + step;
+        t += step;
     }
     return res;
 }
@@ -329,61 +342,110 @@ struct DirectArgs {
     Counters* counters;
 };
 
-// One (light, sample) pair of Job_LMRender_{Point,Spot,Direct}_Inner (lighter.cpp:485-600).
-__global__ void k_direct(DirectArgs a)
+// Unshadowed terms of one (light, sample) pair of
+// Job_LMRender_{Point,Spot,Direct}_Inner (lighter.cpp:485-600). Returns
+// whether the pair needs a shadow trace; `from`/`to` are its segment.
+struct LightTerms {
+    float f_dist, f_ndotl, f_dir;
+    V3 dir;   // sample-to-light (point/spot) or light direction (directional)
+    V3 from, to;
+};
+
+__device__ __forceinline__ bool light_terms(const DirectArgs& a, const DLight& L, u32 s, LightTerms& o)
+{
+    V3 SP = ld3(a.spos[s]), SN = ld3(a.snrm[s]);
+    V3 Lpos = mk(L.pos[0], L.pos[1], L.pos[2]);
+    V3 Ldir = mk(L.dir[0], L.dir[1], L.dir[2]);
+    o.f_dir = 1.0f;
+    o.from = SP + SN * kShadowOffset;
+    if (L.type == 1 || L.type == 2) {
+        V3 s2l = Lpos - SP;
+        float dist = len(s2l);
+        if (dist) s2l = s2l / dist;
+        o.f_dist = powf(1 - fmin_(1.0f, dist / L.range), L.power);
+        o.f_ndotl = fmax_(0.0f, dot(s2l, SN));
+        o.dir = s2l;
+        o.to = Lpos;
+        if (L.type == 2) {
+            float ang = acosf(fmin_(1.0f, dot(s2l, -Ldir)));
+            o.f_dir = fmax_(0.0f, fmin_(1.0f, (ang - L.out_rad) / L.diff));
+            o.f_dir = powf(o.f_dir, L.curve);
+            return !(o.f_dist * o.f_ndotl * o.f_dir <= 0);
+        }
+        return !(o.f_dist * o.f_ndotl <= 0);
+    }
+    if (L.type == 3) {
+        o.f_dist = 1.0f;
+        o.f_ndotl = fmax_(0.0f, dot(Ldir, SN));
+        o.dir = Ldir;
+        o.to = SP + Ldir * L.range;
+        // the reference traces even when N.L = 0; its term is then 0 * vis = 0,
+        // so the trace is skipped without changing the result
+        return o.f_ndotl > 0.0f;
+    }
+    return false;
+}
+
+// Pass 1 over every (light, sample) pair: zero the outputs and flag the
+// pairs that need a shadow trace (lit instance, positive unshadowed term).
+__global__ void k_direct_setup(DirectArgs a, u32* __restrict__ flags)
 {
     unsigned long long total = (unsigned long long) a.n_lights * a.n_samples;
-    unsigned long long c_traced = 0, c_nq = 0, c_nv = 0, c_nt = 0;
     for (unsigned long long w = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; w < total;
          w += (unsigned long long) gridDim.x * blockDim.x) {
         int l = (int) (w / a.n_samples);
         u32 s = (u32) (w % a.n_samples);
         const DLight L = a.lights[l];
         u32 inst = a.sinst[s];
-        float kv = 0.0f;
-        float4 nd = make_float4(0, 0, 0, 0);
-        u32 nq = 0, nv = 0, nt = 0, traced = 0;
+        bool go = false;
         if (a.lit[(size_t) l * a.n_inst + inst]) {
-            V3 SP = ld3(a.spos[s]), SN = ld3(a.snrm[s]);
-            V3 Lpos = mk(L.pos[0], L.pos[1], L.pos[2]);
-            V3 Ldir = mk(L.dir[0], L.dir[1], L.dir[2]);
-            V3 Lcol = mk(L.color[0], L.color[1], L.color[2]);
-            if (L.type == 1 || L.type == 2) {
-                V3 s2l = Lpos - SP;
-                float dist = len(s2l);
-                if (dist) s2l = s2l / dist;
-                float f_dist = powf(1 - fmin_(1.0f, dist / L.range), L.power);
-                float f_ndotl = fmax_(0.0f, dot(s2l, SN));
-                float f_dir = 1.0f;
-                bool go;
-                if (L.type == 2) {
-                    float ang = acosf(fmin_(1.0f, dot(s2l, -Ldir)));
-                    f_dir = fmax_(0.0f, fmin_(1.0f, (ang - L.out_rad) / L.diff));
-                    f_dir = powf(f_dir, L.curve);
-                    go = !(f_dist * f_ndotl * f_dir <= 0);
-                } else {
-                    go = !(f_dist * f_ndotl <= 0);
-                }
-                if (go) {
-                    float vis = inv_shadow(a.bvh, SP + SN * kShadowOffset, Lpos, L.radius, a.err, nq, nv, nt);
-                    traced = 1;
-                    kv = L.type == 2 ? f_dist * f_ndotl * f_dir * vis : f_dist * f_ndotl * vis;
-                    float fac = L.type == 2 ? f_dist * f_dir * vis * f_ndotl * brightness(Lcol)
-                                            : f_dist * vis * f_ndotl * brightness(Lcol);
-                    if (fac > 0) nd = st4(s2l * fac, 1.0f);
-                }
-            } else if (L.type == 3) {
-                float f_ndotl = fmax_(0.0f, dot(Ldir, SN));
-                float vis = inv_shadow(a.bvh, SP + SN * kShadowOffset, SP + Ldir * L.range, L.radius, a.err, nq, nv, nt);
-                traced = 1;
-                kv = f_ndotl * vis;
-                float fac = vis * f_ndotl * brightness(Lcol);
-                if (fac > 0) nd = st4(Ldir * fac, 1.0f);
-            }
+            LightTerms t;
+            go = light_terms(a, L, s, t);
+        }
+        a.kval[w] = 0.0f;
+        if (a.ndir) a.ndir[w] = make_float4(0, 0, 0, 0);
+        flags[w] = go ? 1u : 0u;
+    }
+}
+
+__global__ void k_direct_compact(unsigned long long total, const u32* __restrict__ flags, const u32* __restrict__ scan,
+                                 u32* __restrict__ items)
+{
+    for (unsigned long long w = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; w < total;
+         w += (unsigned long long) gridDim.x * blockDim.x)
+        if (flags[w]) items[scan[w]] = (u32) w;
+}
+
+// Pass 2: persistent threads over the compacted pairs; a thread takes the
+// next pair as soon as its sphere trace ends, so trace lengths that differ by
+// orders of magnitude do not idle the other lanes of its warp.
+__global__ void k_direct_trace(DirectArgs a, const u32* __restrict__ items, u32 n_items, u32* __restrict__ next)
+{
+    unsigned long long c_traced = 0, c_nq = 0, c_nv = 0, c_nt = 0;
+    for (u32 i = atomicAdd(next, 1u); i < n_items; i = atomicAdd(next, 1u)) {
+        u32 w = items[i];
+        int l = (int) (w / a.n_samples);
+        u32 s = w % a.n_samples;
+        const DLight L = a.lights[l];
+        LightTerms t;
+        light_terms(a, L, s, t);
+        u32 nq = 0, nv = 0, nt = 0;
+        float vis = inv_shadow(a.bvh, t.from, t.to, L.radius, a.err, nq, nv, nt);
+        V3 Lcol = mk(L.color[0], L.color[1], L.color[2]);
+        float kv, fac;
+        if (L.type == 2) {
+            kv = t.f_dist * t.f_ndotl * t.f_dir * vis;
+            fac = t.f_dist * t.f_dir * vis * t.f_ndotl * brightness(Lcol);
+        } else if (L.type == 1) {
+            kv = t.f_dist * t.f_ndotl * vis;
+            fac = t.f_dist * vis * t.f_ndotl * brightness(Lcol);
+        } else {
+            kv = t.f_ndotl * vis;
+            fac = vis * t.f_ndotl * brightness(Lcol);
         }
         a.kval[w] = kv;
-        if (a.ndir) a.ndir[w] = (inst == 0) ? make_float4(0, 0, 0, 0) : nd;
-        c_traced += traced;
+        if (a.ndir && a.sinst[s] != 0 && fac > 0) a.ndir[w] = st4(t.dir * fac, 1.0f);
+        c_traced += 1;
         c_nq += nq;
         c_nv += nv;
         c_nt += nt;
@@ -764,6 +826,105 @@ void prexform(ltr_Scene* S, HostInst* mi)
     }
 }
 
+// ---- leaf references for the BVH
+//
+// A triangle much larger than the scene's typical triangle (a 200 m ground
+// quad) gives every BVH node above it a scene-sized box, so nearly every
+// query descends there. Such triangles are split into several leaf
+// references: the triangle is clipped (Sutherland-Hodgman) against recursive
+// midpoint splits of its box until the pieces are no longer than `limit`, and
+// each reference keeps the whole triangle with the clipped piece's box.
+
+struct ClipPoly {
+    V3 v[24];
+    int n = 0;
+};
+
+inline float axis_of(V3 p, int a) { return a == 0 ? p.x : (a == 1 ? p.y : p.z); }
+
+void clip_half(const ClipPoly& in, int axis, float c, bool below, ClipPoly& out)
+{
+    out.n = 0;
+    for (int i = 0; i < in.n; ++i) {
+        V3 a = in.v[i], b = in.v[(i + 1) % in.n];
+        float da = axis_of(a, axis) - c, db = axis_of(b, axis) - c;
+        bool ia = below ? da <= 0 : da >= 0, ib = below ? db <= 0 : db >= 0;
+        if (ia && out.n < 24) out.v[out.n++] = a;
+        if (ia != ib && out.n < 24) {
+            float t = da / (da - db);
+            V3 p = a + (b - a) * t;
+            // pin the cut coordinate on the plane
+            if (axis == 0) p.x = c; else if (axis == 1) p.y = c; else p.z = c;
+            out.v[out.n++] = p;
+        }
+    }
+}
+
+void split_ref(const ClipPoly& p, float limit, int depth, u32 tri, std::vector<u32>& ref_tri, std::vector<float>& ref_box)
+{
+    V3 mn = splat(FLT_MAX), mx = splat(-FLT_MAX);
+    for (int i = 0; i < p.n; ++i) { mn = vmin(mn, p.v[i]); mx = vmax(mx, p.v[i]); }
+    V3 e = mx - mn;
+    int axis = (e.x >= e.y && e.x >= e.z) ? 0 : (e.y >= e.z ? 1 : 2);
+    float ext = axis_of(e, axis);
+    if (ext <= limit || depth >= 12 || p.n < 3) {
+        ref_tri.push_back(tri);
+        ref_box.insert(ref_box.end(), {mn.x, mn.y, mn.z, mx.x, mx.y, mx.z});
+        return;
+    }
+    float c = (axis_of(mn, axis) + axis_of(mx, axis)) * 0.5f;
+    ClipPoly lo, hi;
+    clip_half(p, axis, c, true, lo);
+    clip_half(p, axis, c, false, hi);
+    if (lo.n) split_ref(lo, limit, depth + 1, tri, ref_tri, ref_box);
+    if (hi.n) split_ref(hi, limit, depth + 1, tri, ref_tri, ref_box);
+}
+
+// References for all triangles; the split limit is four times the median
+// triangle extent (and at least 1/512 of the scene).
+void build_refs(const std::vector<float>& xyz, std::vector<u32>& ref_tri, std::vector<float>& ref_box, float* cmin,
+                float* cmax)
+{
+    const size_t n = xyz.size() / 9;
+    std::vector<float> ext(n);
+    V3 smn = splat(FLT_MAX), smx = splat(-FLT_MAX);
+    for (size_t i = 0; i < n; ++i) {
+        const float* q = &xyz[9 * i];
+        V3 a = mk(q[0], q[1], q[2]), b = mk(q[3], q[4], q[5]), c = mk(q[6], q[7], q[8]);
+        V3 mn = vmin(a, vmin(b, c)), mx = vmax(a, vmax(b, c)), e = mx - mn;
+        ext[i] = fmax_(e.x, fmax_(e.y, e.z));
+        smn = vmin(smn, mn);
+        smx = vmax(smx, mx);
+    }
+    float limit = FLT_MAX;
+    if (n) {
+        std::vector<float> tmp(ext);
+        std::nth_element(tmp.begin(), tmp.begin() + n / 2, tmp.end());
+        V3 se = smx - smn;
+        limit = fmax_(4.0f * tmp[n / 2], fmax_(se.x, fmax_(se.y, se.z)) / 512.0f);
+    }
+    ref_tri.clear();
+    ref_box.clear();
+    ref_tri.reserve(n);
+    ref_box.reserve(6 * n);
+    for (size_t i = 0; i < n; ++i) {
+        const float* q = &xyz[9 * i];
+        ClipPoly p;
+        p.n = 3;
+        p.v[0] = mk(q[0], q[1], q[2]);
+        p.v[1] = mk(q[3], q[4], q[5]);
+        p.v[2] = mk(q[6], q[7], q[8]);
+        split_ref(p, limit, 0, (u32) i, ref_tri, ref_box);
+    }
+    for (int c = 0; c < 3; ++c) { cmin[c] = FLT_MAX; cmax[c] = -FLT_MAX; }
+    for (size_t r = 0; r < ref_tri.size(); ++r)
+        for (int c = 0; c < 3; ++c) {
+            float m = (ref_box[6 * r + c] + ref_box[6 * r + 3 + c]) * 0.5f;
+            cmin[c] = fminf(cmin[c], m);
+            cmax[c] = fmaxf(cmax[c], m);
+        }
+}
+
 // Gaussian taps (Generate_Gaussian_Kernel, lighter_math.cpp:357-365), on the
 // host so the weights are the reference's glibc values.
 std::vector<float> gauss_taps(int ext, float radius)
@@ -1020,8 +1181,15 @@ void run_bake(ltr_Scene* S)
     bin.tri_xyz = d_tri_xyz;
     bin.tri_meta = d_tri_meta;
     bin.tri_local = d_tri_local;
-    bin.n = n_tris;
-    for (int c = 0; c < 3; ++c) { bin.scene_min[c] = n_tris ? smin[c] : 0; bin.scene_max[c] = n_tris ? smax[c] : 0; }
+    std::vector<u32> ref_tri;
+    std::vector<float> ref_box;
+    float rmin[3], rmax[3];
+    build_refs(tri_xyz, ref_tri, ref_box, rmin, rmax);
+    bin.ref_tri = A.upload(ref_tri);
+    bin.ref_box = A.upload(ref_box);
+    bin.n = (int) ref_tri.size();
+    for (int c = 0; c < 3; ++c) { bin.scene_min[c] = bin.n ? rmin[c] : 0; bin.scene_max[c] = bin.n ? rmax[c] : 0; }
+    S->stats.reserved[0] = (uint64_t) bin.n;   // leaf references
     bvh_build(bin, bvh, st);
     struct BvhGuard { BvhStorage* b; cudaStream_t s; ~BvhGuard() { bvh_free(*b, s); } } bvh_guard{&bvh, st};
     BvhView bv = bvh.view();
@@ -1157,8 +1325,32 @@ void run_bake(ltr_Scene* S)
         da.ndir = d_ndir;
         da.counters = d_cnt;
         unsigned long long items = (unsigned long long) n_lights * n_samples;
-        k_direct<<<blocks_for(items, 128, 152ull * 256), 128, 0, st>>>(da); note_launch();
+        if (items >= 0xffffffffull) throw std::runtime_error("too many (light, sample) pairs for one bake");
+        u32* d_dflags = A.alloc<u32>(items + 1);
+        u32* d_dscan = A.alloc<u32>(items + 1);
+        CK(cudaMemsetAsync(d_dflags + items, 0, sizeof(u32), st));
+        k_direct_setup<<<blocks_for(items), kThreads, 0, st>>>(da, d_dflags); note_launch();
         CK(cudaGetLastError());
+        size_t tb = 0;
+        CK(cub::DeviceScan::ExclusiveSum(nullptr, tb, d_dflags, d_dscan, (int64_t) (items + 1), st));
+        void* tmp = A.alloc<char>(tb);
+        CK(cub::DeviceScan::ExclusiveSum(tmp, tb, d_dflags, d_dscan, (int64_t) (items + 1), st));
+        u32 n_trace = 0;
+        CK(cudaMemcpyAsync(&n_trace, d_dscan + items, sizeof(u32), cudaMemcpyDeviceToHost, st)); note_d2h(4);
+        u32* d_items = A.alloc<u32>(items);
+        k_direct_compact<<<blocks_for(items), kThreads, 0, st>>>(items, d_dflags, d_dscan, d_items); note_launch();
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(st));
+        if (n_trace) {
+            u32* d_next = A.zeros<u32>(1);
+            int dev_sms = 0;
+            CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, S->opt.device));
+            // persistent grid: a few blocks per SM, capped by the work
+            unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * 8,
+                                                                    (n_trace + 127) / 128);
+            k_direct_trace<<<grid, 128, 0, st>>>(da, d_items, n_trace, d_next); note_launch();
+            CK(cudaGetLastError());
+        }
     }
     if (n_samples) {
         k_accumulate<<<(n_samples + kThreads - 1) / kThreads, kThreads, 0, st>>>(

@@ -12,6 +12,9 @@
 //      computes its box (atomic arrival counters);
 //   5. packing into 64-byte nodes that hold both child boxes, and
 //      triangles reordered into leaf order.
+// Leaves are triangle references: an oversized triangle may be split (on the
+// host, bake.cu) into several references with clipped boxes, each holding the
+// whole triangle, so every query still tests the original triangle.
 #include <cuda_runtime.h>
 #include <cub/cub.cuh>
 
@@ -40,14 +43,12 @@ __device__ __forceinline__ u32 spread10(u32 v)
     return v;
 }
 
-__global__ void k_morton(const float* xyz, int n, float3 mn, float3 inv_ext, u32* codes, u32* ids)
+__global__ void k_morton(const float* ref_box, int n, float3 mn, float3 inv_ext, u32* codes, u32* ids)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float* p = xyz + 9 * (size_t) i;
-    float cx = (p[0] + p[3] + p[6]) * (1.0f / 3.0f);
-    float cy = (p[1] + p[4] + p[7]) * (1.0f / 3.0f);
-    float cz = (p[2] + p[5] + p[8]) * (1.0f / 3.0f);
+    const float* b = ref_box + 6 * (size_t) i;
+    float cx = (b[0] + b[3]) * 0.5f, cy = (b[1] + b[4]) * 0.5f, cz = (b[2] + b[5]) * 0.5f;
     float qx = fminf(fmaxf((cx - mn.x) * inv_ext.x * 1024.0f, 0.0f), 1023.0f);
     float qy = fminf(fmaxf((cy - mn.y) * inv_ext.y * 1024.0f, 0.0f), 1023.0f);
     float qz = fminf(fmaxf((cz - mn.z) * inv_ext.z * 1024.0f, 0.0f), 1023.0f);
@@ -91,12 +92,11 @@ __global__ void k_hierarchy(const u32* codes, int n, int* left, int* right, int*
     if (rc < 0) parent_leaf[~rc] = i; else parent_int[rc] = i;
 }
 
-// Conservative box of a triangle: a few tens of ulps of slack absorb the
-// rounding of the exact hit and distance tests.
-__device__ __forceinline__ void tri_box(const float* p, float* b)
+// Conservative leaf box: the reference's box widened by a few tens of ulps,
+// which absorbs the rounding of the exact hit and distance tests.
+__device__ __forceinline__ void leaf_box_of(const float* r, float* b)
 {
-    float mnx = fminf(p[0], fminf(p[3], p[6])), mny = fminf(p[1], fminf(p[4], p[7])), mnz = fminf(p[2], fminf(p[5], p[8]));
-    float mxx = fmaxf(p[0], fmaxf(p[3], p[6])), mxy = fmaxf(p[1], fmaxf(p[4], p[7])), mxz = fmaxf(p[2], fmaxf(p[5], p[8]));
+    float mnx = r[0], mny = r[1], mnz = r[2], mxx = r[3], mxy = r[4], mxz = r[5];
     float m = fmaxf(fmaxf(fmaxf(fabsf(mnx), fabsf(mxx)), fmaxf(fabsf(mny), fabsf(mxy))), fmaxf(fabsf(mnz), fabsf(mxz)));
     float e = m * 2e-5f + 1e-6f;
     b[0] = mnx - e; b[1] = mny - e; b[2] = mnz - e;
@@ -108,13 +108,13 @@ __device__ __forceinline__ void read_box(const float* boxes, int k, float* b)
     for (int c = 0; c < 6; ++c) b[c] = __ldcg(boxes + 6 * (size_t) k + c);
 }
 
-__global__ void k_refit(const float* xyz, const u32* ids, int n, const int* parent_leaf, const int* parent_int,
+__global__ void k_refit(const float* ref_box, const u32* ids, int n, const int* parent_leaf, const int* parent_int,
                         const int* left, const int* right, float* leaf_box, float* int_box, u32* arrivals)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float b[6];
-    tri_box(xyz + 9 * (size_t) ids[i], b);
+    leaf_box_of(ref_box + 6 * (size_t) ids[i], b);
     for (int c = 0; c < 6; ++c) leaf_box[6 * (size_t) i + c] = b[c];
     __threadfence();
     int p = n > 1 ? parent_leaf[i] : -1;
@@ -149,11 +149,12 @@ __global__ void k_pack_nodes(int n_int, const int* left, const int* right, const
     o[3] = make_float4(__int_as_float(l), __int_as_float(r), 0.0f, 0.0f);
 }
 
-__global__ void k_pack_tris(int n, const u32* ids, const float* xyz, const u32* meta, const u32* local, float4* tris)
+__global__ void k_pack_tris(int n, const u32* ids, const u32* ref_tri, const float* xyz, const u32* meta, const u32* local,
+                            float4* tris)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    u32 s = ids[i];
+    u32 s = ref_tri[ids[i]];
     const float* p = xyz + 9 * (size_t) s;
     tris[3 * (size_t) i + 0] = make_float4(p[0], p[1], p[2], __uint_as_float(meta[s]));
     tris[3 * (size_t) i + 1] = make_float4(p[3], p[4], p[5], __uint_as_float(local[s]));
@@ -199,7 +200,7 @@ void bvh_build(const BvhBuildInput& in, BvhStorage& out, void* stream)
     float3 mn = make_float3(in.scene_min[0], in.scene_min[1], in.scene_min[2]);
     float ex = in.scene_max[0] - in.scene_min[0], ey = in.scene_max[1] - in.scene_min[1], ez = in.scene_max[2] - in.scene_min[2];
     float3 inv_ext = make_float3(ex > 0 ? 1.0f / ex : 0.0f, ey > 0 ? 1.0f / ey : 0.0f, ez > 0 ? 1.0f / ez : 0.0f);
-    k_morton<<<(n + B - 1) / B, B, 0, st>>>(in.tri_xyz, n, mn, inv_ext, codes, ids); note_launch();
+    k_morton<<<(n + B - 1) / B, B, 0, st>>>(in.ref_box, n, mn, inv_ext, codes, ids); note_launch();
     BVH_CHECK(cudaGetLastError());
 
     size_t temp_bytes = 0;
@@ -213,7 +214,7 @@ void bvh_build(const BvhBuildInput& in, BvhStorage& out, void* stream)
         k_hierarchy<<<(n_int + B - 1) / B, B, 0, st>>>(codes2, n, left, right, parent_int, parent_leaf); note_launch();
         BVH_CHECK(cudaGetLastError());
     }
-    k_refit<<<(n + B - 1) / B, B, 0, st>>>(in.tri_xyz, ids2, n, parent_leaf, parent_int, left, right, leaf_box, int_box,
+    k_refit<<<(n + B - 1) / B, B, 0, st>>>(in.ref_box, ids2, n, parent_leaf, parent_int, left, right, leaf_box, int_box,
                                             arrivals); note_launch();
     BVH_CHECK(cudaGetLastError());
 
@@ -223,7 +224,8 @@ void bvh_build(const BvhBuildInput& in, BvhStorage& out, void* stream)
         k_pack_nodes<<<(n_int + B - 1) / B, B, 0, st>>>(n_int, left, right, leaf_box, int_box, out.nodes); note_launch();
         BVH_CHECK(cudaGetLastError());
     }
-    k_pack_tris<<<(n + B - 1) / B, B, 0, st>>>(n, ids2, in.tri_xyz, in.tri_meta, in.tri_local, out.tris); note_launch();
+    k_pack_tris<<<(n + B - 1) / B, B, 0, st>>>(n, ids2, in.ref_tri, in.tri_xyz, in.tri_meta, in.tri_local,
+                                                out.tris); note_launch();
     BVH_CHECK(cudaGetLastError());
 
     void* ptrs[] = {codes, codes2, ids, ids2, left, right, parent_int, parent_leaf, leaf_box, int_box, arrivals, temp};

@@ -8,7 +8,7 @@
 //           n0 = (L.min.xyz, L.max.x)  n1 = (L.max.yz, R.min.xy)
 //           n2 = (R.min.z, R.max.xyz)  n3 = (int L, int R, -, -)
 //           child >= 0: internal node; child < 0: leaf holding triangle ~child.
-//   tris  : 3 x float4 per triangle in leaf order:
+//   tris  : 3 x float4 per leaf (triangle reference) in leaf order:
 //           (P1.xyz, meta) (P2.xyz, local index) (P3.xyz, build index)
 //           meta = instance index (bits 0-29) | occluder flag (bit 31).
 // Child boxes are inflated by a few ulps at build time, so the slab and
@@ -302,8 +302,10 @@ struct BvhBuildInput {
     const float* tri_xyz;   // device: 9 floats per triangle (P1, P2, P3)
     const u32* tri_meta;    // device: instance | occluder bit
     const u32* tri_local;   // device: index within its instance
-    int n;
-    float scene_min[3], scene_max[3];   // centroid bounds
+    const u32* ref_tri;     // device: triangle of each leaf reference
+    const float* ref_box;   // device: exact box of each reference (min xyz, max xyz)
+    int n;                  // number of references (leaves)
+    float scene_min[3], scene_max[3];   // bounds of the reference box centres
 };
 
 struct BvhStorage {
