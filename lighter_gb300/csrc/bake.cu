@@ -419,9 +419,11 @@ __global__ void k_direct_compact(unsigned long long total, const u32* __restrict
 // Pass 2: persistent threads over the compacted pairs; a thread takes the
 // next pair as soon as its sphere trace ends, so trace lengths that differ by
 // orders of magnitude do not idle the other lanes of its warp.
-__global__ void k_direct_trace(DirectArgs a, const u32* __restrict__ items, u32 n_items, u32* __restrict__ next)
+__global__ void k_direct_trace(DirectArgs a, const u32* __restrict__ items, const u32* __restrict__ n_items_dev,
+                               u32* __restrict__ next)
 {
     unsigned long long c_traced = 0, c_nq = 0, c_nv = 0, c_nt = 0;
+    const u32 n_items = *n_items_dev;
     for (u32 i = atomicAdd(next, 1u); i < n_items; i = atomicAdd(next, 1u)) {
         u32 w = items[i];
         int l = (int) (w / a.n_samples);
@@ -472,6 +474,77 @@ __global__ void k_accumulate(u32 n_samples, int n_lights, const DLight* __restri
     lm[s] = st4(c, 0.0f);
 }
 
+// ----------------------------------------------------------------------------- radiosity inputs
+
+// One radiosity element per sample (lighter.cpp:676-718): unit normal,
+// sample_fn albedo and the sample's area (0 and black for probes), emission =
+// lit colour + sample_fn emission.
+__global__ void k_rad_sample_inputs(u32 n, const float4* __restrict__ spos, const float4* __restrict__ snrm,
+                                    const float4* __restrict__ srad, const u32* __restrict__ sinst,
+                                    const float4* __restrict__ diff, const float4* __restrict__ emis,
+                                    const float4* __restrict__ lm, float4* __restrict__ pos, float4* __restrict__ nrm,
+                                    float4* __restrict__ da, float4* __restrict__ emit)
+{
+    u32 s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    pos[s] = spos[s];
+    nrm[s] = st4(normalized(ld3(snrm[s])), 0.0f);
+    float4 d = diff[s];
+    da[s] = make_float4(d.x, d.y, d.z, sinst[s] == 0 ? 0.0f : srad[s].w);
+    V3 e = ld3(lm[s]);
+    e += ld3(emis[s]);
+    emit[s] = st4(e, 0.0f);
+}
+
+// Patch element from its samples (in sample order): total area and
+// area-weighted position, normal, albedo and emission, accumulated in FP64.
+__global__ void k_patch_inputs(u32 np, const u32* __restrict__ off, const u32* __restrict__ idx,
+                               const float4* __restrict__ spos, const float4* __restrict__ snrm,
+                               const float4* __restrict__ srad, const float4* __restrict__ diff,
+                               const float4* __restrict__ emis, const float4* __restrict__ lm, float4* __restrict__ ppos,
+                               float4* __restrict__ pnrm, float4* __restrict__ pda, float4* __restrict__ pemit)
+{
+    u32 p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    double q[13] = {0};
+    for (u32 k = off[p]; k < off[p + 1]; ++k) {
+        u32 s = idx[k];
+        double a = srad[s].w;
+        V3 n = normalized(ld3(snrm[s]));
+        float4 P = spos[s], D = diff[s];
+        V3 e = ld3(lm[s]);
+        e += ld3(emis[s]);
+        q[0] += a;
+        q[1] += a * P.x; q[2] += a * P.y; q[3] += a * P.z;
+        q[4] += a * n.x; q[5] += a * n.y; q[6] += a * n.z;
+        q[7] += a * D.x; q[8] += a * D.y; q[9] += a * D.z;
+        q[10] += a * e.x; q[11] += a * e.y; q[12] += a * e.z;
+    }
+    double a = q[0] > 0 ? q[0] : 1.0;
+    V3 nn = normalized(mk((float) (q[4] / a), (float) (q[5] / a), (float) (q[6] / a)));
+    ppos[p] = make_float4((float) (q[1] / a), (float) (q[2] / a), (float) (q[3] / a), 0);
+    pnrm[p] = st4(nn, 0.0f);
+    pda[p] = make_float4((float) (q[7] / a), (float) (q[8] / a), (float) (q[9] / a), (float) q[0]);
+    pemit[p] = make_float4((float) (q[10] / a), (float) (q[11] / a), (float) (q[12] / a), 0);
+}
+
+// Texel colour = its own emission + its patch's gathered light.
+__global__ void k_patch_apply(u32 n, const int* __restrict__ patch_of, const float4* __restrict__ emis,
+                              const float4* __restrict__ ptot, const float4* __restrict__ pemit, float4* lm)
+{
+    u32 s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    V3 e = ld3(lm[s]);
+    e += ld3(emis[s]);
+    int p = patch_of[s];
+    if (p >= 0) {
+        e.x += ptot[p].x - pemit[p].x;
+        e.y += ptot[p].y - pemit[p].y;
+        e.z += ptot[p].z - pemit[p].z;
+    }
+    lm[s] = st4(e, 0.0f);
+}
+
 // ----------------------------------------------------------------------------- ambient occlusion
 
 __device__ __forceinline__ V3 spiral_dir(V3 dir, float randoff, int i, int count)
@@ -501,34 +574,60 @@ struct AoArgs {
     Counters* counters;
 };
 
-// Job_AORender_Inner (lighter.cpp:799-841): one warp per sample, one lane per
-// ray; the hit fractions are summed in ray order like the reference loop.
-__global__ void k_ao(AoArgs a)
+// Job_AORender_Inner (lighter.cpp:799-841), pass 1: every (sample, ray) is an
+// independent closest-hit query; persistent threads take rays one at a time
+// (consecutive rays of a sample share an origin) and store the hit fraction.
+// Work fetch for persistent threads: the lanes of a warp that ask together
+// share one atomic; each gets `chunk` consecutive items.
+__device__ __forceinline__ unsigned long long warp_fetch(unsigned long long* ctr, unsigned chunk)
 {
-    const int lane = threadIdx.x & 31;
-    const unsigned long long warp = (blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x) >> 5;
-    const unsigned long long nwarps = ((unsigned long long) gridDim.x * blockDim.x) >> 5;
-    for (unsigned long long s = warp; s < a.n_samples; s += nwarps) {
+    unsigned mask = __activemask();
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(mask) - 1;
+    unsigned rank = __popc(mask & ((1u << lane) - 1u));
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(ctr, (unsigned long long) __popc(mask) * chunk);
+    base = __shfl_sync(mask, base, leader);
+    return base + (unsigned long long) rank * chunk;
+}
+
+constexpr unsigned kAoChunk = 4;
+
+__global__ void k_ao_rays(AoArgs a, float* __restrict__ hits, unsigned long long n_rays, unsigned long long* next)
+{
+    unsigned long long c_rays = 0;
+    for (;;) {
+        unsigned long long i0 = warp_fetch(next, kAoChunk);
+        if (i0 >= n_rays) break;
+        unsigned long long i1 = i0 + kAoChunk < n_rays ? i0 + kAoChunk : n_rays;
+        for (unsigned long long i = i0; i < i1; ++i) {
+        u32 s = (u32) (i / a.ns);
+        int r = (int) (i % a.ns);
         V3 SP = ld3(a.spos[s]), SN = ld3(a.snrm[s]);
         V3 ro = SP + SN * (kSmall * 2);
-        float ro_off = a.randoff[s];
-        float f = 0;
-        for (int c = 0; c < a.ns; c += 32) {
-            int r = c + lane;
-            float hit = kNoHit;
-            if (r < a.ns) {
-                V3 rd = spiral_dir(SN, ro_off, r, a.ns) * a.dist;
-                V3 B = ro + rd;
-                V3 dn = normalized(B - ro);
-                hit = bvh_closest(a.bvh, ro + dn * kSmall, B - dn * kSmall, a.err, nullptr);
-            }
-            int m = min(32, a.ns - c);
-            for (int k = 0; k < m; ++k) {
-                float v = __shfl_sync(0xffffffffu, hit, k);
-                if (v < 1.0f) f += 1.0f - v;
-            }
+        V3 rd = spiral_dir(SN, a.randoff[s], r, a.ns) * a.dist;
+        V3 B = ro + rd;
+        V3 dn = normalized(B - ro);
+        hits[i] = bvh_closest(a.bvh, ro + dn * kSmall, B - dn * kSmall, a.err, nullptr);
+        ++c_rays;
         }
-        if (lane == 0) {
+    }
+    if (a.counters) warp_add(&a.counters->ao_rays, c_rays);
+}
+
+// Pass 2: per sample, the hit fractions summed in ray order like the
+// reference loop, then the AO factor and colour blend.
+__global__ void k_ao(AoArgs a, const float* __restrict__ hits)
+{
+    for (unsigned long long s = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; s < a.n_samples;
+         s += (unsigned long long) gridDim.x * blockDim.x) {
+        const float* h = hits + s * (unsigned long long) a.ns;
+        float f = 0;
+        for (int r = 0; r < a.ns; ++r) {
+            float v = h[r];
+            if (v < 1.0f) f += 1.0f - v;
+        }
+        {
             f /= a.ns;
             f = fmin_(f * a.mult, 1.0f);
             if (a.falloff) f = powf(f, a.falloff);
@@ -537,7 +636,6 @@ __global__ void k_ao(AoArgs a)
             if (a.effect >= 0) out = out * (1 - f * (1 - a.effect)) + aoc * f;
             else out = lerp3(out, lerp3(aoc, aoc * out, -a.effect), f);
             a.lm[s] = st4(out, 0.0f);
-            if (a.counters) atomicAdd(&a.counters->ao_rays, (unsigned long long) a.ns);
         }
     }
 }
@@ -1335,22 +1433,17 @@ void run_bake(ltr_Scene* S)
         CK(cub::DeviceScan::ExclusiveSum(nullptr, tb, d_dflags, d_dscan, (int64_t) (items + 1), st));
         void* tmp = A.alloc<char>(tb);
         CK(cub::DeviceScan::ExclusiveSum(tmp, tb, d_dflags, d_dscan, (int64_t) (items + 1), st));
-        u32 n_trace = 0;
-        CK(cudaMemcpyAsync(&n_trace, d_dscan + items, sizeof(u32), cudaMemcpyDeviceToHost, st)); note_d2h(4);
         u32* d_items = A.alloc<u32>(items);
         k_direct_compact<<<blocks_for(items), kThreads, 0, st>>>(items, d_dflags, d_dscan, d_items); note_launch();
         CK(cudaGetLastError());
-        CK(cudaStreamSynchronize(st));
-        if (n_trace) {
-            u32* d_next = A.zeros<u32>(1);
-            int dev_sms = 0;
-            CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, S->opt.device));
-            // persistent grid: a few blocks per SM, capped by the work
-            unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * 8,
-                                                                    (n_trace + 127) / 128);
-            k_direct_trace<<<grid, 128, 0, st>>>(da, d_items, n_trace, d_next); note_launch();
-            CK(cudaGetLastError());
-        }
+        // persistent grid of a few blocks per SM; the number of traced pairs
+        // stays on the device (scan total), so the host does not wait here
+        u32* d_next = A.zeros<u32>(1);
+        int dev_sms = 0;
+        CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, S->opt.device));
+        unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * 8, (items + 127) / 128);
+        k_direct_trace<<<grid, 128, 0, st>>>(da, d_items, d_dscan + items, d_next); note_launch();
+        CK(cudaGetLastError());
     }
     if (n_samples) {
         k_accumulate<<<(n_samples + kThreads - 1) / kThreads, kThreads, 0, st>>>(
@@ -1358,39 +1451,50 @@ void run_bake(ltr_Scene* S)
         CK(cudaGetLastError());
     }
     cudaEvent_t e_direct = clock.mark();
+
+    // Copies on a side stream overlap the direct-light kernels: the sample
+    // arrays the host needs for sample_fn and patch grouping are final once
+    // the sample stage has ended (event e_samples).
+    cudaStream_t st2 = nullptr;
+    CK(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
+    struct StreamGuard {
+        cudaStream_t s;
+        ~StreamGuard() { cudaStreamSynchronize(s); cudaStreamDestroy(s); }
+    } st2_guard{st2};
+    const bool do_rad = cfg.bounce_count && n_samples;
+    std::vector<float4> hpos, hnrm, hrad;
+    std::vector<u32> hloc;
+    if (do_rad) {
+        hpos.resize(n_samples); hnrm.resize(n_samples); hrad.resize(n_samples); hloc.resize(n_samples);
+        CK(cudaStreamWaitEvent(st2, e_samples, 0));
+        CK(cudaMemcpyAsync(hpos.data(), d_spos, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st2)); note_d2h(n_samples * sizeof(float4));
+        CK(cudaMemcpyAsync(hnrm.data(), d_snrm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st2)); note_d2h(n_samples * sizeof(float4));
+        CK(cudaMemcpyAsync(hrad.data(), d_srad, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st2)); note_d2h(n_samples * sizeof(float4));
+        CK(cudaMemcpyAsync(hloc.data(), d_sloc, n_samples * sizeof(u32), cudaMemcpyDeviceToHost, st2)); note_d2h(n_samples * sizeof(u32));
+    }
     check_abort(S);
 
     // ---- radiosity (Int_RDGenLinks + Int_RDBounce)
+    // The host part (sample_fn per sample, patch grouping) runs while the
+    // direct-light kernels are still tracing: the sample arrays it needs were
+    // copied on the side stream as soon as the sample stage ended.
     cudaEvent_t e_rad_links = e_direct, e_rad_bounce = e_direct;
-    if (cfg.bounce_count && n_samples) {
+    std::vector<float> ao_randoff;
+    const bool do_ao = cfg.ao_distance && n_samples && cfg.ao_num_samples > 0;
+    if (do_rad) {
         S->stage = "calculating radiosity";
-        // host side of the sample gathering: sample_fn per sample, in order
-        std::vector<float4> hpos(n_samples), hnrm(n_samples), hrad(n_samples), hlm(n_samples);
-        std::vector<u32> hloc(n_samples);
-        CK(cudaMemcpyAsync(hpos.data(), d_spos, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(float4));
-        CK(cudaMemcpyAsync(hnrm.data(), d_snrm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(float4));
-        CK(cudaMemcpyAsync(hrad.data(), d_srad, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(float4));
-        CK(cudaMemcpyAsync(hlm.data(), d_lm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(float4));
-        CK(cudaMemcpyAsync(hloc.data(), d_sloc, n_samples * sizeof(u32), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(u32));
-        CK(cudaStreamSynchronize(st));
-        RadInputs ri;
-        ri.n = n_samples;
-        ri.pos.resize(n_samples);
-        ri.nrm.resize(n_samples);
-        ri.diff_area.resize(n_samples);
-        ri.emit.resize(n_samples);
+        CK(cudaStreamSynchronize(st2));
+        std::vector<float4> hdiff(n_samples), hemis(n_samples);
         for (int i = 0; i < n_inst; ++i) {
             HostInst* mi = S->insts[i];
             for (u32 k = 0; k < scount[i]; ++k) {
                 u32 s = sbeg[i] + k;
-                V3 P = mk(hpos[s].x, hpos[s].y, hpos[s].z);
-                V3 N = normalized(mk(hnrm[s].x, hnrm[s].y, hnrm[s].z));
-                V3 diff = mk(1, 1, 1);
-                V3 emit = mk(hlm[s].x, hlm[s].y, hlm[s].z);
-                float area = mi->container ? 0 : hrad[s].w;
+                V3 diff = mk(1, 1, 1), emis = mk(0, 0, 0);
                 if (mi->container) {
                     diff = mk(0, 0, 0);
                 } else if (cfg.sample_fn) {   // lighter.cpp:692-714
+                    V3 P = mk(hpos[s].x, hpos[s].y, hpos[s].z);
+                    V3 N = normalized(mk(hnrm[s].x, hnrm[s].y, hnrm[s].z));
                     u32 L = hloc[s];
                     int lx = (int) (L % mi->w), ly = (int) (L / mi->w);
                     ltr_SampleRequest req;
@@ -1405,15 +1509,27 @@ void run_bake(ltr_Scene* S)
                     req.out_emissive_color[0] = req.out_emissive_color[1] = req.out_emissive_color[2] = 0;
                     if (cfg.sample_fn(const_cast<ltr_Config*>(&cfg), &req)) {
                         diff = mk(req.out_diffuse_color[0], req.out_diffuse_color[1], req.out_diffuse_color[2]);
-                        emit += mk(req.out_emissive_color[0], req.out_emissive_color[1], req.out_emissive_color[2]);
+                        emis = mk(req.out_emissive_color[0], req.out_emissive_color[1], req.out_emissive_color[2]);
                     }
                 }
-                ri.pos[s] = make_float4(P.x, P.y, P.z, 0);
-                ri.nrm[s] = make_float4(N.x, N.y, N.z, 0);
-                ri.diff_area[s] = make_float4(diff.x, diff.y, diff.z, area);
-                ri.emit[s] = make_float4(emit.x, emit.y, emit.z, 0);
+                hdiff[s] = make_float4(diff.x, diff.y, diff.z, 0);
+                hemis[s] = make_float4(emis.x, emis.y, emis.z, 0);
             }
         }
+        // AO draws its per-sample random offsets after the last sample_fn call,
+        // as the reference's AO stage comes after radiosity
+        if (do_ao) { ao_randoff.resize(n_samples); for (u32 s = 0; s < n_samples; ++s) ao_randoff[s] = randf_host(); }
+
+        float4* d_diff = A.alloc<float4>(n_samples);
+        float4* d_emis = A.alloc<float4>(n_samples);
+        CK(cudaMemcpyAsync(d_diff, hdiff.data(), n_samples * sizeof(float4), cudaMemcpyHostToDevice, st2)); note_h2d(n_samples * sizeof(float4));
+        CK(cudaMemcpyAsync(d_emis, hemis.data(), n_samples * sizeof(float4), cudaMemcpyHostToDevice, st2)); note_h2d(n_samples * sizeof(float4));
+        // per-sample radiosity inputs once direct light is done
+        float4* d_rpos = A.alloc<float4>(n_samples);
+        float4* d_rnrm = A.alloc<float4>(n_samples);
+        float4* d_rda = A.alloc<float4>(n_samples);
+        float4* d_remit = A.alloc<float4>(n_samples);
+
         RadSettings rs;
         rs.links = S->opt.radiosity_links;
         rs.precision = S->opt.radiosity_precision;
@@ -1421,79 +1537,81 @@ void run_bake(ltr_Scene* S)
         rs.bounces = cfg.bounce_count;
         RadResult rr;
         if (S->opt.radiosity_patches == 0) {
-            rr = radiosity_solve(ri, rs, bv, err_rad, st, d_lm, &S->abort_flag);
+            cudaEvent_t up = nullptr;
+            CK(cudaEventCreateWithFlags(&up, cudaEventDisableTiming));
+            CK(cudaEventRecord(up, st2));
+            CK(cudaStreamWaitEvent(st, up, 0));
+            k_rad_sample_inputs<<<(n_samples + kThreads - 1) / kThreads, kThreads, 0, st>>>(
+                n_samples, d_spos, d_snrm, d_srad, d_sinst, d_diff, d_emis, d_lm, d_rpos, d_rnrm, d_rda, d_remit); note_launch();
+            CK(cudaGetLastError());
+            cudaEventDestroy(up);
+            RadDevInputs ri{n_samples, d_rpos, d_rnrm, d_rda, d_remit};
+            rr = radiosity_solve_dev(ri, rs, bv, err_rad, st, d_lm, &S->abort_flag);
             S->stats.rad_elements = n_samples;
         } else {
             // Patch mode: group samples by (instance, lightmap tile, dominant
-            // normal axis); a patch carries the area-weighted mean position,
-            // normal, albedo and emission of its samples and their total area.
+            // normal axis), first-seen order; dense slot tables, no hashing.
             u32 target = S->opt.radiosity_patches;
             double per = std::max(1.0, (double) n_cov / (double) target);
             u32 tile = (u32) std::max(1.0, std::floor(std::sqrt(per) + 0.5));
             std::vector<int> patch_of(n_samples, -1);
-            std::unordered_map<uint64_t, int> key_to_patch;
-            std::vector<double> acc;   // per patch: area, pos3, nrm3, diff3, emit3 (area-weighted)
+            std::vector<u32> slot_base(n_inst + 1, 0);
+            for (int i = 0; i < n_inst; ++i) {
+                HostInst* mi = S->insts[i];
+                u32 nslots = mi->container ? 0 : ((mi->w + tile - 1) / tile) * ((mi->h + tile - 1) / tile) * 6;
+                slot_base[i + 1] = slot_base[i] + nslots;
+            }
+            std::vector<int> slot_patch(slot_base[n_inst], -1);
+            u32 np = 0;
             for (int i = 1; i < n_inst; ++i) {
                 HostInst* mi = S->insts[i];
+                u32 ntx = (mi->w + tile - 1) / tile;
                 for (u32 k = 0; k < scount[i]; ++k) {
                     u32 s = sbeg[i] + k;
                     u32 L = hloc[s];
                     u32 tx = (L % mi->w) / tile, ty = (L / mi->w) / tile;
-                    float4 n = ri.nrm[s];
+                    V3 n = normalized(mk(hnrm[s].x, hnrm[s].y, hnrm[s].z));
                     float ax = fabsf(n.x), ay = fabsf(n.y), az = fabsf(n.z);
                     u32 axis = (ax >= ay && ax >= az) ? (n.x >= 0 ? 0 : 1) : (ay >= az ? (n.y >= 0 ? 2 : 3) : (n.z >= 0 ? 4 : 5));
-                    uint64_t key = ((uint64_t) i << 40) ^ ((uint64_t) ty << 21) ^ ((uint64_t) tx << 3) ^ axis;
-                    auto it = key_to_patch.find(key);
-                    int p;
-                    if (it == key_to_patch.end()) {
-                        p = (int) key_to_patch.size();
-                        key_to_patch.emplace(key, p);
-                        acc.resize(acc.size() + 13, 0.0);
-                    } else {
-                        p = it->second;
-                    }
-                    patch_of[s] = p;
-                    double a = ri.diff_area[s].w;
-                    double* q = &acc[13 * (size_t) p];
-                    q[0] += a;
-                    q[1] += a * ri.pos[s].x; q[2] += a * ri.pos[s].y; q[3] += a * ri.pos[s].z;
-                    q[4] += a * n.x; q[5] += a * n.y; q[6] += a * n.z;
-                    q[7] += a * ri.diff_area[s].x; q[8] += a * ri.diff_area[s].y; q[9] += a * ri.diff_area[s].z;
-                    q[10] += a * ri.emit[s].x; q[11] += a * ri.emit[s].y; q[12] += a * ri.emit[s].z;
+                    u32 slot = slot_base[i] + (ty * ntx + tx) * 6 + axis;
+                    if (slot_patch[slot] < 0) slot_patch[slot] = (int) np++;
+                    patch_of[s] = slot_patch[slot];
                 }
             }
-            const u32 np = (u32) key_to_patch.size();
-            RadInputs pi;
-            pi.n = np;
-            pi.pos.resize(np); pi.nrm.resize(np); pi.diff_area.resize(np); pi.emit.resize(np);
-            for (u32 p = 0; p < np; ++p) {
-                const double* q = &acc[13 * (size_t) p];
-                double a = q[0] > 0 ? q[0] : 1.0;
-                V3 nn = normalized(mk((float) (q[4] / a), (float) (q[5] / a), (float) (q[6] / a)));
-                pi.pos[p] = make_float4((float) (q[1] / a), (float) (q[2] / a), (float) (q[3] / a), 0);
-                pi.nrm[p] = make_float4(nn.x, nn.y, nn.z, 0);
-                pi.diff_area[p] = make_float4((float) (q[7] / a), (float) (q[8] / a), (float) (q[9] / a), (float) q[0]);
-                pi.emit[p] = make_float4((float) (q[10] / a), (float) (q[11] / a), (float) (q[12] / a), 0);
+            // samples of each patch in sample order (counting sort)
+            std::vector<u32> csr_off(np + 1, 0), csr_idx(n_cov);
+            for (u32 s = 0; s < n_samples; ++s) if (patch_of[s] >= 0) csr_off[patch_of[s] + 1]++;
+            for (u32 p = 0; p < np; ++p) csr_off[p + 1] += csr_off[p];
+            {
+                std::vector<u32> fill(csr_off.begin(), csr_off.end() - 1);
+                for (u32 s = 0; s < n_samples; ++s) if (patch_of[s] >= 0) csr_idx[fill[patch_of[s]]++] = s;
             }
+            int* d_patch_of = A.alloc<int>(n_samples);
+            u32* d_csr_off = A.alloc<u32>(np + 1);
+            u32* d_csr_idx = A.alloc<u32>(n_cov);
+            CK(cudaMemcpyAsync(d_patch_of, patch_of.data(), n_samples * sizeof(int), cudaMemcpyHostToDevice, st2)); note_h2d(n_samples * sizeof(int));
+            CK(cudaMemcpyAsync(d_csr_off, csr_off.data(), (np + 1) * sizeof(u32), cudaMemcpyHostToDevice, st2)); note_h2d((np + 1) * sizeof(u32));
+            CK(cudaMemcpyAsync(d_csr_idx, csr_idx.data(), n_cov * sizeof(u32), cudaMemcpyHostToDevice, st2)); note_h2d(n_cov * sizeof(u32));
+            cudaEvent_t up = nullptr;
+            CK(cudaEventCreateWithFlags(&up, cudaEventDisableTiming));
+            CK(cudaEventRecord(up, st2));
+            CK(cudaStreamWaitEvent(st, up, 0));
+            cudaEventDestroy(up);
+            float4* d_ppos = A.alloc<float4>(np);
+            float4* d_pnrm = A.alloc<float4>(np);
+            float4* d_pda = A.alloc<float4>(np);
+            float4* d_pemit = A.alloc<float4>(np);
             float4* d_ptot = A.alloc<float4>(np);
-            rr = radiosity_solve(pi, rs, bv, err_rad, st, d_ptot, &S->abort_flag);
-            std::vector<float4> ptot(np);
-            CK(cudaMemcpyAsync(ptot.data(), d_ptot, np * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(np * sizeof(float4));
-            CK(cudaStreamSynchronize(st));
-            // texel = own emission + its patch's gathered light
-            std::vector<float4> out(n_samples);
-            for (u32 s = 0; s < n_samples; ++s) {
-                float4 e = ri.emit[s];
-                int p = patch_of[s];
-                if (p >= 0) {
-                    e.x += ptot[p].x - pi.emit[p].x;
-                    e.y += ptot[p].y - pi.emit[p].y;
-                    e.z += ptot[p].z - pi.emit[p].z;
-                }
-                out[s] = e;
+            if (np) {
+                k_patch_inputs<<<(np + 127) / 128, 128, 0, st>>>(np, d_csr_off, d_csr_idx, d_spos, d_snrm, d_srad, d_diff,
+                                                                 d_emis, d_lm, d_ppos, d_pnrm, d_pda, d_pemit); note_launch();
+                CK(cudaGetLastError());
+                RadDevInputs pi{np, d_ppos, d_pnrm, d_pda, d_pemit};
+                rr = radiosity_solve_dev(pi, rs, bv, err_rad, st, d_ptot, &S->abort_flag);
+                k_patch_apply<<<(n_samples + kThreads - 1) / kThreads, kThreads, 0, st>>>(
+                    n_samples, d_patch_of, d_emis, d_ptot, d_pemit, d_lm); note_launch();
+                CK(cudaGetLastError());
             }
-            CK(cudaMemcpyAsync(d_lm, out.data(), n_samples * sizeof(float4), cudaMemcpyHostToDevice, st)); note_h2d(n_samples * sizeof(float4));
-            CK(cudaStreamSynchronize(st));
             S->stats.rad_elements = np;
         }
         S->rad_links = (u32) rr.links;
@@ -1503,16 +1621,17 @@ void run_bake(ltr_Scene* S)
         S->stats.ms_rad_bounce = rr.ms_bounce;
         S->stage = "committing radiosity";
         e_rad_links = e_rad_bounce = clock.mark();
+    } else if (do_ao) {
+        ao_randoff.resize(n_samples);
+        for (u32 s = 0; s < n_samples; ++s) ao_randoff[s] = randf_host();   // instance order, sample order
     }
     check_abort(S);
 
     // ---- ambient occlusion (Job_AORender)
     cudaEvent_t e_ao0 = clock.mark();
-    if (cfg.ao_distance && n_samples) {
+    if (do_ao) {
         S->stage = "rendering ambient occlusion";
-        std::vector<float> ro(n_samples);
-        for (u32 s = 0; s < n_samples; ++s) ro[s] = randf_host();   // instance order, sample order
-        float* d_ro = A.upload(ro);
+        float* d_ro = A.upload(ao_randoff);
         AoArgs aa;
         aa.bvh = bv;
         aa.err = err_ao;
@@ -1529,7 +1648,15 @@ void run_bake(ltr_Scene* S)
         for (int c = 0; c < 3; ++c) aa.aoc[c] = cfg.ao_color_rgb[c];
         aa.counters = d_cnt;
         if (aa.ns > 0) {
-            k_ao<<<blocks_for((size_t) n_samples * 32, 256, 152ull * 64), 256, 0, st>>>(aa); note_launch();
+            unsigned long long n_rays = (unsigned long long) n_samples * aa.ns;
+            float* d_hits = A.alloc<float>(n_rays);
+            unsigned long long* d_next = A.zeros<unsigned long long>(1);
+            int dev_sms = 0;
+            CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, S->opt.device));
+            unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * 16, (n_rays + 127) / 128);
+            k_ao_rays<<<grid, 128, 0, st>>>(aa, d_hits, n_rays, d_next); note_launch();
+            CK(cudaGetLastError());
+            k_ao<<<blocks_for(n_samples), kThreads, 0, st>>>(aa, d_hits); note_launch();
             CK(cudaGetLastError());
         }
     }

@@ -139,8 +139,8 @@ __global__ void k_rad_update(u32 n, const float4* __restrict__ Y, float4* __rest
 }
 
 template <class T>
-RadResult solve_t(const RadInputs& in, const RadSettings& rs, const BvhView& bvh, ErrFlag err, cudaStream_t st,
-                  float4* lm_out, std::atomic<bool>* abort_flag)
+RadResult solve_t(const RadDevInputs& in, const RadSettings& rs, const BvhView& bvh, ErrFlag err, cudaStream_t st,
+                  float4* total_out, std::atomic<bool>* abort_flag)
 {
     RadResult rr;
     const u32 n = in.n;
@@ -148,49 +148,42 @@ RadResult solve_t(const RadInputs& in, const RadSettings& rs, const BvhView& bvh
     RCK(cudaMemGetInfo(&free_b, &total_b));
     size_t fbytes = (size_t) n * n * sizeof(T);
     if (fbytes > free_b / 10 * 9)
-        throw std::runtime_error("radiosity: dense form factors for " + std::to_string(n) + " samples need " +
+        throw std::runtime_error("radiosity: dense form factors for " + std::to_string(n) + " elements need " +
                                  std::to_string(fbytes >> 20) + " MiB, more than the free device memory");
     T* F = nullptr;
-    float4 *pos, *nrm, *da, *out, *total, *X, *Y;
+    float4 *out, *X, *Y;
     unsigned long long* counts;
     RCK(cudaMallocAsync(&F, fbytes ? fbytes : 1, st));
-    RCK(cudaMallocAsync(&pos, n * sizeof(float4), st));
-    RCK(cudaMallocAsync(&nrm, n * sizeof(float4), st));
-    RCK(cudaMallocAsync(&da, n * sizeof(float4), st));
     RCK(cudaMallocAsync(&out, n * sizeof(float4), st));
-    RCK(cudaMallocAsync(&total, n * sizeof(float4), st));
     RCK(cudaMallocAsync(&X, n * sizeof(float4), st));
     RCK(cudaMallocAsync(&Y, n * sizeof(float4), st));
     RCK(cudaMallocAsync(&counts, 2 * sizeof(unsigned long long), st));
     struct Free {
-        cudaStream_t st; void* p[9];
+        cudaStream_t st; void* p[5];
         ~Free() { for (void* q : p) if (q) cudaFreeAsync(q, st); }
-    } guard{st, {F, pos, nrm, da, out, total, X, Y, counts}};
-    RCK(cudaMemcpyAsync(pos, in.pos.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st)); note_h2d(n * sizeof(float4));
-    RCK(cudaMemcpyAsync(nrm, in.nrm.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st)); note_h2d(n * sizeof(float4));
-    RCK(cudaMemcpyAsync(da, in.diff_area.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st)); note_h2d(n * sizeof(float4));
-    RCK(cudaMemcpyAsync(out, in.emit.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st)); note_h2d(n * sizeof(float4));
-    RCK(cudaMemcpyAsync(total, in.emit.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st)); note_h2d(n * sizeof(float4));
+    } guard{st, {F, out, X, Y, counts}};
+    float4* total = total_out;
+    RCK(cudaMemcpyAsync(out, in.emit, n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    if (total != in.emit) RCK(cudaMemcpyAsync(total, in.emit, n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
     RCK(cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned long long), st));
 
     cudaEvent_t e0, e1, e2;
     RCK(cudaEventCreate(&e0)); RCK(cudaEventCreate(&e1)); RCK(cudaEventCreate(&e2));
     RCK(cudaEventRecord(e0, st));
     u32 nb = (n + 31) / 32;
-    if (nb > 65535) throw std::runtime_error("radiosity: too many samples for the tile grid");
+    if (nb > 65535) throw std::runtime_error("radiosity: too many elements for the tile grid");
     dim3 grid(nb, nb), block(32, 8);
-    k_form_factors<T><<<grid, block, 0, st>>>(n, pos, nrm, bvh, err, rs.links, F, counts); note_launch();
+    k_form_factors<T><<<grid, block, 0, st>>>(n, in.pos, in.nrm, bvh, err, rs.links, F, counts); note_launch();
     RCK(cudaGetLastError());
     RCK(cudaEventRecord(e1, st));
     for (int b = 0; b < rs.bounces; ++b) {
         if (abort_flag && abort_flag->load()) break;
-        k_rad_x<<<(n + 255) / 256, 256, 0, st>>>(n, out, da, X); note_launch();
+        k_rad_x<<<(n + 255) / 256, 256, 0, st>>>(n, out, in.diff_area, X); note_launch();
         k_rad_gemv<T><<<(unsigned) (((size_t) n * 32 + 255) / 256), 256, 0, st>>>(n, F, X, Y); note_launch();
         k_rad_update<<<(n + 255) / 256, 256, 0, st>>>(n, Y, total, out); note_launch();
         RCK(cudaGetLastError());
     }
     RCK(cudaEventRecord(e2, st));
-    RCK(cudaMemcpyAsync(lm_out, total, n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
     unsigned long long hc[2];
     RCK(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(hc));
     RCK(cudaStreamSynchronize(st));
@@ -208,13 +201,30 @@ RadResult solve_t(const RadInputs& in, const RadSettings& rs, const BvhView& bvh
 
 }  // namespace
 
+RadResult radiosity_solve_dev(const RadDevInputs& in, const RadSettings& rs, const BvhView& bvh, ErrFlag err,
+                              cudaStream_t st, float4* total_out, std::atomic<bool>* abort_flag)
+{
+    if (in.n == 0) return RadResult();
+    if (rs.precision == 1) return solve_t<__half>(in, rs, bvh, err, st, total_out, abort_flag);
+    if (rs.precision == 2) return solve_t<__nv_bfloat16>(in, rs, bvh, err, st, total_out, abort_flag);
+    return solve_t<float>(in, rs, bvh, err, st, total_out, abort_flag);
+}
+
 RadResult radiosity_solve(const RadInputs& in, const RadSettings& rs, const BvhView& bvh, ErrFlag err, cudaStream_t st,
                           float4* lm_out, std::atomic<bool>* abort_flag)
 {
     if (in.n == 0) return RadResult();
-    if (rs.precision == 1) return solve_t<__half>(in, rs, bvh, err, st, lm_out, abort_flag);
-    if (rs.precision == 2) return solve_t<__nv_bfloat16>(in, rs, bvh, err, st, lm_out, abort_flag);
-    return solve_t<float>(in, rs, bvh, err, st, lm_out, abort_flag);
+    const u32 n = in.n;
+    float4* buf = nullptr;
+    RCK(cudaMallocAsync(&buf, 4 * (size_t) n * sizeof(float4), st));
+    struct Free { cudaStream_t st; void* p; ~Free() { cudaFreeAsync(p, st); } } guard{st, buf};
+    const std::vector<float4>* src[4] = {&in.pos, &in.nrm, &in.diff_area, &in.emit};
+    for (int k = 0; k < 4; ++k) {
+        RCK(cudaMemcpyAsync(buf + (size_t) k * n, src[k]->data(), n * sizeof(float4), cudaMemcpyHostToDevice, st));
+        note_h2d(n * sizeof(float4));
+    }
+    RadDevInputs d{n, buf, buf + n, buf + 2 * (size_t) n, buf + 3 * (size_t) n};
+    return radiosity_solve_dev(d, rs, bvh, err, st, lm_out, abort_flag);
 }
 
 }  // namespace lg

@@ -36,7 +36,21 @@ struct RadResult {
     double ms_links = 0, ms_bounce = 0;
 };
 
-// Builds F, runs the bounces and writes `total` into lm_out (float4 per sample).
+// Inputs already on the device (same meaning as RadInputs).
+struct RadDevInputs {
+    uint32_t n;
+    const float4* pos;
+    const float4* nrm;
+    const float4* diff_area;
+    const float4* emit;
+};
+
+// Builds F, runs the bounces and writes `total` (float4 per element) to
+// total_out, which may alias in.emit.
+RadResult radiosity_solve_dev(const RadDevInputs& in, const RadSettings& rs, const BvhView& bvh, ErrFlag err,
+                              cudaStream_t st, float4* total_out, std::atomic<bool>* abort_flag);
+
+// Same from host vectors (uploads them first).
 RadResult radiosity_solve(const RadInputs& in, const RadSettings& rs, const BvhView& bvh, ErrFlag err, cudaStream_t st,
                           float4* lm_out, std::atomic<bool>* abort_flag);
 
