@@ -496,6 +496,33 @@ __global__ void k_rad_sample_inputs(u32 n, const float4* __restrict__ spos, cons
     emit[s] = st4(e, 0.0f);
 }
 
+// ltrg_TableSampleFn (api.cpp) evaluated on the device with the same
+// contract: the entry is chosen by (u32) tex0u (radinfo.x); negative or
+// out-of-range ids keep the defaults (albedo 1, no emission); probes are
+// black (lighter.cpp:685-714). has_fn = 0 stands for a NULL sample_fn.
+__global__ void k_table_samples(u32 n, const float4* __restrict__ srad, const u32* __restrict__ sinst, int has_fn,
+                                u32 count, const float* __restrict__ tdiff, const float* __restrict__ temis,
+                                float4* __restrict__ diff, float4* __restrict__ emis)
+{
+    u32 s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    V3 d = mk(1, 1, 1), e = mk(0, 0, 0);
+    if (sinst[s] == 0) {
+        d = mk(0, 0, 0);
+    } else if (has_fn) {
+        float fid = srad[s].x;
+        if (fid >= 0.0f) {
+            u32 id = (u32) fid;
+            if (id < count) {
+                if (tdiff) d = mk(tdiff[3 * id], tdiff[3 * id + 1], tdiff[3 * id + 2]);
+                if (temis) e = mk(temis[3 * id], temis[3 * id + 1], temis[3 * id + 2]);
+            }
+        }
+    }
+    diff[s] = st4(d, 0.0f);
+    emis[s] = st4(e, 0.0f);
+}
+
 // Patch element from its samples (in sample order): total area and
 // area-weighted position, normal, albedo and emission, accumulated in FP64.
 __global__ void k_patch_inputs(u32 np, const u32* __restrict__ off, const u32* __restrict__ idx,
@@ -1351,6 +1378,22 @@ void run_bake(ltr_Scene* S)
         scount[i] = e - b;
     }
 
+    // sample_fn runs on the device when it is the library's table function
+    // (or NULL); any other callback is called on this thread, in sample order.
+    const bool gpu_sample_fn = !cfg.sample_fn || cfg.sample_fn == ltrg_TableSampleFn;
+    // AO's per-sample rand() draws (lighter.cpp:819) come after every user
+    // callback that could call rand() itself: here unless a host sample_fn
+    // still has to run, in which case they follow its calls.
+    std::vector<float> ao_randoff;
+    std::thread ao_thread;
+    const bool do_ao = cfg.ao_distance && n_samples && cfg.ao_num_samples > 0;
+    if (do_ao && (gpu_sample_fn || !cfg.bounce_count))
+        ao_thread = std::thread([&ao_randoff, n_samples]() {
+            ao_randoff.resize(n_samples);
+            for (u32 s = 0; s < n_samples; ++s) ao_randoff[s] = randf_host();   // instance order, sample order
+        });
+    struct JoinGuard { std::thread& t; ~JoinGuard() { if (t.joinable()) t.join(); } } ao_guard{ao_thread};
+
     float4* d_spos = A.alloc<float4>(n_samples);
     float4* d_snrm = A.alloc<float4>(n_samples);
     float4* d_srad = A.zeros<float4>(n_samples);
@@ -1465,12 +1508,17 @@ void run_bake(ltr_Scene* S)
     std::vector<float4> hpos, hnrm, hrad;
     std::vector<u32> hloc;
     if (do_rad) {
-        hpos.resize(n_samples); hnrm.resize(n_samples); hrad.resize(n_samples); hloc.resize(n_samples);
         CK(cudaStreamWaitEvent(st2, e_samples, 0));
-        CK(cudaMemcpyAsync(hpos.data(), d_spos, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st2)); note_d2h(n_samples * sizeof(float4));
-        CK(cudaMemcpyAsync(hnrm.data(), d_snrm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st2)); note_d2h(n_samples * sizeof(float4));
-        CK(cudaMemcpyAsync(hrad.data(), d_srad, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st2)); note_d2h(n_samples * sizeof(float4));
-        CK(cudaMemcpyAsync(hloc.data(), d_sloc, n_samples * sizeof(u32), cudaMemcpyDeviceToHost, st2)); note_d2h(n_samples * sizeof(u32));
+        if (!gpu_sample_fn) {   // the host calls sample_fn with position and texcoords
+            hpos.resize(n_samples); hrad.resize(n_samples);
+            CK(cudaMemcpyAsync(hpos.data(), d_spos, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st2)); note_d2h(n_samples * sizeof(float4));
+            CK(cudaMemcpyAsync(hrad.data(), d_srad, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st2)); note_d2h(n_samples * sizeof(float4));
+        }
+        if (!gpu_sample_fn || S->opt.radiosity_patches) {   // sample_fn requests and patch grouping
+            hnrm.resize(n_samples); hloc.resize(n_samples);
+            CK(cudaMemcpyAsync(hnrm.data(), d_snrm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st2)); note_d2h(n_samples * sizeof(float4));
+            CK(cudaMemcpyAsync(hloc.data(), d_sloc, n_samples * sizeof(u32), cudaMemcpyDeviceToHost, st2)); note_d2h(n_samples * sizeof(u32));
+        }
     }
     check_abort(S);
 
@@ -1479,12 +1527,26 @@ void run_bake(ltr_Scene* S)
     // direct-light kernels are still tracing: the sample arrays it needs were
     // copied on the side stream as soon as the sample stage ended.
     cudaEvent_t e_rad_links = e_direct, e_rad_bounce = e_direct;
-    std::vector<float> ao_randoff;
-    const bool do_ao = cfg.ao_distance && n_samples && cfg.ao_num_samples > 0;
     if (do_rad) {
         S->stage = "calculating radiosity";
         CK(cudaStreamSynchronize(st2));
-        std::vector<float4> hdiff(n_samples), hemis(n_samples);
+        float4* d_diff = A.alloc<float4>(n_samples);
+        float4* d_emis = A.alloc<float4>(n_samples);
+        std::vector<float4> hdiff, hemis;
+        if (gpu_sample_fn) {
+            const ltrg_SampleTable* tab = cfg.sample_fn ? (const ltrg_SampleTable*) cfg.userdata : nullptr;
+            u32 count = tab ? tab->count : 0;
+            std::vector<float> td, te;
+            if (tab && tab->diffuse_rgb) td.assign(tab->diffuse_rgb, tab->diffuse_rgb + 3 * (size_t) count);
+            if (tab && tab->emissive_rgb) te.assign(tab->emissive_rgb, tab->emissive_rgb + 3 * (size_t) count);
+            float* d_td = td.empty() ? nullptr : A.upload(td);
+            float* d_te = te.empty() ? nullptr : A.upload(te);
+            k_table_samples<<<(n_samples + kThreads - 1) / kThreads, kThreads, 0, st>>>(
+                n_samples, d_srad, d_sinst, cfg.sample_fn != nullptr && tab != nullptr, count, d_td, d_te, d_diff, d_emis); note_launch();
+            CK(cudaGetLastError());
+        } else {
+        hdiff.resize(n_samples);
+        hemis.resize(n_samples);
         for (int i = 0; i < n_inst; ++i) {
             HostInst* mi = S->insts[i];
             for (u32 k = 0; k < scount[i]; ++k) {
@@ -1518,12 +1580,13 @@ void run_bake(ltr_Scene* S)
         }
         // AO draws its per-sample random offsets after the last sample_fn call,
         // as the reference's AO stage comes after radiosity
-        if (do_ao) { ao_randoff.resize(n_samples); for (u32 s = 0; s < n_samples; ++s) ao_randoff[s] = randf_host(); }
-
-        float4* d_diff = A.alloc<float4>(n_samples);
-        float4* d_emis = A.alloc<float4>(n_samples);
+        if (do_ao && !ao_thread.joinable()) {
+            ao_randoff.resize(n_samples);
+            for (u32 s = 0; s < n_samples; ++s) ao_randoff[s] = randf_host();
+        }
         CK(cudaMemcpyAsync(d_diff, hdiff.data(), n_samples * sizeof(float4), cudaMemcpyHostToDevice, st2)); note_h2d(n_samples * sizeof(float4));
         CK(cudaMemcpyAsync(d_emis, hemis.data(), n_samples * sizeof(float4), cudaMemcpyHostToDevice, st2)); note_h2d(n_samples * sizeof(float4));
+        }
         // per-sample radiosity inputs once direct light is done
         float4* d_rpos = A.alloc<float4>(n_samples);
         float4* d_rnrm = A.alloc<float4>(n_samples);
@@ -1621,10 +1684,8 @@ void run_bake(ltr_Scene* S)
         S->stats.ms_rad_bounce = rr.ms_bounce;
         S->stage = "committing radiosity";
         e_rad_links = e_rad_bounce = clock.mark();
-    } else if (do_ao) {
-        ao_randoff.resize(n_samples);
-        for (u32 s = 0; s < n_samples; ++s) ao_randoff[s] = randf_host();   // instance order, sample order
     }
+    if (ao_thread.joinable()) ao_thread.join();
     check_abort(S);
 
     // ---- ambient occlusion (Job_AORender)

@@ -161,6 +161,37 @@ __global__ void k_pack_tris(int n, const u32* ids, const u32* ref_tri, const flo
     tris[3 * (size_t) i + 2] = make_float4(p[6], p[7], p[8], __uint_as_float(s));
 }
 
+// Triangle-only terms of the two exact tests per leaf (layout in bvh.cuh),
+// computed with the expressions of seg_tri / point_tri_dist in common.cuh.
+__global__ void k_pack_records(int nleaf, const float4* __restrict__ tris, float4* __restrict__ srec,
+                               float4* __restrict__ drec)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nleaf) return;
+    float4 a = tris[3 * (size_t) i], b = tris[3 * (size_t) i + 1], c = tris[3 * (size_t) i + 2];
+    V3 t0 = mk(a.x, a.y, a.z), t1 = mk(b.x, b.y, b.z), t2 = mk(c.x, c.y, c.z);
+    float meta = a.w;
+    V3 u = t1 - t0, v = t2 - t0;
+    V3 n = cross(u, v);
+    float4* s = srec + 4 * (size_t) i;
+    s[0] = make_float4(t0.x, t0.y, t0.z, meta);
+    s[1] = make_float4(u.x, u.y, u.z, dot(u, u));
+    s[2] = make_float4(v.x, v.y, v.z, dot(u, v));
+    s[3] = make_float4(n.x, n.y, n.z, dot(v, v));
+    V3 nrm = normalized(cross(t1 - t0, t2 - t0));
+    V3 tan0 = normalized(t1 - t0), tan1 = normalized(t2 - t1), tan2 = normalized(t0 - t2);
+    V3 en0 = normalized(cross(t1 - t0, nrm)), en1 = normalized(cross(t2 - t1, nrm)), en2 = normalized(cross(t0 - t2, nrm));
+    float4* d = drec + 8 * (size_t) i;
+    d[0] = make_float4(nrm.x, nrm.y, nrm.z, dot(nrm, t0));
+    d[1] = make_float4(tan0.x, tan0.y, tan0.z, dot(tan0, t0));
+    d[2] = make_float4(tan1.x, tan1.y, tan1.z, dot(tan1, t1));
+    d[3] = make_float4(tan2.x, tan2.y, tan2.z, dot(tan2, t2));
+    d[4] = make_float4(dot(tan0, t1), dot(tan1, t2), dot(tan2, t0), meta);
+    d[5] = make_float4(en0.x, en0.y, en0.z, dot(en0, t0));
+    d[6] = make_float4(en1.x, en1.y, en1.z, dot(en1, t1));
+    d[7] = make_float4(en2.x, en2.y, en2.z, dot(en2, t2));
+}
+
 template <class T>
 T* alloc(size_t count, cudaStream_t st, size_t& bytes)
 {
@@ -227,6 +258,10 @@ void bvh_build(const BvhBuildInput& in, BvhStorage& out, void* stream)
     k_pack_tris<<<(n + B - 1) / B, B, 0, st>>>(n, ids2, in.ref_tri, in.tri_xyz, in.tri_meta, in.tri_local,
                                                 out.tris); note_launch();
     BVH_CHECK(cudaGetLastError());
+    out.srec = alloc<float4>(4 * (size_t) n, st, out.bytes);
+    out.drec = alloc<float4>(8 * (size_t) n, st, out.bytes);
+    k_pack_records<<<(n + B - 1) / B, B, 0, st>>>(n, out.tris, out.srec, out.drec); note_launch();
+    BVH_CHECK(cudaGetLastError());
 
     void* ptrs[] = {codes, codes2, ids, ids2, left, right, parent_int, parent_leaf, leaf_box, int_box, arrivals, temp};
     for (void* p : ptrs) BVH_CHECK(cudaFreeAsync(p, st));
@@ -274,8 +309,12 @@ void bvh_free(BvhStorage& s, void* stream)
     cudaStream_t st = (cudaStream_t) stream;
     if (s.nodes) cudaFreeAsync(s.nodes, st);
     if (s.tris) cudaFreeAsync(s.tris, st);
+    if (s.srec) cudaFreeAsync(s.srec, st);
+    if (s.drec) cudaFreeAsync(s.drec, st);
     s.nodes = nullptr;
     s.tris = nullptr;
+    s.srec = nullptr;
+    s.drec = nullptr;
     s.n_tris = 0;
 }
 

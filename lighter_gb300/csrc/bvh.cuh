@@ -30,9 +30,20 @@ constexpr u32 kInstMask = 0x3fffffffu;
 struct BvhView {
     const float4* nodes;
     const float4* tris;
-    int n_tris;      // 0: empty scene
+    const float4* srec;   // 4 per leaf: segment-test record (see below)
+    const float4* drec;   // 8 per leaf: distance-test record (see below)
+    int n_tris;      // number of leaves; 0: empty scene
     int root;        // >= 0 internal node, < 0 leaf (single triangle)
 };
+
+// Per-leaf records with the triangle-only terms of the two exact tests,
+// computed once per bake with the reference's own expressions (so a test
+// that reads them rounds exactly like one that recomputes them):
+//   srec: (P1, meta) (u = P2-P1, uu) (v = P3-P1, uv) (n = u x v, vv)
+//   drec: (nrm, nrm.t0) (tan0, tan0.t0) (tan1, tan1.t1) (tan2, tan2.t2)
+//         (tan0.t1, tan1.t2, tan2.t0, meta) (en0, en0.t0) (en1, en1.t1) (en2, en2.t2)
+// with nrm = |(t1-t0) x (t2-t0)|, tan0..2 the unit edges and en0..2 the unit
+// edge normals of PointTriangleDistance (lighter_math.cpp:875-913).
 
 // Error word shared by all kernels of one bake: bit 0 stack overflow, bit 1
 // candidate-list overflow, bit 2 index out of range.
@@ -141,16 +152,67 @@ __device__ __forceinline__ void walk_segment(const BvhView& b, V3 o, V3 e, ErrFl
     }
 }
 
+// IntersectLineSegmentTriangle (lighter_math.cpp:315-354) with the
+// triangle-only terms read from the leaf's record.
+__device__ __forceinline__ float seg_tri_rec(V3 L1, V3 L2, const float4* r, u32& meta)
+{
+    float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
+    meta = __float_as_uint(r0.w);
+    V3 P1 = mk(r0.x, r0.y, r0.z), u = mk(r1.x, r1.y, r1.z), v = mk(r2.x, r2.y, r2.z), n = mk(r3.x, r3.y, r3.z);
+    float uu = r1.w, uv = r2.w, vv = r3.w;
+    if (near_zero(n)) return kNoHit;
+    V3 dir = L2 - L1, w0 = L1 - P1;
+    float a = -dot(n, w0);
+    float b = dot(n, dir);
+    if (fabsf(b) < kSmall) return kNoHit;
+    float rr = a / b;
+    if (rr < 0.0f || rr > 1.0f) return kNoHit;
+    V3 I = L1 + rr * dir;
+    V3 w = I - P1;
+    float wu = dot(w, u), wv = dot(w, v);
+    float D = uv * uv - uu * vv;
+    float s = (uv * wv - vv * wu) / D;
+    if (s < 0.0f || s > 1.0f) return kNoHit;
+    float t = (uv * wu - uu * wv) / D;
+    if (t < 0.0f || (s + t) > 1.0f) return kNoHit;
+    return rr;
+}
+
+// PointTriangleDistance (lighter_math.cpp:875-913) with the triangle-only
+// terms read from the leaf's record; the vertices are read only for the
+// corner regions.
+__device__ __forceinline__ float point_tri_dist_rec(const BvhView& b, int t, V3 pt)
+{
+    const float4* r = b.drec + 8 * (size_t) t;
+    float4 f0 = __ldg(r), f1 = __ldg(r + 1), f2 = __ldg(r + 2), f3 = __ldg(r + 3), f4 = __ldg(r + 4);
+    V3 nrm = mk(f0.x, f0.y, f0.z);
+    float pd = fabsf(dot(nrm, pt) - f0.w);
+    float t0p = dot(mk(f1.x, f1.y, f1.z), pt), t0min = f1.w, t0max = f4.x;
+    float t1p = dot(mk(f2.x, f2.y, f2.z), pt), t1min = f2.w, t1max = f4.y;
+    float t2p = dot(mk(f3.x, f3.y, f3.z), pt), t2min = f3.w, t2max = f4.z;
+    if (t0min >= t0p && t2max <= t2p) { float4 v = __ldg(&b.tris[3 * (size_t) t]); return len(pt - mk(v.x, v.y, v.z)); }
+    if (t1min >= t1p && t0max <= t0p) { float4 v = __ldg(&b.tris[3 * (size_t) t + 1]); return len(pt - mk(v.x, v.y, v.z)); }
+    if (t2min >= t2p && t1max <= t1p) { float4 v = __ldg(&b.tris[3 * (size_t) t + 2]); return len(pt - mk(v.x, v.y, v.z)); }
+    float4 f5 = __ldg(r + 5), f6 = __ldg(r + 6), f7 = __ldg(r + 7);
+    float d0 = dot(mk(f5.x, f5.y, f5.z), pt) - f5.w;
+    float d1 = dot(mk(f6.x, f6.y, f6.z), pt) - f6.w;
+    float d2 = dot(mk(f7.x, f7.y, f7.z), pt) - f7.w;
+    if (d0 >= 0 && t0p >= t0min && t0p <= t0max) return len2(mk2(pd, d0));
+    if (d1 >= 0 && t1p >= t1min && t1p <= t1max) return len2(mk2(pd, d1));
+    if (d2 >= 0 && t2p >= t2min && t2p <= t2max) return len2(mk2(pd, d2));
+    return pd;
+}
+
 // Any occluder triangle hit with r < 1 on [o, e] (TriTree::IntersectRay,
 // lighter_math.cpp:804-832, over every shadowing instance).
 __device__ __forceinline__ bool bvh_any_hit(const BvhView& b, V3 o, V3 e, ErrFlag err)
 {
     bool hit = false;
     walk_segment(b, o, e, err, [&](int t, float&) {
-        V3 P1, P2, P3; u32 meta, local;
-        load_tri(b, t, P1, P2, P3, meta, local);
+        u32 meta;
+        float r = seg_tri_rec(o, e, b.srec + 4 * (size_t) t, meta);
         if (!(meta & kOccluderBit)) return true;
-        if (seg_tri(o, e, P1, P2, P3) < 1.0f) { hit = true; return false; }
+        if (r < 1.0f) { hit = true; return false; }
         return true;
     });
     return hit;
@@ -163,10 +225,9 @@ __device__ __forceinline__ float bvh_closest(const BvhView& b, V3 o, V3 e, ErrFl
     float best = kNoHit;
     int bt = -1;
     walk_segment(b, o, e, err, [&](int t, float& tlimit) {
-        V3 P1, P2, P3; u32 meta, local;
-        load_tri(b, t, P1, P2, P3, meta, local);
+        u32 meta;
+        float r = seg_tri_rec(o, e, b.srec + 4 * (size_t) t, meta);
         if (!(meta & kOccluderBit)) return true;
-        float r = seg_tri(o, e, P1, P2, P3);
         if (r < best || (r == best && r < kNoHit && t < bt)) {
             best = r; bt = t;
             tlimit = fminf(1.0f, r);
@@ -185,10 +246,10 @@ __device__ __forceinline__ float bvh_closest_inst(const BvhView& b, V3 o, V3 e, 
     float best = kNoHit;
     int bl = -1;
     walk_segment(b, o, e, err, [&](int t, float& tlimit) {
-        V3 P1, P2, P3; u32 meta, local;
-        load_tri(b, t, P1, P2, P3, meta, local);
+        u32 meta;
+        float r = seg_tri_rec(o, e, b.srec + 4 * (size_t) t, meta);
         if ((meta & kInstMask) != inst) return true;
-        float r = seg_tri(o, e, P1, P2, P3);
+        u32 local = __float_as_uint(__ldg(&b.tris[3 * (size_t) t + 1]).w);
         if (r < best || (r == best && r < kNoHit && (int) local < bl)) {
             best = r; bl = (int) local;
             tlimit = fminf(1.0f, r);
@@ -232,10 +293,10 @@ __device__ __forceinline__ float bvh_distance(const BvhView& b, V3 p, float d0, 
             if (hl) { cur = nb.l; continue; }
             if (hr) { cur = nb.r; continue; }
         } else {
-            V3 P1, P2, P3; u32 meta, local;
-            load_tri(b, ~cur, P1, P2, P3, meta, local);
+            int t = ~cur;
+            u32 meta = __float_as_uint(__ldg(&b.drec[8 * (size_t) t + 4]).w);
             if (meta & kOccluderBit) {
-                float nd = point_tri_dist(p, P1, P2, P3);
+                float nd = point_tri_dist_rec(b, t, p);
                 ++nt;
                 if (nd < dist) dist = nd;
             }
@@ -254,47 +315,6 @@ __device__ __forceinline__ float bvh_distance(const BvhView& b, V3 p, float d0, 
     return dist;
 }
 
-// Among the triangles of instance `inst` whose boxes overlap [qmn, qmx]
-// (AABBTree::Query over one instance, lighter_int.hpp:786-806), the one with
-// the smallest instance-local index greater than `after`. Repeated calls
-// visit the overlapping triangles in the instance's own order without a
-// candidate buffer. Returns the leaf-order index or -1.
-__device__ __forceinline__ int bvh_next_inst(const BvhView& b, V3 qmn, V3 qmx, u32 inst, int after, int* local_out,
-                                             ErrFlag err)
-{
-    if (b.n_tris <= 0) return -1;
-    int best_t = -1;
-    u32 best_l = 0xffffffffu;
-    int stack[kStack];
-    int sp = 0;
-    int cur = b.root;
-    for (;;) {
-        if (cur >= 0) {
-            NodeBoxes nb = load_node(b, cur);
-            bool hl = box_overlap(nb.lmin, nb.lmax, qmn, qmx);
-            bool hr = box_overlap(nb.rmin, nb.rmax, qmn, qmx);
-            if (hl && hr) {
-                if (sp < kStack) stack[sp++] = nb.r; else raise_err(err, 1u);
-                cur = nb.l;
-                continue;
-            }
-            if (hl) { cur = nb.l; continue; }
-            if (hr) { cur = nb.r; continue; }
-        } else {
-            int t = ~cur;
-            u32 meta = __float_as_uint(__ldg(&b.tris[3 * t]).w);
-            if ((meta & kInstMask) == inst) {
-                u32 l = __float_as_uint(__ldg(&b.tris[3 * t + 1]).w);
-                if ((int) l > after && l < best_l) { best_l = l; best_t = t; }
-            }
-        }
-        if (sp == 0) break;
-        cur = stack[--sp];
-    }
-    *local_out = (int) best_l;
-    return best_t;
-}
-
 #endif  // __CUDACC__
 
 // Host side of the build (bvh.cu).
@@ -310,12 +330,14 @@ struct BvhBuildInput {
 
 struct BvhStorage {
     float4* nodes = nullptr;   // 4 per internal node
-    float4* tris = nullptr;    // 3 per triangle
+    float4* tris = nullptr;    // 3 per leaf
+    float4* srec = nullptr;    // 4 per leaf
+    float4* drec = nullptr;    // 8 per leaf
     int n_tris = 0;
     int root = 0;
     size_t bytes = 0;
     void* scratch = nullptr;   // build scratch, freed by bvh_free
-    BvhView view() const { BvhView v = {nodes, tris, n_tris, root}; return v; }
+    BvhView view() const { BvhView v = {nodes, tris, srec, drec, n_tris, root}; return v; }
 };
 
 // Builds into `out` on `stream` (allocations with cudaMallocAsync on that stream).
