@@ -3,6 +3,8 @@
 // reference's contract: parts are copied at ltr_MeshAddPart time, outputs are
 // owned by the scene until ltr_DestroyScene, ltr_Start returns at once and
 // ltr_GetStatus polls a bake running on a host thread of its own.
+#include <cuda_runtime.h>
+
 #include <chrono>
 #include <cstring>
 #include <stdexcept>
@@ -25,11 +27,7 @@ ltr_Scene::ltr_Scene()
 
 void ltr_Scene::clear_outputs()
 {
-    for (auto& o : outputs) {
-        delete[] o.lightmap_rgb;
-        delete[] o.normals_xyzf;
-    }
-    outputs.clear();
+    outputs.clear();   // the buffers live in `pinned`, which the next bake reuses
     dump.clear();
 }
 
@@ -37,6 +35,7 @@ ltr_Scene::~ltr_Scene()
 {
     if (worker.joinable()) worker.join();
     clear_outputs();
+    if (pinned) cudaFreeHost(pinned);
     for (HostInst* mi : insts) delete mi;
     for (ltr_Mesh* m : meshes) delete m;
 }

@@ -523,6 +523,53 @@ __global__ void k_table_samples(u32 n, const float4* __restrict__ srad, const u3
     emis[s] = st4(e, 0.0f);
 }
 
+// Patch slot of a sample: (instance, lightmap tile, dominant axis of its
+// unit normal); marks the slot occupied.
+__global__ void k_patch_slots(u32 n, const float4* __restrict__ snrm, const u32* __restrict__ sloc,
+                              const u32* __restrict__ sinst, const u32* __restrict__ inst_w,
+                              const u32* __restrict__ slot_base, const u32* __restrict__ ntx, u32 tile,
+                              u32* __restrict__ slot_of, u32* __restrict__ occ)
+{
+    u32 s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    u32 inst = sinst[s];
+    if (inst == 0) { slot_of[s] = 0xffffffffu; return; }
+    u32 w = inst_w[inst], L = sloc[s];
+    u32 tx = (L % w) / tile, ty = (L / w) / tile;
+    V3 nn = normalized(ld3(snrm[s]));
+    float ax = fabsf(nn.x), ay = fabsf(nn.y), az = fabsf(nn.z);
+    u32 axis = (ax >= ay && ax >= az) ? (nn.x >= 0 ? 0 : 1) : (ay >= az ? (nn.y >= 0 ? 2 : 3) : (nn.z >= 0 ? 4 : 5));
+    u32 slot = slot_base[inst] + (ty * ntx[inst] + tx) * 6 + axis;
+    slot_of[s] = slot;
+    occ[slot] = 1;
+}
+
+// Patch id = rank of the slot among occupied slots; (patch, sample) pairs
+// of the covered samples for the stable sort that lists each patch's samples.
+__global__ void k_patch_ids(u32 n, u32 n_probe, const u32* __restrict__ slot_of, const u32* __restrict__ slot_scan,
+                            int* __restrict__ patch_of, u32* __restrict__ keys, u32* __restrict__ vals)
+{
+    u32 s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    u32 slot = slot_of[s];
+    int p = slot == 0xffffffffu ? -1 : (int) slot_scan[slot];
+    patch_of[s] = p;
+    if (s >= n_probe) {
+        keys[s - n_probe] = (u32) p;
+        vals[s - n_probe] = s;
+    }
+}
+
+// First position of each patch in the sorted list (every patch id occurs).
+__global__ void k_patch_offsets(u32 n, u32 np, const u32* __restrict__ sorted_keys, u32* __restrict__ off)
+{
+    u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    u32 k = sorted_keys[i];
+    if (i == 0 || sorted_keys[i - 1] != k) off[k] = i;
+    if (i == 0) off[np] = n;
+}
+
 // Patch element from its samples (in sample order): total area and
 // area-weighted position, normal, albedo and emission, accumulated in FP64.
 __global__ void k_patch_inputs(u32 np, const u32* __restrict__ off, const u32* __restrict__ idx,
@@ -1084,12 +1131,21 @@ void run_bake(ltr_Scene* S)
     cudaStream_t st = A.st;
 
     // ---- host: transform + lightmap sizing (Job_PreXForm)
+    // LTRG_TRACE=1: host timeline of the bake on stderr
+    const bool trace_on = getenv("LTRG_TRACE") != nullptr;
+    const auto t_start = std::chrono::steady_clock::now();
+    auto TRACE = [&](const char* what) {
+        if (trace_on)
+            fprintf(stderr, "[ltrg] %9.3f ms  %s\n",
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count(), what);
+    };
     S->stage = "transforming spatial data";
     const int n_inst = (int) S->insts.size();
     for (int i = 1; i < n_inst; ++i) prexform(S, S->insts[i]);
     check_abort(S);
 
     // ---- host: triangle soup of shadow parts (Job_ColInfo) + instance boxes
+    TRACE("prexform done");
     S->stage = "generating data structures";
     std::vector<float> tri_xyz;
     std::vector<u32> tri_meta, tri_local;
@@ -1274,6 +1330,7 @@ void run_bake(ltr_Scene* S)
         woff[pass][n_rt] = acc;
     }
 
+    TRACE("host records done");
     // ---- upload
     cudaEvent_t e_up0 = clock.mark();
     const u32 n_probe = (u32) S->samples.size();
@@ -1300,6 +1357,7 @@ void run_bake(ltr_Scene* S)
     cudaEvent_t e_up1 = clock.mark();
     check_abort(S);
 
+    TRACE("upload issued");
     // ---- BVH
     BvhStorage bvh;
     BvhBuildInput bin;
@@ -1330,6 +1388,7 @@ void run_bake(ltr_Scene* S)
     checkpoint("build");
 
     // ---- samples (Job_Samples)
+    TRACE("bvh issued");
     S->stage = "generating samples";
     u32* d_keys = A.zeros<u32>(ntex);
     for (int pass = 0; pass < 2; ++pass) {
@@ -1365,6 +1424,7 @@ void run_bake(ltr_Scene* S)
                            cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     const u32 n_cov = inst_sbeg[n_inst];
+    TRACE("sample counts read");
     const u32 n_samples = n_probe + n_cov;
     S->stats.samples = n_samples;
     // sample ranges: instance 0 = probes [0, n_probe); instance i = n_probe + [scan(tex_off[i]), scan(tex_off[i+1]))
@@ -1439,6 +1499,7 @@ void run_bake(ltr_Scene* S)
         CK(cudaGetLastError());
         checkpoint("sample fixup");
     }
+    TRACE("fixup issued");
     cudaEvent_t e_samples = clock.mark();
     check_abort(S);
 
@@ -1493,6 +1554,7 @@ void run_bake(ltr_Scene* S)
             n_samples, n_lights, d_lights, d_kval, cfg.ambient_color[0], cfg.ambient_color[1], cfg.ambient_color[2], d_lm); note_launch();
         CK(cudaGetLastError());
     }
+    TRACE("direct issued");
     cudaEvent_t e_direct = clock.mark();
 
     // Copies on a side stream overlap the direct-light kernels: the sample
@@ -1514,7 +1576,7 @@ void run_bake(ltr_Scene* S)
             CK(cudaMemcpyAsync(hpos.data(), d_spos, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st2)); note_d2h(n_samples * sizeof(float4));
             CK(cudaMemcpyAsync(hrad.data(), d_srad, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st2)); note_d2h(n_samples * sizeof(float4));
         }
-        if (!gpu_sample_fn || S->opt.radiosity_patches) {   // sample_fn requests and patch grouping
+        if (!gpu_sample_fn) {   // sample_fn requests
             hnrm.resize(n_samples); hloc.resize(n_samples);
             CK(cudaMemcpyAsync(hnrm.data(), d_snrm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st2)); note_d2h(n_samples * sizeof(float4));
             CK(cudaMemcpyAsync(hloc.data(), d_sloc, n_samples * sizeof(u32), cudaMemcpyDeviceToHost, st2)); note_d2h(n_samples * sizeof(u32));
@@ -1530,6 +1592,7 @@ void run_bake(ltr_Scene* S)
     if (do_rad) {
         S->stage = "calculating radiosity";
         CK(cudaStreamSynchronize(st2));
+        TRACE("sample copies done");
         float4* d_diff = A.alloc<float4>(n_samples);
         float4* d_emis = A.alloc<float4>(n_samples);
         std::vector<float4> hdiff, hemis;
@@ -1613,53 +1676,53 @@ void run_bake(ltr_Scene* S)
             S->stats.rad_elements = n_samples;
         } else {
             // Patch mode: group samples by (instance, lightmap tile, dominant
-            // normal axis), first-seen order; dense slot tables, no hashing.
+            // normal axis) on the device. Patches are numbered in slot order;
+            // each patch's samples are listed in sample order (stable sort).
             u32 target = S->opt.radiosity_patches;
             double per = std::max(1.0, (double) n_cov / (double) target);
             u32 tile = (u32) std::max(1.0, std::floor(std::sqrt(per) + 0.5));
-            std::vector<int> patch_of(n_samples, -1);
-            std::vector<u32> slot_base(n_inst + 1, 0);
+            std::vector<u32> slot_base(n_inst + 1, 0), ntx(n_inst, 0);
             for (int i = 0; i < n_inst; ++i) {
                 HostInst* mi = S->insts[i];
-                u32 nslots = mi->container ? 0 : ((mi->w + tile - 1) / tile) * ((mi->h + tile - 1) / tile) * 6;
+                ntx[i] = mi->container ? 0 : (mi->w + tile - 1) / tile;
+                u32 nslots = mi->container ? 0 : ntx[i] * ((mi->h + tile - 1) / tile) * 6;
                 slot_base[i + 1] = slot_base[i] + nslots;
             }
-            std::vector<int> slot_patch(slot_base[n_inst], -1);
-            u32 np = 0;
-            for (int i = 1; i < n_inst; ++i) {
-                HostInst* mi = S->insts[i];
-                u32 ntx = (mi->w + tile - 1) / tile;
-                for (u32 k = 0; k < scount[i]; ++k) {
-                    u32 s = sbeg[i] + k;
-                    u32 L = hloc[s];
-                    u32 tx = (L % mi->w) / tile, ty = (L / mi->w) / tile;
-                    V3 n = normalized(mk(hnrm[s].x, hnrm[s].y, hnrm[s].z));
-                    float ax = fabsf(n.x), ay = fabsf(n.y), az = fabsf(n.z);
-                    u32 axis = (ax >= ay && ax >= az) ? (n.x >= 0 ? 0 : 1) : (ay >= az ? (n.y >= 0 ? 2 : 3) : (n.z >= 0 ? 4 : 5));
-                    u32 slot = slot_base[i] + (ty * ntx + tx) * 6 + axis;
-                    if (slot_patch[slot] < 0) slot_patch[slot] = (int) np++;
-                    patch_of[s] = slot_patch[slot];
-                }
-            }
-            // samples of each patch in sample order (counting sort)
-            std::vector<u32> csr_off(np + 1, 0), csr_idx(n_cov);
-            for (u32 s = 0; s < n_samples; ++s) if (patch_of[s] >= 0) csr_off[patch_of[s] + 1]++;
-            for (u32 p = 0; p < np; ++p) csr_off[p + 1] += csr_off[p];
+            const u32 nslots = slot_base[n_inst];
+            u32* d_slot_base = A.upload(slot_base);
+            u32* d_ntx = A.upload(ntx);
+            u32* d_slot_of = A.alloc<u32>(n_samples);
+            u32* d_occ = A.zeros<u32>(nslots + 1);
+            u32* d_slot_scan = A.alloc<u32>(nslots + 1);
+            k_patch_slots<<<(n_samples + kThreads - 1) / kThreads, kThreads, 0, st>>>(
+                n_samples, d_snrm, d_sloc, d_sinst, d_inst_w, d_slot_base, d_ntx, tile, d_slot_of, d_occ); note_launch();
+            CK(cudaGetLastError());
             {
-                std::vector<u32> fill(csr_off.begin(), csr_off.end() - 1);
-                for (u32 s = 0; s < n_samples; ++s) if (patch_of[s] >= 0) csr_idx[fill[patch_of[s]]++] = s;
+                size_t tb = 0;
+                CK(cub::DeviceScan::ExclusiveSum(nullptr, tb, d_occ, d_slot_scan, (int64_t) (nslots + 1), st));
+                void* tmp = A.alloc<char>(tb);
+                CK(cub::DeviceScan::ExclusiveSum(tmp, tb, d_occ, d_slot_scan, (int64_t) (nslots + 1), st));
             }
+            u32 np = 0;
+            CK(cudaMemcpyAsync(&np, d_slot_scan + nslots, sizeof(u32), cudaMemcpyDeviceToHost, st)); note_d2h(4);
             int* d_patch_of = A.alloc<int>(n_samples);
-            u32* d_csr_off = A.alloc<u32>(np + 1);
+            u32* d_keys_in = A.alloc<u32>(n_cov);
+            u32* d_keys_out = A.alloc<u32>(n_cov);
+            u32* d_vals_in = A.alloc<u32>(n_cov);
             u32* d_csr_idx = A.alloc<u32>(n_cov);
-            CK(cudaMemcpyAsync(d_patch_of, patch_of.data(), n_samples * sizeof(int), cudaMemcpyHostToDevice, st2)); note_h2d(n_samples * sizeof(int));
-            CK(cudaMemcpyAsync(d_csr_off, csr_off.data(), (np + 1) * sizeof(u32), cudaMemcpyHostToDevice, st2)); note_h2d((np + 1) * sizeof(u32));
-            CK(cudaMemcpyAsync(d_csr_idx, csr_idx.data(), n_cov * sizeof(u32), cudaMemcpyHostToDevice, st2)); note_h2d(n_cov * sizeof(u32));
-            cudaEvent_t up = nullptr;
-            CK(cudaEventCreateWithFlags(&up, cudaEventDisableTiming));
-            CK(cudaEventRecord(up, st2));
-            CK(cudaStreamWaitEvent(st, up, 0));
-            cudaEventDestroy(up);
+            k_patch_ids<<<(n_samples + kThreads - 1) / kThreads, kThreads, 0, st>>>(
+                n_samples, n_probe, d_slot_of, d_slot_scan, d_patch_of, d_keys_in, d_vals_in); note_launch();
+            CK(cudaGetLastError());
+            {
+                size_t tb = 0;
+                CK(cub::DeviceRadixSort::SortPairs(nullptr, tb, d_keys_in, d_keys_out, d_vals_in, d_csr_idx, (int) n_cov, 0, 32, st));
+                void* tmp = A.alloc<char>(tb);
+                CK(cub::DeviceRadixSort::SortPairs(tmp, tb, d_keys_in, d_keys_out, d_vals_in, d_csr_idx, (int) n_cov, 0, 32, st));
+            }
+            CK(cudaStreamSynchronize(st));
+            u32* d_csr_off = A.alloc<u32>(np + 1);
+            k_patch_offsets<<<(n_cov + kThreads - 1) / kThreads, kThreads, 0, st>>>(n_cov, np, d_keys_out, d_csr_off); note_launch();
+            CK(cudaGetLastError());
             float4* d_ppos = A.alloc<float4>(np);
             float4* d_pnrm = A.alloc<float4>(np);
             float4* d_pda = A.alloc<float4>(np);
@@ -1677,6 +1740,7 @@ void run_bake(ltr_Scene* S)
             }
             S->stats.rad_elements = np;
         }
+        TRACE("radiosity done");
         S->rad_links = (u32) rr.links;
         S->stats.rad_pairs = rr.pairs;
         S->stats.rad_vis_rays = rr.vis_rays;
@@ -1721,6 +1785,7 @@ void run_bake(ltr_Scene* S)
             CK(cudaGetLastError());
         }
     }
+    TRACE("ao issued");
     cudaEvent_t e_ao1 = clock.mark();
     check_abort(S);
 
@@ -1795,6 +1860,7 @@ void run_bake(ltr_Scene* S)
             CK(cudaGetLastError());
         }
     }
+    TRACE("finalize issued");
     cudaEvent_t e_fin = clock.mark();
 
     // ---- readback
@@ -1802,9 +1868,20 @@ void run_bake(ltr_Scene* S)
     Counters cnt;
     CK(cudaMemcpyAsync(err_words, d_err, sizeof(err_words), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(err_words));
     CK(cudaMemcpyAsync(&cnt, d_cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(Counters));
-    std::vector<float> himg(3 * nout), hnimg(d_nimg ? 4 * nout : 0);
-    if (nout) CK(cudaMemcpyAsync(himg.data(), d_out, himg.size() * sizeof(float), cudaMemcpyDeviceToHost, st)); note_d2h(himg.size() * sizeof(float));
-    if (d_nimg) CK(cudaMemcpyAsync(hnimg.data(), d_nimg, hnimg.size() * sizeof(float), cudaMemcpyDeviceToHost, st)); note_d2h(hnimg.size() * sizeof(float));
+    // Outputs land directly in the scene's page-locked buffer (kept across
+    // bakes, freed with the scene); the work outputs point into it.
+    const size_t out_floats = 3 * (size_t) nout + (d_nimg ? 4 * (size_t) nout : 0);
+    if (S->pinned_bytes < out_floats * sizeof(float)) {
+        if (S->pinned) cudaFreeHost(S->pinned);
+        S->pinned = nullptr;
+        S->pinned_bytes = 0;
+        CK(cudaHostAlloc(&S->pinned, std::max<size_t>(out_floats * sizeof(float), 1), cudaHostAllocDefault));
+        S->pinned_bytes = out_floats * sizeof(float);
+    }
+    float* himg = (float*) S->pinned;
+    float* hnimg = himg + 3 * (size_t) nout;
+    if (nout) CK(cudaMemcpyAsync(himg, d_out, 3 * (size_t) nout * sizeof(float), cudaMemcpyDeviceToHost, st)); note_d2h(3 * (size_t) nout * sizeof(float));
+    if (d_nimg) CK(cudaMemcpyAsync(hnimg, d_nimg, 4 * (size_t) nout * sizeof(float), cudaMemcpyDeviceToHost, st)); note_d2h(4 * (size_t) nout * sizeof(float));
     std::vector<float4> probe_lm(n_probe);
     if (n_probe) CK(cudaMemcpyAsync(probe_lm.data(), d_lm, n_probe * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_probe * sizeof(float4));
     std::vector<float4> dpos, dnrm, drad, dlm;
@@ -1819,6 +1896,7 @@ void run_bake(ltr_Scene* S)
     }
     cudaEvent_t e_down = clock.mark();
     CK(cudaStreamSynchronize(st));
+    TRACE("readback done");
     static const char* kStageName[4] = {"sample fixup", "direct light", "radiosity", "ambient occlusion"};
     for (int k = 0; k < 4; ++k) {
         if (!err_words[k]) continue;
@@ -1836,14 +1914,8 @@ void run_bake(ltr_Scene* S)
     for (int i = 0; i < n_inst; ++i) {
         HostInst* mi = S->insts[i];
         if (mi->container) continue;
-        size_t n = (size_t) out_w[i] * out_h[i];
-        float* img = new float[n * 3];
-        memcpy(img, himg.data() + 3 * out_off[i], n * 3 * sizeof(float));
-        float* nimg = nullptr;
-        if (d_nimg) {
-            nimg = new float[n * 4];
-            memcpy(nimg, hnimg.data() + 4 * out_off[i], n * 4 * sizeof(float));
-        }
+        float* img = himg + 3 * out_off[i];
+        float* nimg = d_nimg ? hnimg + 4 * out_off[i] : nullptr;
         if (cfg.ds2x) { mi->w = out_w[i]; mi->h = out_h[i]; }
         ltr_WorkOutput wo = {(u32) i, mi->mesh->ident.c_str(), mi->mesh->ident.size(), mi->ident.c_str(),
                              mi->ident.size(), img, nimg, out_w[i], out_h[i]};

@@ -61,7 +61,9 @@ struct ltr_Scene {
     std::vector<lg::HostInst*> insts;   // [0] = probe-sample container
     std::vector<lg::HostLight> lights;
     std::vector<ltr_SampleInfo> samples;
-    std::vector<ltr_WorkOutput> outputs;
+    std::vector<ltr_WorkOutput> outputs;   // buffers point into `pinned`
+    void* pinned = nullptr;                 // page-locked output storage, reused across bakes
+    size_t pinned_bytes = 0;
     std::vector<lg::SampleDump> dump;
     lg::u32 rad_links = 0;
     ltrg_Stats stats;
