@@ -304,10 +304,11 @@ __device__ __forceinline__ float inv_shadow(const BvhView& bvh, V3 from, V3 to, 
     float maxt = len(to - from);
     float res = 1.0f;
     // Warm start: the nearest triangle of the previous point lies within
-    // h_prev + step of the next one, so the query starts with that radius
-    // (plus slack for rounding) instead of MAX_PENUMBRA_SIZE. If nothing lies
-    // inside it, the query is repeated with the full radius, so the result is
-    // the reference's min(MAX_PENUMBRA_SIZE, nearest distance) either way.
+    // h_prev + step of the next one (triangle inequality), so the query starts
+    // with that radius (plus slack for rounding) instead of MAX_PENUMBRA_SIZE.
+    // If nothing lies inside it, the query is repeated with the full radius,
+    // so the result is the reference's min(MAX_PENUMBRA_SIZE, nearest distance)
+    // either way (Distance() starts at MAX_PENUMBRA_SIZE, lighter.cpp:150-188).
     float reach = kMaxPenumbraSize;
     for (float t = 0.001f; t < maxt;) {
         V3 p = from + rd * t;

@@ -80,20 +80,27 @@ __device__ __forceinline__ NodeBoxes load_node(const BvhView& b, int n)
 }
 
 // Segment o + t*d, t in [0, tlimit], against a box; returns the entry t.
-__device__ __forceinline__ bool slab(V3 mn, V3 mx, V3 o, V3 inv, float tlimit, float& tin)
+// `oinv` = o * inv, so each plane costs one FMA; the boxes are inflated, so
+// the FMA's different rounding cannot drop a triangle the exact test keeps.
+__device__ __forceinline__ bool slab(V3 mn, V3 mx, V3 oinv, V3 inv, float tlimit, float& tin)
 {
-    float tx0 = (mn.x - o.x) * inv.x, tx1 = (mx.x - o.x) * inv.x;
-    float ty0 = (mn.y - o.y) * inv.y, ty1 = (mx.y - o.y) * inv.y;
-    float tz0 = (mn.z - o.z) * inv.z, tz1 = (mx.z - o.z) * inv.z;
+    float tx0 = __fmaf_rn(mn.x, inv.x, -oinv.x), tx1 = __fmaf_rn(mx.x, inv.x, -oinv.x);
+    float ty0 = __fmaf_rn(mn.y, inv.y, -oinv.y), ty1 = __fmaf_rn(mx.y, inv.y, -oinv.y);
+    float tz0 = __fmaf_rn(mn.z, inv.z, -oinv.z), tz1 = __fmaf_rn(mx.z, inv.z, -oinv.z);
     float t0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
     float t1 = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tlimit));
     tin = t0;
     return t0 <= t1;
 }
 
+// 1/d with zero components replaced by +-1e-30 (finite, no NaN in the slab).
 __device__ __forceinline__ V3 inv_dir(V3 d)
 {
-    return mk(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    const float tiny = 1e-30f;
+    float x = fabsf(d.x) < tiny ? copysignf(tiny, d.x) : d.x;
+    float y = fabsf(d.y) < tiny ? copysignf(tiny, d.y) : d.y;
+    float z = fabsf(d.z) < tiny ? copysignf(tiny, d.z) : d.z;
+    return mk(1.0f / x, 1.0f / y, 1.0f / z);
 }
 
 // Squared distance from p to a box (0 inside).
@@ -119,6 +126,7 @@ __device__ __forceinline__ void walk_segment(const BvhView& b, V3 o, V3 e, ErrFl
     if (b.n_tris <= 0) return;
     V3 d = e - o;
     V3 inv = inv_dir(d);
+    V3 oinv = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
     float tlimit = 1.0f;
     int stack[kStack];
     float stack_t[kStack];
@@ -128,8 +136,8 @@ __device__ __forceinline__ void walk_segment(const BvhView& b, V3 o, V3 e, ErrFl
         if (cur >= 0) {
             NodeBoxes nb = load_node(b, cur);
             float tl, tr;
-            bool hl = slab(nb.lmin, nb.lmax, o, inv, tlimit, tl);
-            bool hr = slab(nb.rmin, nb.rmax, o, inv, tlimit, tr);
+            bool hl = slab(nb.lmin, nb.lmax, oinv, inv, tlimit, tl);
+            bool hr = slab(nb.rmin, nb.rmax, oinv, inv, tlimit, tr);
             if (hl && hr) {
                 bool lfirst = tl <= tr;
                 if (sp < kStack) { stack[sp] = lfirst ? nb.r : nb.l; stack_t[sp] = lfirst ? tr : tl; ++sp; }
@@ -265,7 +273,7 @@ __device__ __forceinline__ float bvh_closest_inst(const BvhView& b, V3 o, V3 e, 
 // lighter_math.cpp:954-989). The reference shrinks a query cube; a sphere
 // test against the child boxes prunes the same triangles.
 __device__ __forceinline__ float bvh_distance(const BvhView& b, V3 p, float d0, ErrFlag err, u32* visits = nullptr,
-                                              u32* tests = nullptr)
+                                              u32* tests = nullptr, int* best_leaf = nullptr)
 {
     u32 nt = 0;
     float dist = d0;
@@ -298,7 +306,10 @@ __device__ __forceinline__ float bvh_distance(const BvhView& b, V3 p, float d0, 
             if (meta & kOccluderBit) {
                 float nd = point_tri_dist_rec(b, t, p);
                 ++nt;
-                if (nd < dist) dist = nd;
+                if (nd < dist) {
+                    dist = nd;
+                    if (best_leaf) *best_leaf = t;
+                }
             }
         }
         bool done = false;
