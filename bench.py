@@ -53,6 +53,14 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+def _peaks_tensor():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"])
+    except Exception:
+        return 1900.0
+
+
 def _traffic_from_profile():
     """dram bytes per launch of the direct-light kernel from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "k_direct_mid.md")
@@ -220,6 +228,84 @@ def run_ours(args, world, rank, local, dist):
     return rays, dev_ms, wall, stats, clocks, stats[-1]["bytes_h2d"], stats[-1]["bytes_d2h"], launches
 
 
+GATHER_WORKLOAD = ("multi-RHS radiosity: seeded room with furniture, {n} patches, {t} triangles, "
+                   "{c} light configurations (R = {r} RGB right-hand sides), {b} bounces")
+GATHER_MODES = [("fp32", 0, 0), ("fp16_rhs", 1, 1), ("fp16", 1, 0), ("bf16_rhs", 2, 1), ("fp16_full", 1, 2),
+                ("bf16_full", 2, 2)]
+
+
+def run_gather(args, local):
+    """Form factors once, then timed solves of every precision mode on device-resident
+    inputs; errors against an FP64 Jacobi (torch float64 on the device over the FP32
+    form factors) for the first 8 configurations."""
+    import numpy as np
+    import torch
+
+    from lighter_gb300 import library, patches
+    from lighter_gb300.gather import Gather
+
+    lib = library()
+    sc = patches.room(seed=1, n_patches=args.gather_patches, n_configs=args.gather_configs)
+    n, R, bounces = len(sc["pos"]), sc["emission"].shape[1], args.gather_bounces
+    dev = torch.device("cuda", local)
+    out = {"workload": GATHER_WORKLOAD.format(n=n, t=len(sc["tri"]), c=args.gather_configs, r=R, b=bounces)}
+    with Gather(lib, sc["tri"], sc["pos"], sc["nrm"], sc["area"], device=local) as g:
+        alb = torch.from_numpy(sc["albedo"]).to(dev)
+        E = torch.from_numpy(sc["emission"]).to(dev)
+        B = torch.empty((n, R), dtype=torch.float32, device=dev)
+        # FP64 reference for the first 8 configurations
+        ncheck = min(R, 24)
+        Gd = torch.from_numpy(g.G()).to(dev)
+        albc = alb[:, torch.arange(ncheck, device=dev) % 3].double()
+        E64 = E[:, :ncheck].double()
+        B64 = E64.clone()
+        for _ in range(bounces):
+            X = albc * B64
+            Y = torch.empty_like(B64)
+            for r0 in range(0, n, 4096):
+                Y[r0:r0 + 4096] = Gd[r0:r0 + 4096].double() @ X
+            B64 = E64 + Y
+        del Gd
+        torch.cuda.empty_cache()
+        modes = {}
+        for name, prec, refine in GATHER_MODES:
+            st = g.solve_device(alb.data_ptr(), E.data_ptr(), R, bounces, B.data_ptr(), prec, refine)   # warm-up
+            conv = st["ms_convert"]
+            per = []
+            for _ in range(args.gather_steps):
+                st = g.solve_device(alb.data_ptr(), E.data_ptr(), R, bounces, B.data_ptr(), prec, refine)
+                per.append(st)
+            d = B[:, :ncheck].double() - B64
+            fro = float(torch.linalg.norm(d) / torch.linalg.norm(B64))
+            mx = float((d.abs() / B64.abs().amax(dim=0, keepdim=True).clamp_min(1e-30)).max())
+            spb = statistics.median(p["ms_per_bounce"] for p in per) / 1000.0
+            gemm = statistics.median(p["ms_gemm"] for p in per) / 1000.0 / max(1, bounces)
+            modes[name] = {
+                "s_per_bounce": spb, "gemm_s_per_bounce": gemm,
+                "tflops": st["flops_per_bounce"] / gemm / 1e12 if gemm > 0 else 0.0,
+                "f_gbs": st["bytes_per_bounce"] / gemm / 1e9 if gemm > 0 else 0.0,
+                "bytes_per_bounce": st["bytes_per_bounce"], "products": st["products"],
+                "tensor_cores": bool(st["tensor_cores"]), "stages": st["stages"], "ctas": st["ctas"],
+                "convert_ms": conv, "rel_err_fro_vs_fp64": fro, "rel_err_max_vs_fp64": mx,
+            }
+        # end to end through the host-buffer entry point (inputs and result cross PCIe/C2C)
+        t0 = time.perf_counter()
+        for _ in range(args.gather_steps):
+            g.solve(sc["albedo"], sc["emission"], bounces, 1, 1)
+        e2e = (time.perf_counter() - t0) / args.gather_steps
+        st0 = g.solve_device(alb.data_ptr(), E.data_ptr(), R, 0, B.data_ptr(), 1, 1)
+        out.update({
+            "build_ms": st0["ms_build"], "visibility_rays": st0["vis_rays"], "links": st0["links"],
+            "visibility_rays_per_s": st0["vis_rays"] / (st0["ms_build"] / 1000.0),
+            "modes": modes,
+            "e2e_s_per_solve_fp16_rhs": e2e, "e2e_bytes": {"h2d": int(n * (R + 3) * 4), "d2h": int(n * R * 4)},
+            "speedup_fp16_rhs_vs_fp32": modes["fp32"]["s_per_bounce"] / modes["fp16_rhs"]["s_per_bounce"],
+            "error_reference": "FP64 Jacobi (torch float64 on the device) over the FP32 form factors, "
+                               "first %d right-hand sides" % ncheck,
+        })
+    return out
+
+
 def _bake_once(lib, scene):
     lib.ltr_Start(scene)
     if not lib.ltrg_Wait(scene):
@@ -237,6 +323,11 @@ def main():
     ap.add_argument("--patches", type=int, default=16384)
     ap.add_argument("--cpu-lm", type=int, default=256, help="lightmap side of the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--gather-patches", type=int, default=32768)
+    ap.add_argument("--gather-configs", type=int, default=64)
+    ap.add_argument("--gather-bounces", type=int, default=4)
+    ap.add_argument("--gather-steps", type=int, default=3)
+    ap.add_argument("--no-gather", action="store_true")
     args = ap.parse_args()
     world, rank, local, dist = _dist()
     if args.impl == "reference":
@@ -295,6 +386,18 @@ def main():
                                                     "ms_rad_bounce", "ms_ao", "ms_finalize", "ms_download",
                                                     "ms_device", "ms_total")},
     }
+    if not args.no_gather:
+        gat = run_gather(args, 0)
+        line["gather"] = gat
+        peak_tf = _peaks_tensor()
+        m = gat["modes"]["fp16_rhs"]
+        line["s_per_bounce"] = {"gather_fp16_rhs": m["s_per_bounce"], "gather_fp32": gat["modes"]["fp32"]["s_per_bounce"],
+                                "bake_mid_fp32": line["s_per_bounce"]}
+        line["gather_roofline"] = {
+            "kernel": "k_umma_gather (tcgen05, FP16 G, split right-hand side)", "bound": "hbm",
+            "achieved": m["f_gbs"], "peak": peak, "unit": "GB/s", "frac": m["f_gbs"] / peak,
+            "tensor_tflops": m["tflops"], "tensor_peak_tflops": peak_tf, "tensor_frac": m["tflops"] / peak_tf,
+            "traffic": None}
     if not args.no_cpu_baseline:
         from lighter_gb300 import scenes
         threads = os.cpu_count() or 1

@@ -116,6 +116,67 @@ LTRAPI LTRBOOL ltrg_TableSampleFn(ltr_Config* config, ltr_SampleRequest* req);
 LTRAPI int ltrg_FinalizeLightmapNoAlloc(const float* rgb, const unsigned char* mask, float* out, u32 width,
                                         u32 height, float blur_size, void* stream);
 
+/* Multi-right-hand-side radiosity gather. The reference runs its bounces
+ * (Int_RDBounce, lighter.cpp:767-797) for one light configuration at a time,
+ * over sparse links; here the form factors of a patch set are built once as
+ * a dense matrix and many light configurations are bounced together:
+ *   B_0 = E,  B_k = E + K B_{k-1},  K_ij = F_ij * area_j * albedo_j(c)
+ * for R right-hand sides (column r uses albedo channel c = r mod 3, so R =
+ * 3 x configurations for RGB). F_ij is the reference's pair factor
+ * (lighter.cpp:733-757) for pairs that pass the link predicate, 0 elsewhere.
+ *
+ * ltrg_GatherCreate traces the visibility rays and keeps G_ij = F_ij * area_j
+ * in FP32 on the device.
+ *   tri_xyz  n_tris x 9 floats: occluders (world space)
+ *   pos3, nrm3, area  per patch (normals need not be unit length)
+ *   links    LTRG_LINKS_*
+ * Returns NULL on error (message on stderr). */
+typedef struct ltrg_Gather ltrg_Gather;
+
+/* Contraction of one bounce for FP16/BF16 storage (ignored for FP32):
+ *   LTRG_REFINE_NONE   G16 x X16, one tensor-core product
+ *   LTRG_REFINE_RHS    X split into a 16-bit head and tail (two products), so
+ *                      only G's own rounding remains
+ *   LTRG_REFINE_FULL   also G's rounding residual G - G16, kept as a second
+ *                      16-bit matrix, contracted with the head and added in
+ *                      FP32 (three products; FP32-level accuracy) */
+#define LTRG_REFINE_NONE 0
+#define LTRG_REFINE_RHS  1
+#define LTRG_REFINE_FULL 2
+
+typedef struct ltrg_GatherStats {
+    double ms_build;        /* form factors (pair tests + visibility rays), CUDA events */
+    double ms_convert;      /* FP32 -> 16-bit copies of G made by this solve (0 when cached) */
+    double ms_bounces;      /* all bounces, CUDA events */
+    double ms_per_bounce;   /* ms_bounces / bounces */
+    double ms_gemm;         /* contraction kernels only, summed over the bounces */
+    double flops_per_bounce;     /* 2 n^2 R per product issued */
+    uint64_t bytes_per_bounce;   /* bytes of G (and residual) streamed per bounce */
+    uint64_t links, vis_rays, pairs;
+    int32_t tensor_cores;   /* 1 when the tcgen05 path ran */
+    int32_t stages, ctas, products;
+    uint32_t reserved[8];
+} ltrg_GatherStats;
+
+LTRAPI ltrg_Gather* ltrg_GatherCreate(const float* tri_xyz, u32 n_tris, const float* pos3, const float* nrm3,
+                                      const float* area, u32 n, int links, int device);
+LTRAPI void ltrg_GatherDestroy(ltrg_Gather* g);
+LTRAPI u32 ltrg_GatherSize(ltrg_Gather* g);
+/* Copies G (n x n FP32, row-major) to host memory. */
+LTRAPI LTRBOOL ltrg_GatherGetG(ltrg_Gather* g, float* out);
+LTRAPI const char* ltrg_GatherLastError(ltrg_Gather* g);
+/* B after `bounces` sweeps for R right-hand sides; host buffers:
+ *   albedo_rgb n x 3, emission n x R, out n x R (row-major).
+ * precision LTRG_F_*, refine LTRG_REFINE_*; R <= 192 for FP16/BF16.
+ * Returns 1, or 0 with ltrg_GatherLastError set. */
+LTRAPI LTRBOOL ltrg_GatherSolve(ltrg_Gather* g, const float* albedo_rgb, const float* emission, u32 R, int bounces,
+                                int precision, int refine, float* out, ltrg_GatherStats* stats);
+/* Same on device buffers of the gather's device, enqueued on `stream` (NULL:
+ * the gather's own stream) and completed before return. */
+LTRAPI LTRBOOL ltrg_GatherSolveDevice(ltrg_Gather* g, const float* albedo_rgb, const float* emission, u32 R,
+                                      int bounces, int precision, int refine, float* out, ltrg_GatherStats* stats,
+                                      void* stream);
+
 /* Read-only introspection of a finished bake (requires keep_samples = 1).
  * Instance 0 is the probe-sample container of ltr_SampleAdd, as in the
  * reference (lighter_int.hpp:975-980). */

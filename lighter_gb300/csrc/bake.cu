@@ -1112,6 +1112,12 @@ std::vector<float> gauss_taps(int ext, float radius)
 
 }  // namespace
 
+void build_refs_host(const std::vector<float>& xyz, std::vector<u32>& ref_tri, std::vector<float>& ref_box, float* cmin,
+                     float* cmax)
+{
+    build_refs(xyz, ref_tri, ref_box, cmin, cmax);
+}
+
 // ----------------------------------------------------------------------------- the bake
 
 void run_bake(ltr_Scene* S)

@@ -18,6 +18,7 @@
 #pragma once
 
 #include <string>
+#include <vector>
 
 #include "common.cuh"
 
@@ -355,5 +356,11 @@ struct BvhStorage {
 void bvh_build(const BvhBuildInput& in, BvhStorage& out, void* stream);
 void bvh_free(BvhStorage& s, void* stream);
 std::string bvh_validate(const BvhStorage& s, void* stream);
+
+// Leaf references of a triangle soup (9 floats per triangle): oversized
+// triangles are split into several references with clipped boxes; cmin/cmax
+// receive the bounds of the reference box centres (bake.cu).
+void build_refs_host(const std::vector<float>& xyz, std::vector<u32>& ref_tri, std::vector<float>& ref_box, float* cmin,
+                     float* cmax);
 
 }  // namespace lg

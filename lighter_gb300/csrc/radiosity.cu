@@ -210,6 +210,29 @@ RadResult radiosity_solve_dev(const RadDevInputs& in, const RadSettings& rs, con
     return solve_t<float>(in, rs, bvh, err, st, total_out, abort_flag);
 }
 
+RadFormFactors radiosity_form_factors_f32(uint32_t n, const float4* pos, const float4* nrm, const BvhView& bvh,
+                                          ErrFlag err, int links, float* F, cudaStream_t st)
+{
+    RadFormFactors out;
+    if (n == 0) return out;
+    u32 nb = (n + 31) / 32;
+    if (nb > 65535) throw std::runtime_error("radiosity: too many elements for the tile grid");
+    unsigned long long* counts = nullptr;
+    RCK(cudaMallocAsync(&counts, 2 * sizeof(unsigned long long), st));
+    RCK(cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned long long), st));
+    dim3 grid(nb, nb), block(32, 8);
+    k_form_factors<float><<<grid, block, 0, st>>>(n, pos, nrm, bvh, err, links, F, counts); note_launch();
+    cudaError_t le = cudaGetLastError();
+    unsigned long long hc[2] = {0, 0};
+    if (le == cudaSuccess) le = cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(counts, st);
+    RCK(le);
+    RCK(cudaStreamSynchronize(st));
+    out.links = hc[0];
+    out.vis_rays = hc[1];
+    return out;
+}
+
 RadResult radiosity_solve(const RadInputs& in, const RadSettings& rs, const BvhView& bvh, ErrFlag err, cudaStream_t st,
                           float4* lm_out, std::atomic<bool>* abort_flag)
 {

@@ -50,6 +50,15 @@ struct RadDevInputs {
 RadResult radiosity_solve_dev(const RadDevInputs& in, const RadSettings& rs, const BvhView& bvh, ErrFlag err,
                               cudaStream_t st, float4* total_out, std::atomic<bool>* abort_flag);
 
+// Only the form factors: F (n x n FP32, row-major) with the pair test and the
+// `links` predicate; returns the link and visibility-ray counts (synchronises
+// the stream).
+struct RadFormFactors {
+    uint64_t links = 0, vis_rays = 0;
+};
+RadFormFactors radiosity_form_factors_f32(uint32_t n, const float4* pos, const float4* nrm, const BvhView& bvh,
+                                          ErrFlag err, int links, float* F, cudaStream_t st);
+
 // Same from host vectors (uploads them first).
 RadResult radiosity_solve(const RadInputs& in, const RadSettings& rs, const BvhView& bvh, ErrFlag err, cudaStream_t st,
                           float4* lm_out, std::atomic<bool>* abort_flag);

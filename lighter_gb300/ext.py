@@ -62,3 +62,31 @@ NOALLOC_MAX_TEXELS = 1 << 20
 NOALLOC_OK, NOALLOC_EINVAL, NOALLOC_ETOOBIG, NOALLOC_ECUDA = 0, -1, -2, -3
 EXT_API["ltrg_FinalizeLightmapNoAlloc"] = (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, u32, u32, C.c_float,
                                                      C.c_void_p])
+
+# Multi-right-hand-side radiosity gather (include/lighter_gb300.h).
+LTRG_REFINE_NONE = 0
+LTRG_REFINE_RHS = 1
+LTRG_REFINE_FULL = 2
+
+
+class GatherStats(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "ms_build", "ms_convert", "ms_bounces", "ms_per_bounce", "ms_gemm", "flops_per_bounce")] + [
+        (n, C.c_uint64) for n in ("bytes_per_bounce", "links", "vis_rays", "pairs")] + [
+        (n, C.c_int32) for n in ("tensor_cores", "stages", "ctas", "products")] + [("reserved", u32 * 8)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
+
+
+EXT_API.update({
+    "ltrg_GatherCreate": (C.c_void_p, [C.c_void_p, u32, C.c_void_p, C.c_void_p, C.c_void_p, u32, C.c_int, C.c_int]),
+    "ltrg_GatherDestroy": (None, [C.c_void_p]),
+    "ltrg_GatherSize": (u32, [C.c_void_p]),
+    "ltrg_GatherGetG": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ltrg_GatherLastError": (C.c_char_p, [C.c_void_p]),
+    "ltrg_GatherSolve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, u32, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                                   C.POINTER(GatherStats)]),
+    "ltrg_GatherSolveDevice": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, u32, C.c_int, C.c_int, C.c_int,
+                                         C.c_void_p, C.POINTER(GatherStats), C.c_void_p]),
+})

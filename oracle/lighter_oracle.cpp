@@ -1501,6 +1501,49 @@ API void orc_GetCounters(unsigned long long* out)
     out[0] = g_shadow_evals; out[1] = g_distance_queries; out[2] = g_ao_rays; out[3] = g_rad_vis;
 }
 
+// Form factors of a patch set, for checking the multi-right-hand-side gather:
+// the reference's pair test and factor (lighter.cpp:733-757) and its
+// VisibilityTest (lighter.cpp:138-147: segment shrunk by SMALL_FLOAT at both
+// ends, any hit in the triangle tree, lighter_math.cpp:804-832) over one tree
+// of all triangles (9 floats each). G_ij = f_ij * area_j for pairs that pass
+// the predicate (links 0: occluded, as the reference; 1: unoccluded), else 0.
+API void orc_gather_form_factors(const float* tri9, u32 n_tris, const float* pos3, const float* nrm3,
+                                 const float* area, u32 n, int links, float* G, int threads)
+{
+    std::vector<Tri> tris(n_tris);
+    for (u32 t = 0; t < n_tris; ++t) {
+        const float* q = tri9 + 9 * (size_t) t;
+        tris[t].P1 = mk(q[0], q[1], q[2]);
+        tris[t].P2 = mk(q[3], q[4], q[5]);
+        tris[t].P3 = mk(q[6], q[7], q[8]);
+    }
+    TriTree tree;
+    tree.set(tris.data(), tris.size());
+    std::vector<V3> P(n), N(n);
+    for (u32 i = 0; i < n; ++i) {
+        P[i] = mk(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2]);
+        N[i] = normalized(mk(nrm3[3 * i], nrm3[3 * i + 1], nrm3[3 * i + 2]));
+    }
+    memset(G, 0, sizeof(float) * (size_t) n * n);
+    parallel_for(threads, n, [&](size_t i) {
+        V3 AP = P[i], AN = N[i];
+        for (size_t j = i + 1; j < n; ++j) {
+            V3 BP = P[j], BN = N[j];
+            V3 pd = BP - AP;
+            float dA = dot(AN, pd), dB = dot(BN, -pd);
+            if (dA <= kSmall || dB <= kSmall) continue;
+            float l2 = lensq(pd);
+            float f = dA * dB / (l2 * l2 * (float) M_PI);
+            if (f < kSmall) continue;
+            V3 dn = normalized(BP - AP);
+            bool occ = tree.any_hit(AP + dn * kSmall, BP - dn * kSmall);
+            if ((links == 0) != occ) continue;
+            G[i * n + j] = f * area[j];
+            G[j * n + i] = f * area[i];
+        }
+    });
+}
+
 struct ltrg_SampleTable { u32 count; const float* diffuse_rgb; const float* emissive_rgb; };
 API int ltrg_TableSampleFn(ltr_Config* cfg, ltr_SampleRequest* req)
 {
