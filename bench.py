@@ -230,8 +230,9 @@ def run_ours(args, world, rank, local, dist):
 
 GATHER_WORKLOAD = ("multi-RHS radiosity: seeded room with furniture, {n} patches, {t} triangles, "
                    "{c} light configurations (R = {r} RGB right-hand sides), {b} bounces")
-GATHER_MODES = [("fp32", 0, 0), ("fp16_rhs", 1, 1), ("fp16", 1, 0), ("bf16_rhs", 2, 1), ("fp16_full", 1, 2),
-                ("bf16_full", 2, 2)]
+# (name, precision, refine, TMEM accumulation length in k blocks)
+GATHER_MODES = [("fp32", 0, 0, 0), ("fp16", 1, 0, 0), ("fp16_rhs", 1, 1, 0), ("bf16_rhs", 2, 1, 0),
+                ("fp16_full", 1, 2, 0), ("bf16_full", 2, 2, 0), ("fp16_full_chunk64", 1, 2, 64)]
 
 
 def run_gather(args, local):
@@ -265,10 +266,25 @@ def run_gather(args, local):
             for r0 in range(0, n, 4096):
                 Y[r0:r0 + 4096] = Gd[r0:r0 + 4096].double() @ X
             B64 = E64 + Y
-        del Gd
+        # library reference point for plain FP32 on the GPU: cuBLAS SGEMM (TF32 off) of one bounce
+        tf32 = torch.backends.cuda.matmul.allow_tf32
+        torch.backends.cuda.matmul.allow_tf32 = False
+        X32 = alb[:, torch.arange(R, device=dev) % 3] * E
+        for _ in range(2):
+            Yc = torch.mm(Gd, X32)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record()
+        for _ in range(3):
+            Yc = E + torch.mm(Gd, X32)
+        ev[1].record()
+        torch.cuda.synchronize()
+        cublas_s = ev[0].elapsed_time(ev[1]) / 3 / 1000.0
+        torch.backends.cuda.matmul.allow_tf32 = tf32
+        del Gd, X32, Yc
         torch.cuda.empty_cache()
         modes = {}
-        for name, prec, refine in GATHER_MODES:
+        for name, prec, refine, chunk in GATHER_MODES:
+            g.set_chunk(chunk)
             st = g.solve_device(alb.data_ptr(), E.data_ptr(), R, bounces, B.data_ptr(), prec, refine)   # warm-up
             conv = st["ms_convert"]
             per = []
@@ -286,8 +302,9 @@ def run_gather(args, local):
                 "f_gbs": st["bytes_per_bounce"] / gemm / 1e9 if gemm > 0 else 0.0,
                 "bytes_per_bounce": st["bytes_per_bounce"], "products": st["products"],
                 "tensor_cores": bool(st["tensor_cores"]), "stages": st["stages"], "ctas": st["ctas"],
-                "convert_ms": conv, "rel_err_fro_vs_fp64": fro, "rel_err_max_vs_fp64": mx,
+                "convert_ms": conv, "rel_err_fro_vs_fp64": fro, "rel_err_max_vs_fp64": mx, "k_chunk": chunk,
             }
+        g.set_chunk(0)
         # end to end through the host-buffer entry point (inputs and result cross PCIe/C2C)
         t0 = time.perf_counter()
         for _ in range(args.gather_steps):
@@ -300,6 +317,9 @@ def run_gather(args, local):
             "modes": modes,
             "e2e_s_per_solve_fp16_rhs": e2e, "e2e_bytes": {"h2d": int(n * (R + 3) * 4), "d2h": int(n * R * 4)},
             "speedup_fp16_rhs_vs_fp32": modes["fp32"]["s_per_bounce"] / modes["fp16_rhs"]["s_per_bounce"],
+            "speedup_fp16_vs_fp32": modes["fp32"]["s_per_bounce"] / modes["fp16"]["s_per_bounce"],
+            "fp32_cublas_sgemm_s_per_bounce": cublas_s,
+            "speedup_fp16_vs_cublas_fp32": cublas_s / modes["fp16"]["s_per_bounce"],
             "error_reference": "FP64 Jacobi (torch float64 on the device) over the FP32 form factors, "
                                "first %d right-hand sides" % ncheck,
         })

@@ -133,13 +133,17 @@ LTRAPI int ltrg_FinalizeLightmapNoAlloc(const float* rgb, const unsigned char* m
  * Returns NULL on error (message on stderr). */
 typedef struct ltrg_Gather ltrg_Gather;
 
-/* Contraction of one bounce for FP16/BF16 storage (ignored for FP32):
+/* Contraction of one bounce for FP16/BF16 storage (ignored for FP32). Both
+ * operands are scaled by exact powers of two (G's peak near 2^14, the
+ * emission peak at 2^9) so that FP16 keeps small values out of its subnormal
+ * range; the scaling is undone in FP32.
  *   LTRG_REFINE_NONE   G16 x X16, one tensor-core product
  *   LTRG_REFINE_RHS    X split into a 16-bit head and tail (two products), so
  *                      only G's own rounding remains
  *   LTRG_REFINE_FULL   also G's rounding residual G - G16, kept as a second
  *                      16-bit matrix, contracted with the head and added in
- *                      FP32 (three products; FP32-level accuracy) */
+ *                      FP32 (three products; about 2^-16 relative per entry
+ *                      for BF16 and 2^-22 for FP16) */
 #define LTRG_REFINE_NONE 0
 #define LTRG_REFINE_RHS  1
 #define LTRG_REFINE_FULL 2
@@ -161,13 +165,21 @@ typedef struct ltrg_GatherStats {
 LTRAPI ltrg_Gather* ltrg_GatherCreate(const float* tri_xyz, u32 n_tris, const float* pos3, const float* nrm3,
                                       const float* area, u32 n, int links, int device);
 LTRAPI void ltrg_GatherDestroy(ltrg_Gather* g);
+/* Accumulation length of the tensor-core path: the FP32 accumulator in TMEM
+ * takes k_blocks x 64 products per row before it is added (round to nearest)
+ * into the FP32 workspace and restarted. The tensor cores' own accumulation
+ * drifts by a small systematic amount per step (about 1e-5 relative after
+ * 32k products), which this bounds at the cost of workspace traffic. 0: no
+ * limit (default). */
+LTRAPI LTRBOOL ltrg_GatherSetChunk(ltrg_Gather* g, u32 k_blocks);
 LTRAPI u32 ltrg_GatherSize(ltrg_Gather* g);
 /* Copies G (n x n FP32, row-major) to host memory. */
 LTRAPI LTRBOOL ltrg_GatherGetG(ltrg_Gather* g, float* out);
 LTRAPI const char* ltrg_GatherLastError(ltrg_Gather* g);
 /* B after `bounces` sweeps for R right-hand sides; host buffers:
  *   albedo_rgb n x 3, emission n x R, out n x R (row-major).
- * precision LTRG_F_*, refine LTRG_REFINE_*; R <= 192 for FP16/BF16.
+ * precision LTRG_F_*, refine LTRG_REFINE_*; for FP16/BF16 R <= 256 (R <= 192
+ * with LTRG_REFINE_FULL).
  * Returns 1, or 0 with ltrg_GatherLastError set. */
 LTRAPI LTRBOOL ltrg_GatherSolve(ltrg_Gather* g, const float* albedo_rgb, const float* emission, u32 R, int bounces,
                                 int precision, int refine, float* out, ltrg_GatherStats* stats);

@@ -193,6 +193,7 @@ struct UmmaArgs {
     u32 mode;             // LTRG_REFINE_*
     u32 idesc;
     u32 max_slots;
+    u32 kchunk;           // k blocks accumulated in TMEM before moving to the FP32 workspace (0: no limit)
     const u32* rp_first;  // first CTA whose range touches each row block
     float* partial;       // [rp][slot][R][256]
     u32* err;
@@ -267,8 +268,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             u32 seg = 0;
             for (uint64_t u = lo; u < hi; ++u, ++i) {
                 const u32 kb = (u32) (u % a.nkb);
-                const bool first = u == lo || kb == 0;
-                const bool last = u + 1 == hi || kb + 1 == a.nkb;
+                const bool first = u == lo || kb == 0 || (a.kchunk && kb % a.kchunk == 0);
+                const bool last = u + 1 == hi || kb + 1 == a.nkb || (a.kchunk && (kb + 1) % a.kchunk == 0);
                 if (first && seg > 0 && !mbar_wait(acce, (seg - 1) & 1u, a.err, kErrMma)) break;
                 const u32 s = (u32) (i % a.stages);
                 if (!mbar_wait(&full[s], (u32) (i / a.stages) & 1u, a.err, kErrMma)) break;
@@ -295,30 +296,43 @@ __global__ void __launch_bounds__(kThreads, 1)
     } else {
         // epilogue: TMEM lanes of quadrant q = rows 32q .. 32q+31 of each 128-row half
         const int q = warp & 3;
-        if (hi > lo) {
-            const u32 rp0 = (u32) (lo / a.nkb), rp1 = (u32) ((hi - 1) / a.nkb);
-            for (u32 rp = rp0, seg = 0; rp <= rp1; ++rp, ++seg) {
-                // every lane waits; the warp goes on only if all of them saw the phase, so the
-                // .sync.aligned loads below always run converged
-                const bool ok = mbar_wait(accf, seg & 1u, a.err, kErrEpilogue);
-                if (!__all_sync(0xffffffffu, ok)) break;
-                tc_fence_after();
-                const u32 slot = blockIdx.x - __ldg(&a.rp_first[rp]);
-                float* P = a.partial + ((size_t) rp * a.max_slots + slot) * a.R * ROWS;
-                for (int h = 0; h < 2; ++h) {
-                    const u32 row = h * BM + q * 32 + lane;
-                    for (u32 c0 = 0; c0 < a.BN; c0 += 32) {
-                        uint32_t v[32];
-                        tmem_ld32(tmem + ((uint32_t) (q * 32) << 16) + h * 256 + c0, v);
+        // Segments (the MMA issuer's accumulations) in the same order: maximal runs of
+        // units within one row block and, when kchunk > 0, within one k chunk. The
+        // first segment of a row block writes its workspace slot, later ones add to it.
+        uint64_t u = lo;
+        for (u32 seg = 0; u < hi; ++seg) {
+            const u32 rp = (u32) (u / a.nkb), kb = (u32) (u % a.nkb);
+            const u32 kend = a.kchunk ? min(a.nkb, (kb / a.kchunk + 1) * a.kchunk) : a.nkb;
+            const bool fresh = u == lo || kb == 0;
+            u = min(hi, (uint64_t) rp * a.nkb + kend);
+            // every lane waits; the warp goes on only if all of them saw the phase, so the
+            // .sync.aligned loads below always run converged
+            const bool ok = mbar_wait(accf, seg & 1u, a.err, kErrEpilogue);
+            if (!__all_sync(0xffffffffu, ok)) break;
+            tc_fence_after();
+            const u32 slot = blockIdx.x - __ldg(&a.rp_first[rp]);
+            float* P = a.partial + ((size_t) rp * a.max_slots + slot) * a.R * ROWS;
+            for (int h = 0; h < 2; ++h) {
+                const u32 row = h * BM + q * 32 + lane;
+                for (u32 c0 = 0; c0 < a.BN; c0 += 32) {
+                    uint32_t v[32];
+                    tmem_ld32(tmem + ((uint32_t) (q * 32) << 16) + h * 256 + c0, v);
+                    float* d = P + (size_t) c0 * ROWS + row;
+                    if (!fresh) {   // all loads first, then all stores: one round trip per 32 columns
+                        float prev[32];
 #pragma unroll
-                        for (int c = 0; c < 32; ++c)
-                            if (c0 + c < a.R) P[(size_t) (c0 + c) * ROWS + row] = __uint_as_float(v[c]);
+                        for (int c = 0; c < 32; ++c) prev[c] = c0 + c < a.R ? d[(size_t) c * ROWS] : 0.0f;
+#pragma unroll
+                        for (int c = 0; c < 32; ++c) v[c] = __float_as_uint(__uint_as_float(v[c]) + prev[c]);
                     }
+#pragma unroll
+                    for (int c = 0; c < 32; ++c)
+                        if (c0 + c < a.R) d[(size_t) c * ROWS] = __uint_as_float(v[c]);
                 }
-                tc_fence_before();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(acce);
             }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acce);
         }
     }
     tc_fence_before();
@@ -338,19 +352,37 @@ template <> __device__ __forceinline__ __nv_bfloat16 to16<__nv_bfloat16>(float f
 __device__ __forceinline__ float from16(__half h) { return __half2float(h); }
 __device__ __forceinline__ float from16(__nv_bfloat16 h) { return __bfloat162float(h); }
 
+// Exponent of the power-of-two scale of X: the largest emission maps below
+// 2^9, which leaves room for the bounced light to grow 100x and keeps small
+// values out of the FP16 subnormal range.
+__device__ __forceinline__ int x_scale_exp(const u32* emax_bits)
+{
+    const float emax = __uint_as_float(*emax_bits);
+    if (!(emax > 0.0f) || !(emax < 3.0e38f)) return 0;
+    int p;
+    frexpf(emax, &p);
+    return 9 - p;
+}
+
 // One 32 (patches) x 32 (right-hand sides) tile:
-//   B[j][r] = E[j][r] + sum over the row block's slots of the partials (slot order)
-//   X^T[r][j] = head (+ tail) of albedo_j(r mod 3) * B[j][r], zero for j >= n or r >= R
+//   B[j][r] = E[j][r] + 2^-(g_exp + x_exp) * sum over the row block's slots of
+//             the partials (slot order)
+//   X^T[r][j] = head (+ tail) of 2^x_exp * albedo_j(r mod 3) * B[j][r], zero for
+//             j >= n or r >= R
+// The G operand holds 2^g_exp G, the X operand 2^x_exp X (exact scalings).
 // B_out and xh may be null (not wanted); partial null means B = E.
 template <class T>
 __global__ void __launch_bounds__(256) k_combine(u32 n, u32 ld, u32 R, u32 Rpad, const float* __restrict__ partial,
                                                  u32 max_slots, const u32* __restrict__ rp_cnt,
                                                  const float* __restrict__ E, const float* __restrict__ albedo,
-                                                 float* __restrict__ B_out, T* __restrict__ xh, T* __restrict__ xl)
+                                                 float* __restrict__ B_out, T* __restrict__ xh, T* __restrict__ xl,
+                                                 int g_exp, const u32* __restrict__ emax_bits)
 {
     __shared__ float tile[32][33];
     const u32 j0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
     const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x_exp = x_scale_exp(emax_bits);
+    const float unscale = ldexpf(1.0f, -(g_exp + x_exp)), xscale = ldexpf(1.0f, x_exp);
     for (int k = ty; k < 32; k += 8) {   // tx along j
         const u32 r = r0 + k, j = j0 + tx;
         float v = 0.0f;
@@ -367,9 +399,9 @@ __global__ void __launch_bounds__(256) k_combine(u32 n, u32 ld, u32 R, u32 Rpad,
         float x = 0.0f;
         if (j < n && r < R) {
             const size_t o = (size_t) j * R + r;
-            const float b = E[o] + tile[tx][k];
+            const float b = E[o] + tile[tx][k] * unscale;
             if (B_out) B_out[o] = b;
-            x = albedo[3 * j + r % 3] * b;
+            x = albedo[3 * j + r % 3] * b * xscale;
         }
         tile[tx][k] = x;
     }
@@ -389,33 +421,40 @@ __global__ void __launch_bounds__(256) k_combine(u32 n, u32 ld, u32 R, u32 Rpad,
 // ----------------------------------------------------------------------------- FP32 SIMT gather
 
 // B_new = E + G X, G (n x n FP32), X (n x R FP32, row-major): 128 x 192 tile
-// per block, 16 x 16 threads with 8 x 12 outputs each, k step 8, the next
-// k tile prefetched into registers while the current one is consumed.
-constexpr int SBM = 128, SBN = 192, SBK = 8;
+// per block, 16 x 16 threads with 8 x 12 outputs each, k tiles of 16 in two
+// shared-memory buffers (one barrier per tile); the next tile's global loads
+// are in flight in registers while the current tile is consumed.
+constexpr int SBM = 128, SBN = 192, SBK = 16;
 __global__ void __launch_bounds__(256) k_sgemm_bounce(u32 n, u32 R, const float* __restrict__ G,
                                                       const float* __restrict__ X, const float* __restrict__ E,
                                                       float* __restrict__ Bnew)
 {
-    __shared__ __align__(16) float As[SBK][SBM + 4];
-    __shared__ __align__(16) float Bs[SBK][SBN];
+    __shared__ __align__(16) float As[2][SBK][SBM + 4];
+    __shared__ __align__(16) float Bs[2][SBK][SBN];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const u32 m0 = blockIdx.x * SBM, n0 = blockIdx.y * SBN;
-    // loader coordinates: A 128 rows x 8 k (row ar, k ak..ak+3); B 8 k x 192 (k bk, cols bc..bc+5)
-    const int ar = tid >> 1, ak = (tid & 1) * 4, bk = tid >> 5, bc = (tid & 31) * 6;
-    float pa[4], pb[6];
+    // loader coordinates: A 128 rows x 16 k (row ar, k ak..ak+7); B 16 k x 192 (k bk, cols bc..bc+11)
+    const int ar = tid >> 1, ak = (tid & 1) * 8, bk = tid >> 4, bc = (tid & 15) * 12;
+    float pa[8], pb[12];
     auto fetch = [&](u32 k0) {
         const u32 gi = m0 + ar;
 #pragma unroll
-        for (int t = 0; t < 4; ++t) {
+        for (int t = 0; t < 8; ++t) {
             const u32 gk = k0 + ak + t;
             pa[t] = (gi < n && gk < n) ? __ldg(&G[(size_t) gi * n + gk]) : 0.0f;
         }
         const u32 gk = k0 + bk;
 #pragma unroll
-        for (int t = 0; t < 6; ++t) {
+        for (int t = 0; t < 12; ++t) {
             const u32 gc = n0 + bc + t;
             pb[t] = (gk < n && gc < R) ? __ldg(&X[(size_t) gk * R + gc]) : 0.0f;
         }
+    };
+    auto stash = [&](int buf) {
+#pragma unroll
+        for (int t = 0; t < 8; ++t) As[buf][ak + t][ar] = pa[t];
+#pragma unroll
+        for (int t = 0; t < 12; ++t) Bs[buf][bk][bc + t] = pb[t];
     };
     float acc[8][12];
 #pragma unroll
@@ -423,20 +462,19 @@ __global__ void __launch_bounds__(256) k_sgemm_bounce(u32 n, u32 R, const float*
 #pragma unroll
         for (int j = 0; j < 12; ++j) acc[i][j] = 0.0f;
     fetch(0);
+    stash(0);
+    __syncthreads();
+    int cur = 0;
     for (u32 k0 = 0; k0 < n; k0 += SBK) {
-#pragma unroll
-        for (int t = 0; t < 4; ++t) As[ak + t][ar] = pa[t];
-#pragma unroll
-        for (int t = 0; t < 6; ++t) Bs[bk][bc + t] = pb[t];
-        __syncthreads();
-        if (k0 + SBK < n) fetch(k0 + SBK);
+        const bool more = k0 + SBK < n;
+        if (more) fetch(k0 + SBK);
 #pragma unroll
         for (int k = 0; k < SBK; ++k) {
-            const float4 a0 = *reinterpret_cast<const float4*>(&As[k][ty * 8]);
-            const float4 a1 = *reinterpret_cast<const float4*>(&As[k][ty * 8 + 4]);
-            const float4 b0 = *reinterpret_cast<const float4*>(&Bs[k][tx * 12]);
-            const float4 b1 = *reinterpret_cast<const float4*>(&Bs[k][tx * 12 + 4]);
-            const float4 b2 = *reinterpret_cast<const float4*>(&Bs[k][tx * 12 + 8]);
+            const float4 a0 = *reinterpret_cast<const float4*>(&As[cur][k][ty * 8]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&As[cur][k][ty * 8 + 4]);
+            const float4 b0 = *reinterpret_cast<const float4*>(&Bs[cur][k][tx * 12]);
+            const float4 b1 = *reinterpret_cast<const float4*>(&Bs[cur][k][tx * 12 + 4]);
+            const float4 b2 = *reinterpret_cast<const float4*>(&Bs[cur][k][tx * 12 + 8]);
             const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
             const float bv[12] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w, b2.x, b2.y, b2.z, b2.w};
 #pragma unroll
@@ -444,7 +482,9 @@ __global__ void __launch_bounds__(256) k_sgemm_bounce(u32 n, u32 R, const float*
 #pragma unroll
                 for (int j = 0; j < 12; ++j) acc[i][j] = __fmaf_rn(av[i], bv[j], acc[i][j]);
         }
+        if (more) stash(cur ^ 1);
         __syncthreads();
+        cur ^= 1;
     }
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
@@ -481,14 +521,25 @@ __global__ void k_scale_cols(u32 n, float* __restrict__ G, const float* __restri
     G[t] *= area[t % n];
 }
 
-// hi = 16-bit G (row stride ld, zero columns j >= n); lo = 16-bit (G - hi) when requested.
+// *out = max |x| as float bits (non-negative floats order like their bits); *out starts at 0.
+__global__ void k_absmax(const float* __restrict__ x, size_t count, u32* out)
+{
+    float m = 0.0f;
+    for (size_t t = blockIdx.x * (size_t) blockDim.x + threadIdx.x; t < count; t += (size_t) gridDim.x * blockDim.x)
+        m = fmaxf(m, fabsf(x[t]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+// hi = 16-bit 2^g_exp G (row stride ld, zero columns j >= n); lo = 16-bit residual when requested.
 template <class T>
-__global__ void k_g_to_16(u32 n, u32 ld, const float* __restrict__ G, T* __restrict__ hi, T* __restrict__ lo)
+__global__ void k_g_to_16(u32 n, u32 ld, const float* __restrict__ G, T* __restrict__ hi, T* __restrict__ lo,
+                          float gscale)
 {
     const size_t t = blockIdx.x * (size_t) blockDim.x + threadIdx.x;
     if (t >= (size_t) n * ld) return;
     const u32 i = (u32) (t / ld), j = (u32) (t % ld);
-    const float g = j < n ? G[(size_t) i * n + j] : 0.0f;
+    const float g = j < n ? G[(size_t) i * n + j] * gscale : 0.0f;
     const T h = to16<T>(g);
     hi[t] = h;
     if (lo) lo[t] = to16<T>(g - from16(h));
@@ -564,12 +615,14 @@ struct ltrg_Gather {
     DevBuf G32;                   // n x n FP32
     DevBuf G16, G16lo;            // n x ld 16-bit head and residual
     int g16_kind = -1;            // precision held in G16 (-1: none)
+    int g_exp = 0;                // G16 holds 2^g_exp G: max |G| maps below 2^14
     bool g16_has_lo = false;
     // stream-K schedule of the tcgen05 kernel (fixed by n and the SM count)
     u32 n_rp = 0, nkb = 0, n_cta = 0, max_slots = 0;
+    u32 kchunk = 0;               // k blocks per TMEM accumulation (0: whole range of a CTA)
     DevBuf rp_tab;                // rp_first[n_rp], rp_cnt[n_rp]
     // solve scratch
-    DevBuf partial, xh, xl, x32, btmp, err;
+    DevBuf partial, xh, xl, x32, btmp, err, emax;
     DevBuf h_alb, h_E, h_out;     // device copies for the host-buffer entry point
     uint64_t links = 0, vis_rays = 0, pairs = 0;
     double ms_build = 0;
@@ -581,7 +634,8 @@ struct ltrg_Gather {
         if (!st) return;
         cudaSetDevice(device);
         cudaStreamSynchronize(st);
-        DevBuf* all[] = {&G32, &G16, &G16lo, &rp_tab, &partial, &xh, &xl, &x32, &btmp, &err, &h_alb, &h_E, &h_out};
+        DevBuf* all[] = {&G32,  &G16, &G16lo, &rp_tab, &partial, &xh,    &xl,
+                         &x32,  &btmp, &err,  &emax,   &h_alb,   &h_E,   &h_out};
         for (DevBuf* b : all) b->release();
         cudaStreamDestroy(st);
     }
@@ -673,12 +727,13 @@ void ltrg_Gather::solve(const float* alb, const float* E, u32 R, int bounces, in
             if (need_lo) G16lo.ensure((size_t) n * ld * 2);
             const size_t tot = (size_t) n * ld;
             const unsigned grid = (unsigned) ((tot + 255) / 256);
+            const float gscale = ldexpf(1.0f, g_exp);
             if (precision == LTRG_F_FP16)
                 k_g_to_16<__half><<<grid, 256, 0, s>>>(n, ld, G32.as<float>(), G16.as<__half>(),
-                                                       need_lo ? G16lo.as<__half>() : nullptr);
+                                                       need_lo ? G16lo.as<__half>() : nullptr, gscale);
             else
                 k_g_to_16<__nv_bfloat16><<<grid, 256, 0, s>>>(n, ld, G32.as<float>(), G16.as<__nv_bfloat16>(),
-                                                              need_lo ? G16lo.as<__nv_bfloat16>() : nullptr);
+                                                              need_lo ? G16lo.as<__nv_bfloat16>() : nullptr, gscale);
             note_launch();
             GCK(cudaGetLastError());
             cudaEvent_t c1 = event();
@@ -713,10 +768,15 @@ void ltrg_Gather::solve(const float* alb, const float* E, u32 R, int bounces, in
         ua.stages = (u32) stages; ua.stage_bytes = stage_bytes; ua.mode = (u32) refine;
         ua.idesc = idesc_f16(precision == LTRG_F_BF16 ? 1u : 0u, BN);
         ua.max_slots = max_slots;
+        ua.kchunk = kchunk;
         ua.rp_first = rp_tab.as<u32>();
         ua.partial = partial.as<float>();
         ua.err = err.as<u32>();
         const u32* rp_cnt = rp_tab.as<u32>() + n_rp;
+        emax.ensure(4);
+        GCK(cudaMemsetAsync(emax.p, 0, 4, s));
+        k_absmax<<<std::max<u32>(1, std::min<u32>(1024, (u32) (((size_t) n * R + 255) / 256))), 256, 0, s>>>(
+            E, (size_t) n * R, emax.as<u32>()); note_launch();
         dim3 cb(32, 8), cg((ld + 31) / 32, (BN + 31) / 32);
         auto combine = [&](bool with_partial, bool last) {
             float* bo = last ? out : nullptr;
@@ -724,11 +784,12 @@ void ltrg_Gather::solve(const float* alb, const float* E, u32 R, int bounces, in
             if (precision == LTRG_F_FP16)
                 k_combine<__half><<<cg, cb, 0, s>>>(n, ld, R, BN, P, max_slots, rp_cnt, E, alb, bo,
                                                     last ? nullptr : xh.as<__half>(),
-                                                    (last || refine == LTRG_REFINE_NONE) ? nullptr : xl.as<__half>());
+                                                    (last || refine == LTRG_REFINE_NONE) ? nullptr : xl.as<__half>(),
+                                                    g_exp, emax.as<u32>());
             else
                 k_combine<__nv_bfloat16><<<cg, cb, 0, s>>>(
                     n, ld, R, BN, P, max_slots, rp_cnt, E, alb, bo, last ? nullptr : xh.as<__nv_bfloat16>(),
-                    (last || refine == LTRG_REFINE_NONE) ? nullptr : xl.as<__nv_bfloat16>());
+                    (last || refine == LTRG_REFINE_NONE) ? nullptr : xl.as<__nv_bfloat16>(), g_exp, emax.as<u32>());
             note_launch();
         };
         cudaEvent_t e0 = event();
@@ -857,7 +918,11 @@ LTRAPI ltrg_Gather* ltrg_GatherCreate(const float* tri_xyz, u32 n_tris, const fl
         k_scale_cols<<<(unsigned) ((nn2 + 255) / 256), 256, 0, st>>>(n, g->G32.as<float>(), da); note_launch();
         GCK(cudaGetLastError());
         GCK(cudaEventRecord(e1, st));
-        u32 herr = 0;
+        u32* dgmax = (u32*) up(nullptr, 0);
+        GCK(cudaMemsetAsync(dgmax, 0, 4, st));
+        k_absmax<<<1024, 256, 0, st>>>(g->G32.as<float>(), nn2, dgmax); note_launch();
+        u32 herr = 0, hgmax = 0;
+        GCK(cudaMemcpyAsync(&hgmax, dgmax, 4, cudaMemcpyDeviceToHost, st));
         GCK(cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, st));
         GCK(cudaStreamSynchronize(st));
         float ms = 0;
@@ -865,6 +930,13 @@ LTRAPI ltrg_Gather* ltrg_GatherCreate(const float* tri_xyz, u32 n_tris, const fl
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         if (herr) throw std::runtime_error("form-factor traversal error word " + std::to_string(herr));
+        float gmax;
+        memcpy(&gmax, &hgmax, 4);
+        if (gmax > 0.0f && gmax < 3.0e38f) {
+            int p;
+            frexpf(gmax, &p);
+            g->g_exp = 14 - p;
+        }
         g->ms_build = ms;
         g->links = ff.links;
         g->vis_rays = ff.vis_rays;
@@ -879,6 +951,14 @@ LTRAPI ltrg_Gather* ltrg_GatherCreate(const float* tri_xyz, u32 n_tris, const fl
 }
 
 LTRAPI void ltrg_GatherDestroy(ltrg_Gather* g) { delete g; }
+
+LTRAPI LTRBOOL ltrg_GatherSetChunk(ltrg_Gather* g, u32 k_blocks)
+{
+    if (!g) return 0;
+    std::lock_guard<std::mutex> lk(g->mu);
+    g->kchunk = k_blocks;
+    return 1;
+}
 
 LTRAPI u32 ltrg_GatherSize(ltrg_Gather* g) { return g ? g->n : 0; }
 

@@ -82,6 +82,7 @@ class GatherStats(C.Structure):
 EXT_API.update({
     "ltrg_GatherCreate": (C.c_void_p, [C.c_void_p, u32, C.c_void_p, C.c_void_p, C.c_void_p, u32, C.c_int, C.c_int]),
     "ltrg_GatherDestroy": (None, [C.c_void_p]),
+    "ltrg_GatherSetChunk": (C.c_int, [C.c_void_p, u32]),
     "ltrg_GatherSize": (u32, [C.c_void_p]),
     "ltrg_GatherGetG": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ltrg_GatherLastError": (C.c_char_p, [C.c_void_p]),

@@ -64,6 +64,11 @@ class Gather:
         msg = self.lib.ltrg_GatherLastError(self.h)
         raise RuntimeError(f"{what}: {msg.decode() if msg else 'unknown error'}")
 
+    def set_chunk(self, k_blocks: int):
+        """TMEM accumulation length in 64-wide k blocks (0: unlimited)."""
+        if not self.lib.ltrg_GatherSetChunk(self.h, int(k_blocks)):
+            raise RuntimeError("ltrg_GatherSetChunk failed")
+
     def G(self) -> np.ndarray:
         """G_ij = F_ij * area_j (FP32, n x n) as built on the device."""
         out = np.empty((self.n, self.n), np.float32)
