@@ -61,9 +61,9 @@ def _peaks_tensor():
         return 1900.0
 
 
-def _traffic_from_profile():
-    """dram bytes per launch of the direct-light kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_direct_mid.md")
+def _traffic_from_profile(name="k_direct_mid.md"):
+    """dram bytes per launch of a kernel from its committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", name)
     try:
         with open(path) as f:
             for line in f:
@@ -348,10 +348,16 @@ def main():
     ap.add_argument("--gather-bounces", type=int, default=4)
     ap.add_argument("--gather-steps", type=int, default=3)
     ap.add_argument("--no-gather", action="store_true")
+    ap.add_argument("--no-bake", action="store_true",
+                    help="gather only (profiling of the gather kernels on a smaller patch set)")
     args = ap.parse_args()
     world, rank, local, dist = _dist()
     if args.impl == "reference":
         return run_reference(args, world, rank, dist)
+    if args.no_bake:
+        if rank == 0:
+            print(json.dumps({"gather": run_gather(args, local)}), flush=True)
+        return 0
 
     rays, dev_ms, wall, stats, clocks, h2d, d2h, launches = run_ours(args, world, rank, local, dist)
     if dist is not None:
@@ -410,14 +416,21 @@ def main():
         gat = run_gather(args, 0)
         line["gather"] = gat
         peak_tf = _peaks_tensor()
-        m = gat["modes"]["fp16_rhs"]
-        line["s_per_bounce"] = {"gather_fp16_rhs": m["s_per_bounce"], "gather_fp32": gat["modes"]["fp32"]["s_per_bounce"],
+        gm = gat["modes"]
+        m, mf = gm["fp16"], gm["fp16_full"]
+        line["s_per_bounce"] = {"gather_fp16": m["s_per_bounce"], "gather_fp16_full": mf["s_per_bounce"],
+                                "gather_fp32": gm["fp32"]["s_per_bounce"],
+                                "gather_fp32_cublas_sgemm": gat["fp32_cublas_sgemm_s_per_bounce"],
                                 "bake_mid_fp32": line["s_per_bounce"]}
         line["gather_roofline"] = {
-            "kernel": "k_umma_gather (tcgen05, FP16 G, split right-hand side)", "bound": "hbm",
-            "achieved": m["f_gbs"], "peak": peak, "unit": "GB/s", "frac": m["f_gbs"] / peak,
-            "tensor_tflops": m["tflops"], "tensor_peak_tflops": peak_tf, "tensor_frac": m["tflops"] / peak_tf,
-            "traffic": None}
+            "kernel": "k_umma_gather (tcgen05, FP16 G, one product)", "bound": "hbm",
+            "achieved": m["f_gbs"], "peak": peak, "unit": "GB/s", "frac": m["f_gbs"] / peak, "peak_source": peak_kind,
+            "traffic": _traffic_from_profile("k_umma_gather_c5.md"),
+            "algorithmic_bytes_per_launch": m["bytes_per_bounce"]}
+        line["gather_roofline_tensor"] = {
+            "kernel": "k_umma_gather (tcgen05, FP16 G + residual, split right-hand side: 3 products)",
+            "bound": "tensor", "achieved": mf["tflops"], "peak": peak_tf, "unit": "TFLOP/s",
+            "frac": mf["tflops"] / peak_tf, "peak_source": "measured bf16 dense burst (MEASURED_PEAKS.json)"}
     if not args.no_cpu_baseline:
         from lighter_gb300 import scenes
         threads = os.cpu_count() or 1

@@ -751,11 +751,10 @@ void ltrg_Gather::solve(const float* alb, const float* E, u32 R, int bounces, in
         if (stages < 2) throw std::runtime_error("tensor-core gather: stage does not fit in shared memory");
         const size_t smem = (size_t) stages * stage_bytes + kSmemExtra;
         products = 1 + (refine >= LTRG_REFINE_RHS) + (refine == LTRG_REFINE_FULL);
+        // every element of X^T (padding included) is written by the first k_combine
         xh.ensure((size_t) BN * ld * 2);
         xl.ensure((size_t) BN * ld * 2);
         partial.ensure((size_t) n_rp * max_slots * R * ROWS * 4);
-        GCK(cudaMemsetAsync(xh.p, 0, (size_t) BN * ld * 2, s));
-        GCK(cudaMemsetAsync(xl.p, 0, (size_t) BN * ld * 2, s));
         const CUtensorMapDataType dt =
             precision == LTRG_F_FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
         const CUtensorMap mG = make_map(G16.p, dt, ld, n, ROWS);
