@@ -383,25 +383,38 @@ __global__ void __launch_bounds__(256) k_combine(u32 n, u32 ld, u32 R, u32 Rpad,
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int x_exp = x_scale_exp(emax_bits);
     const float unscale = ldexpf(1.0f, -(g_exp + x_exp)), xscale = ldexpf(1.0f, x_exp);
-    for (int k = ty; k < 32; k += 8) {   // tx along j
-        const u32 r = r0 + k, j = j0 + tx;
-        float v = 0.0f;
-        if (partial && j < n && r < R) {
-            const u32 rp = j / ROWS, cnt = rp_cnt[rp];
-            const float* P = partial + ((size_t) rp * max_slots * R + r) * ROWS + (j % ROWS);
-            for (u32 s = 0; s < cnt; ++s) v += P[(size_t) s * R * ROWS];
-        }
-        tile[k][tx] = v;
+    // the loads of the second phase (E, albedo) go out together with those of the first,
+    // so a block waits for about one memory round trip instead of three
+    float e[4], al[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {   // tx along r
+        const u32 j = j0 + ty + 8 * i, r = r0 + tx;
+        const bool in = j < n && r < R;
+        e[i] = in ? __ldg(&E[(size_t) j * R + r]) : 0.0f;
+        al[i] = in ? __ldg(&albedo[3 * j + r % 3]) : 0.0f;
     }
+    // the 32 patches of a tile lie in one 256-row block (j0 is a multiple of 32)
+    const u32 rp = j0 / ROWS, cnt = (partial && j0 < n) ? __ldg(&rp_cnt[rp]) : 0u;
+    float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (u32 s = 0; s < cnt; ++s) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {   // tx along j
+            const u32 r = r0 + ty + 8 * i, j = j0 + tx;
+            if (j < n && r < R) v[i] += __ldg(&partial[(((size_t) rp * max_slots + s) * R + r) * ROWS + (j % ROWS)]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) tile[ty + 8 * i][tx] = v[i];
     __syncthreads();
-    for (int k = ty; k < 32; k += 8) {   // tx along r
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {   // tx along r
+        const int k = ty + 8 * i;
         const u32 j = j0 + k, r = r0 + tx;
         float x = 0.0f;
         if (j < n && r < R) {
-            const size_t o = (size_t) j * R + r;
-            const float b = E[o] + tile[tx][k] * unscale;
-            if (B_out) B_out[o] = b;
-            x = albedo[3 * j + r % 3] * b * xscale;
+            const float b = e[i] + tile[tx][k] * unscale;
+            if (B_out) B_out[(size_t) j * R + r] = b;
+            x = al[i] * b * xscale;
         }
         tile[tx][k] = x;
     }
