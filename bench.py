@@ -38,6 +38,9 @@ sys.path.insert(0, ROOT)
 METRIC = "rays/s & s/radiosity bounce: batched FP16-F vs plain FP32 GPU @1e-3 rel err"
 WORKLOAD = ("mid: 200x200 m ground + 400 boxes + 50 icospheres (320 tris), ~21k tris, 4 x 1024^2 lightmaps, "
             "8 point + 2 spot lights, AO 32 rays r=2 m, radiosity 2 bounces over 16k patches, FP32")
+WORKLOAD_LARGE = ("large: fBm terrain 1024x512 quads (1.05M tris) in 16 tiles + 2000 80-tri rocks, ~1.2M tris, "
+                  "16 x 2048^2 lightmaps, 1 directional + 32 point lights, AO 64 rays r=2 m, radiosity 3 bounces "
+                  "over ~64k patches, FP32")
 CPU_SAMPLE = ("same mid scene (geometry, lights, AO) at 256^2 lightmaps = 1/16 of the texels, "
               "radiosity off (texel-level radiosity of the reference is not runnable at this size)")
 NODE_BYTES = 64
@@ -200,7 +203,10 @@ def run_ours(args, world, rank, local, dist):
     from lighter_gb300.ext import get_stats
 
     lib = library()
-    desc = scenes.mid(seed=1, lm=args.lm)
+    if args.scene == "large":
+        desc = scenes.large(seed=1, lm=args.lm)
+    else:
+        desc = scenes.mid(seed=1, lm=args.lm)
     gpu_opts = {"device": local, "radiosity_patches": args.patches, "radiosity_links": 1}
     # ingest once through the C API; every step is ltr_Start .. finished
     from lighter_gb300.scene import ingest
@@ -339,7 +345,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--lm", type=int, default=1024, help="lightmap side of the mid scene")
+    ap.add_argument("--scene", choices=["mid", "large"], default="mid",
+                    help="mid: the headline workload; large: 1.2M-triangle terrain, 16 x 2048^2 lightmaps")
+    ap.add_argument("--lm", type=int, default=None, help="lightmap side (default 1024 mid, 2048 large)")
     ap.add_argument("--patches", type=int, default=16384)
     ap.add_argument("--cpu-lm", type=int, default=256, help="lightmap side of the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -351,6 +359,10 @@ def main():
     ap.add_argument("--no-bake", action="store_true",
                     help="gather only (profiling of the gather kernels on a smaller patch set)")
     args = ap.parse_args()
+    if args.lm is None:
+        args.lm = 2048 if args.scene == "large" else 1024
+    if args.scene == "large" and args.patches == 16384:
+        args.patches = 65536
     world, rank, local, dist = _dist()
     if args.impl == "reference":
         return run_reference(args, world, rank, dist)
@@ -373,7 +385,7 @@ def main():
     peak, peak_kind = _peaks()
     direct_bytes = s0["node_visits"] * NODE_BYTES + s0["tri_tests"] * TRI_BYTES
     achieved = direct_bytes / (s0["ms_direct"] / 1000.0) / 1e9 if s0["ms_direct"] > 0 else 0.0
-    bounces = 2
+    bounces = 3 if args.scene == "large" else 2
     line = {
         "metric": METRIC,
         "value": rays_all / (dev_ms_max / 1000.0),
@@ -388,7 +400,7 @@ def main():
         "dtype": "f32",
         "data": "synthetic (seeded procedural scene, seed 1)",
         "config": {
-            "workload": WORKLOAD,
+            "workload": WORKLOAD if args.scene == "mid" else WORKLOAD_LARGE,
             "lightmap": args.lm,
             "radiosity_patches": args.patches,
             "radiosity_links": "visible pairs (patch mode)",
@@ -431,7 +443,11 @@ def main():
             "kernel": "k_umma_gather (tcgen05, FP16 G + residual, split right-hand side: 3 products)",
             "bound": "tensor", "achieved": mf["tflops"], "peak": peak_tf, "unit": "TFLOP/s",
             "frac": mf["tflops"] / peak_tf, "peak_source": "measured bf16 dense burst (MEASURED_PEAKS.json)"}
-    if not args.no_cpu_baseline:
+    if args.scene == "large" and not args.no_cpu_baseline:
+        line["cpu_baseline"] = None
+        line["cpu_baseline_note"] = ("not run for the 1.2M-triangle scene: the reference's per-instance BSP "
+                                     "(PickSplitPlane, O(points^2) per node) makes its sample stage impractical")
+    elif not args.no_cpu_baseline:
         from lighter_gb300 import scenes
         threads = os.cpu_count() or 1
         r, dt, cnt = _oracle_bake(scenes.mid(seed=1, lm=args.cpu_lm, bounces=0), threads)

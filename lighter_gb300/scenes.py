@@ -314,3 +314,129 @@ def mid(seed: int = 1, lm: int = 1024, n_boxes: int = 400, n_spheres: int = 50, 
     cfg = {"bounce_count": bounces, "ao_distance": 2.0 if ao_rays else 0.0, "ao_num_samples": max(ao_rays, 1)}
     return SceneDesc(f"mid{lm}", meshes, insts, lights, cfg, fixed_lm_size=(lm, lm),
                      sample_table=(albedo, None), seed=seed)
+
+
+def _value_noise(x, y, rng_table):
+    """Smooth value noise on the integer lattice (hashed through a 256-entry
+    permutation of seeded random values), bilinear with a quintic fade."""
+    perm, vals = rng_table
+    xi, yi = np.floor(x).astype(np.int64), np.floor(y).astype(np.int64)
+    fx, fy = x - xi, y - yi
+    fx = fx * fx * fx * (fx * (fx * 6 - 15) + 10)
+    fy = fy * fy * fy * (fy * (fy * 6 - 15) + 10)
+
+    def h(ix, iy):
+        return vals[perm[(perm[ix & 255] + iy) & 255]]
+
+    a, b = h(xi, yi), h(xi + 1, yi)
+    c, d = h(xi, yi + 1), h(xi + 1, yi + 1)
+    return (a * (1 - fx) + b * fx) * (1 - fy) + (c * (1 - fx) + d * fx) * fy
+
+
+def fbm_heights(rng, nx, ny, spacing, octaves=6, base_period=256.0, amplitude=60.0):
+    """(ny+1, nx+1) heights of a seeded fBm: octave k has period base/2^k and weight 0.5^k."""
+    table = (rng.permutation(256), rng.uniform(-1.0, 1.0, 256))
+    xs = np.arange(nx + 1) * spacing
+    ys = np.arange(ny + 1) * spacing
+    X, Y = np.meshgrid(xs, ys)
+    z = np.zeros_like(X)
+    for k in range(octaves):
+        f = (2.0 ** k) / base_period
+        z += (0.5 ** k) * _value_noise(X * f + 17.3 * k, Y * f - 9.1 * k, table)
+    return z * amplitude
+
+
+def large(seed: int = 1, lm: int = 2048, grid=(1024, 512), tiles=(4, 4), n_rocks: int = 2000, n_points: int = 32,
+          ao_rays: int = 64, bounces: int = 3, spacing: float = 2.0) -> SceneDesc:
+    """C3: seeded fBm heightfield terrain (6 octaves, grid[0] x grid[1] quads =
+    2 * grid[0] * grid[1] triangles; 1024 x 512 -> 1.05M) cut into tiles[0] x
+    tiles[1] instances, each with an lm^2 lightmap, plus `n_rocks` 80-triangle
+    icospheres (scale lognormal(0, 0.5)) scattered on it; every rock is packed
+    into a strip of its tile's lightmap. 1 directional light (128 samples) and
+    `n_points` point lights; AO `ao_rays` rays of radius 2 m; `bounces`
+    radiosity bounces."""
+    rng = np.random.default_rng(seed)
+    nx, ny = grid
+    tx, ty = tiles
+    Z = fbm_heights(rng, nx, ny, spacing)
+    W, D = nx * spacing, ny * spacing
+
+    def height_at(x, y):
+        i = np.clip((x / spacing).astype(int), 0, nx - 1)
+        j = np.clip((y / spacing).astype(int), 0, ny - 1)
+        return Z[j, i]
+
+    # rocks: positions, scales, unit icosphere (80 triangles)
+    unit = icosphere(1)
+    unit_n = np.stack([_face_normal(f) for f in unit])
+    chart_cache = {}
+    rx, ry = rng.uniform(0, W, n_rocks), rng.uniform(0, D, n_rocks)
+    rs = np.exp(rng.normal(0.0, 0.5, n_rocks))
+    rz = height_at(rx, ry) + 0.3 * rs
+    qx, qy = nx // tx, ny // ty
+    strip = 0.125                  # lightmap fraction (v) that holds the tile's rocks
+    margin = 2.0 / lm
+    meshes, insts = [], []
+    n_faces = 0
+    for t_y in range(ty):
+        for t_x in range(tx):
+            i0, j0 = t_x * qx, t_y * qy
+            ii, jj = np.meshgrid(np.arange(qx + 1), np.arange(qy + 1))
+            gx, gy = (i0 + ii) * spacing, (j0 + jj) * spacing
+            gz = Z[j0:j0 + qy + 1, i0:i0 + qx + 1]
+            P = np.stack([gx, gy, gz], -1).reshape(-1, 3)
+            # vertex normals from central differences of the heightfield
+            zc = Z[max(j0 - 1, 0):j0 + qy + 2, max(i0 - 1, 0):i0 + qx + 2]
+            dzdx = np.gradient(zc, spacing, axis=1)[(1 if j0 > 0 else 0):, (1 if i0 > 0 else 0):][:qy + 1, :qx + 1]
+            dzdy = np.gradient(zc, spacing, axis=0)[(1 if j0 > 0 else 0):, (1 if i0 > 0 else 0):][:qy + 1, :qx + 1]
+            N = np.stack([-dzdx, -dzdy, np.ones_like(dzdx)], -1).reshape(-1, 3)
+            N /= np.linalg.norm(N, axis=1, keepdims=True)
+            u = margin + ii / qx * (1 - 2 * margin)
+            v = margin + jj / qy * (1 - strip - 2 * margin)
+            T2 = np.stack([u, v], -1).reshape(-1, 2)
+            T1 = np.tile(np.array([[n_faces + 0.5, 0.0]]), (len(P), 1))
+            n_faces += 1
+            a = (jj[:-1, :-1] * (qx + 1) + ii[:-1, :-1]).ravel()
+            b, c, d = a + 1, a + qx + 2, a + qx + 1
+            I = np.stack([a, b, c, a, c, d], 1).ravel()
+            parts = [Part(P.astype(np.float32), N.astype(np.float32), T1.astype(np.float32), T2.astype(np.float32),
+                          I.astype(np.uint32), 1)]
+            # this tile's rocks, each a cell of the strip with per-face charts
+            sel = np.nonzero((rx >= i0 * spacing) & (rx < (i0 + qx) * spacing) &
+                             (ry >= j0 * spacing) & (ry < (j0 + qy) * spacing))[0]
+            if len(sel):
+                cols = max(1, int(math.ceil(math.sqrt(len(sel) / strip))))
+                rows = int(math.ceil(len(sel) / cols))
+                cw, ch = 1.0 / cols, strip / rows
+                cell_px = int(min(cw, ch) * lm)
+                # a rock is a scaled, translated unit icosphere: its charts and face normals are
+                # the unit sphere's, computed once per cell size
+                key = max(cell_px, 8)
+                if key not in chart_cache:
+                    chart_cache[key] = np.stack(pack_faces(list(unit), key, pad_texels=1.0))   # (80, 3, 2)
+                uv_unit = chart_cache[key]
+                k = np.arange(len(sel))
+                corner = np.stack([(k % cols) * cw, 1 - strip + (k // cols) * ch], 1)          # (m, 2)
+                sc = min(cw, ch)
+                RP = unit[None] * rs[sel][:, None, None, None] + np.stack([rx[sel], ry[sel], rz[sel]], 1)[:, None, None]
+                R2 = uv_unit[None] * sc + corner[:, None, None]
+                RN = np.broadcast_to(unit_n[None, :, None, :], RP.shape)
+                R1 = np.zeros(RP.shape[:3] + (2,))
+                R1[..., 0] = (n_faces + k + 0.5)[:, None, None]
+                n_faces += len(sel)
+                parts.append(Part(RP.reshape(-1, 3).astype(np.float32), RN.reshape(-1, 3).astype(np.float32),
+                                  R1.reshape(-1, 2).astype(np.float32), R2.reshape(-1, 2).astype(np.float32),
+                                  np.arange(RP.shape[0] * RP.shape[1] * 3, dtype=np.uint32), 1))
+            meshes.append(Mesh(f"tile{t_x}_{t_y}", parts))
+            insts.append(Instance(len(meshes) - 1, ident=f"tile{t_x}_{t_y}"))
+    albedo = rng.uniform(0.3, 0.8, (n_faces, 3)).astype(np.float32)
+    lights = [Light(LTR_LT_DIRECT, direction=(0.3, 0.2, 1.0), color=(1.0, 0.95, 0.85), range=400.0, power=1.0,
+                    light_radius=0.5, shadow_sample_count=128)]
+    for _ in range(n_points):
+        x, y = rng.uniform(0, W), rng.uniform(0, D)
+        lights.append(Light(LTR_LT_POINT, (x, y, float(height_at(np.array([x]), np.array([y]))[0]) + rng.uniform(5, 20)),
+                            color=tuple(rng.uniform(0.5, 1.0, 3)), range=float(rng.uniform(60, 120)), power=1.0,
+                            light_radius=0.3, shadow_sample_count=16))
+    cfg = {"bounce_count": bounces, "ao_distance": 2.0 if ao_rays else 0.0, "ao_num_samples": max(ao_rays, 1)}
+    return SceneDesc(f"large{lm}", meshes, insts, lights, cfg, fixed_lm_size=(lm, lm),
+                     sample_table=(albedo, None), seed=seed)

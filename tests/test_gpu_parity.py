@@ -92,6 +92,18 @@ def test_spot_lights_and_many_instances(gpu, oracle):
     compare(rg, ro, "mid128")
 
 
+def test_large_terrain_scaled_down(gpu, oracle):
+    # the C3 generator (fBm terrain tiles + rocks packed into each tile's lightmap) at a small size;
+    # the oracle's result does not depend on its thread count
+    import os
+    d = scenes.large(2, lm=64, grid=(64, 32), n_rocks=40, n_points=4, ao_rays=4, bounces=0)
+    st = {}
+    rg = bake(gpu, d, stats=st)
+    ro = bake(oracle, d, threads=os.cpu_count() or 1)
+    compare(rg, ro, "large64")
+    assert st["triangles"] == d.triangle_count() and len(rg.lightmaps) == 16
+
+
 def test_normal_map_and_blur(gpu, oracle):
     d = scenes.cornell(5, lm=32, bounces=0, ao=True)
     d.config.update(generate_normalmap_data=1, blur_size=1.5)
