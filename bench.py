@@ -332,6 +332,61 @@ def run_gather(args, local):
     return out
 
 
+BATCH_WORKLOAD = ("batch: {n} seeded scenes, triangles lognormal (median 2k, 200-20k), lightmap side log-uniform "
+                  "64-512, 1-8 point lights with 16-64 samples, AO 16 rays r=2 m, no radiosity")
+
+
+def run_batch(args, local):
+    """The batch workload baked one scene after another (ltr_Start, ltrg_Wait) and
+    as one batch (ltrg_StartBatch): wall time of all scenes through the C API."""
+    import ctypes as C
+
+    from lighter_gb300 import library, scenes
+    from lighter_gb300.ext import get_stats
+    from lighter_gb300.scene import ingest
+
+    lib = library()
+    descs = [scenes.batch_scene(s) for s in range(1, args.batch_scenes + 1)]
+    handles = [ingest(lib, d, gpu_options={"device": local}) for d in descs]
+    arr = (C.c_void_p * len(handles))(*[h for h, _ in handles])
+    try:
+        def sequential():
+            t0 = time.perf_counter()
+            for h, _ in handles:
+                lib.ltr_Start(h)
+                if not lib.ltrg_Wait(h):
+                    raise RuntimeError("bake failed: " + (lib.ltrg_LastError(h) or b"").decode())
+            return time.perf_counter() - t0
+
+        def batched():
+            t0 = time.perf_counter()
+            if not lib.ltrg_StartBatch(arr, len(handles)):
+                raise RuntimeError("ltrg_StartBatch rejected the batch")
+            for h, _ in handles:
+                if not lib.ltrg_Wait(h):
+                    raise RuntimeError("batch bake failed: " + (lib.ltrg_LastError(h) or b"").decode())
+            return time.perf_counter() - t0
+
+        sequential()
+        t_seq = min(sequential() for _ in range(max(1, args.batch_steps)))
+        batched()
+        t_bat = min(batched() for _ in range(max(1, args.batch_steps)))
+        st = [get_stats(lib, h) for h, _ in handles]
+    finally:
+        for h, _ in handles:
+            lib.ltr_DestroyScene(h)
+    rays = sum(x["shadow_evals"] + x["ao_rays"] for x in st)
+    texels = sum(x["samples"] for x in st)
+    return {
+        "workload": BATCH_WORKLOAD.format(n=len(descs)),
+        "sequential_s": t_seq, "batch_s": t_bat, "speedup": t_seq / t_bat,
+        "rays": rays, "rays_per_s_sequential": rays / t_seq, "rays_per_s_batch": rays / t_bat,
+        "texels": texels, "texels_per_s_batch": texels / t_bat,
+        "triangles": sum(x["triangles"] for x in st),
+        "timing": "host wall clock of all scenes through the C API, best of %d after one warm-up" % max(1, args.batch_steps),
+    }
+
+
 def _bake_once(lib, scene):
     lib.ltr_Start(scene)
     if not lib.ltrg_Wait(scene):
@@ -356,6 +411,9 @@ def main():
     ap.add_argument("--gather-bounces", type=int, default=4)
     ap.add_argument("--gather-steps", type=int, default=3)
     ap.add_argument("--no-gather", action="store_true")
+    ap.add_argument("--batch-scenes", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=2)
+    ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-bake", action="store_true",
                     help="gather only (profiling of the gather kernels on a smaller patch set)")
     args = ap.parse_args()
@@ -424,6 +482,8 @@ def main():
                                                     "ms_rad_bounce", "ms_ao", "ms_finalize", "ms_download",
                                                     "ms_device", "ms_total")},
     }
+    if not args.no_batch:
+        line["batch"] = run_batch(args, 0)
     if not args.no_gather:
         gat = run_gather(args, 0)
         line["gather"] = gat

@@ -189,6 +189,16 @@ LTRAPI LTRBOOL ltrg_GatherSolveDevice(ltrg_Gather* g, const float* albedo_rgb, c
                                       int bounces, int precision, int refine, float* out, ltrg_GatherStats* stats,
                                       void* stream);
 
+/* Bakes `count` scenes as one batch. Each scene bakes as if ltr_Start had
+ * been called on it (same outputs, status and ltrg_Wait), but the direct-light
+ * shadow traces and the AO rays of all scenes run in one persistent kernel
+ * launch each, so many small scenes fill the GPU together. The scenes' AO
+ * rand() draws are taken in array order, as bakes run one after another in
+ * that order would take them. All scenes must use the same device and none
+ * may be running; returns 0 (starting nothing) otherwise. No counterpart in
+ * the reference, which bakes one scene per ltr_Start. */
+LTRAPI LTRBOOL ltrg_StartBatch(ltr_Scene** scenes, u32 count);
+
 /* Read-only introspection of a finished bake (requires keep_samples = 1).
  * Instance 0 is the probe-sample container of ltr_SampleAdd, as in the
  * reference (lighter_int.hpp:975-980). */

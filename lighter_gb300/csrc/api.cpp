@@ -100,9 +100,39 @@ LTRAPI void ltr_DestroyScene(ltr_Scene* scene)
     delete scene;
 }
 
+static void start_bake(ltr_Scene* scene);
+
 LTRAPI void ltr_Start(ltr_Scene* scene)
 {
     if (scene->worker.joinable()) scene->worker.join();
+    scene->batch.reset();
+    scene->batch_index = -1;
+    start_bake(scene);
+}
+
+// Starts the bakes of `count` scenes as one batch (include/lighter_gb300.h).
+LTRAPI LTRBOOL ltrg_StartBatch(ltr_Scene** scenes, u32 count)
+{
+    if (!scenes || count == 0) return 0;
+    for (u32 k = 0; k < count; ++k) {
+        if (!scenes[k] || scenes[k]->running.load()) return 0;
+        if (scenes[k]->opt.device != scenes[0]->opt.device) return 0;
+        for (u32 j = 0; j < k; ++j)
+            if (scenes[j] == scenes[k]) return 0;
+    }
+    for (u32 k = 0; k < count; ++k)
+        if (scenes[k]->worker.joinable()) scenes[k]->worker.join();
+    std::shared_ptr<BatchCtx> ctx = make_batch((int) count, scenes[0]->opt.device);
+    for (u32 k = 0; k < count; ++k) {
+        scenes[k]->batch = ctx;
+        scenes[k]->batch_index = (int) k;
+    }
+    for (u32 k = 0; k < count; ++k) start_bake(scenes[k]);
+    return 1;
+}
+
+static void start_bake(ltr_Scene* scene)
+{
     scene->clear_outputs();
     scene->error.clear();
     scene->abort_flag = false;
@@ -123,6 +153,7 @@ LTRAPI void ltr_Start(ltr_Scene* scene)
             scene->completion = 1;
             scene->stage = scene->abort_flag ? "aborted" : "error: bake failed (see ltrg_LastError)";
         }
+        scene->batch.reset();
         scene->running = false;
     });
 }

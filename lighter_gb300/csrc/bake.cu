@@ -20,6 +20,9 @@
 #include <cmath>
 #include <unordered_map>
 #include <chrono>
+#include <condition_variable>
+#include <memory>
+#include <mutex>
 #include <thread>
 #include <cstring>
 #include <stdexcept>
@@ -420,34 +423,39 @@ __global__ void k_direct_compact(unsigned long long total, const u32* __restrict
 // Pass 2: persistent threads over the compacted pairs; a thread takes the
 // next pair as soon as its sphere trace ends, so trace lengths that differ by
 // orders of magnitude do not idle the other lanes of its warp.
+// One traced (light, sample) pair w = light * n_samples + sample.
+__device__ __forceinline__ void direct_pair(const DirectArgs& a, u32 w, u32& nq, u32& nv, u32& nt)
+{
+    int l = (int) (w / a.n_samples);
+    u32 s = w % a.n_samples;
+    const DLight L = a.lights[l];
+    LightTerms t;
+    light_terms(a, L, s, t);
+    float vis = inv_shadow(a.bvh, t.from, t.to, L.radius, a.err, nq, nv, nt);
+    V3 Lcol = mk(L.color[0], L.color[1], L.color[2]);
+    float kv, fac;
+    if (L.type == 2) {
+        kv = t.f_dist * t.f_ndotl * t.f_dir * vis;
+        fac = t.f_dist * t.f_dir * vis * t.f_ndotl * brightness(Lcol);
+    } else if (L.type == 1) {
+        kv = t.f_dist * t.f_ndotl * vis;
+        fac = t.f_dist * vis * t.f_ndotl * brightness(Lcol);
+    } else {
+        kv = t.f_ndotl * vis;
+        fac = vis * t.f_ndotl * brightness(Lcol);
+    }
+    a.kval[w] = kv;
+    if (a.ndir && a.sinst[s] != 0 && fac > 0) a.ndir[w] = st4(t.dir * fac, 1.0f);
+}
+
 __global__ void k_direct_trace(DirectArgs a, const u32* __restrict__ items, const u32* __restrict__ n_items_dev,
                                u32* __restrict__ next)
 {
     unsigned long long c_traced = 0, c_nq = 0, c_nv = 0, c_nt = 0;
     const u32 n_items = *n_items_dev;
     for (u32 i = atomicAdd(next, 1u); i < n_items; i = atomicAdd(next, 1u)) {
-        u32 w = items[i];
-        int l = (int) (w / a.n_samples);
-        u32 s = w % a.n_samples;
-        const DLight L = a.lights[l];
-        LightTerms t;
-        light_terms(a, L, s, t);
         u32 nq = 0, nv = 0, nt = 0;
-        float vis = inv_shadow(a.bvh, t.from, t.to, L.radius, a.err, nq, nv, nt);
-        V3 Lcol = mk(L.color[0], L.color[1], L.color[2]);
-        float kv, fac;
-        if (L.type == 2) {
-            kv = t.f_dist * t.f_ndotl * t.f_dir * vis;
-            fac = t.f_dist * t.f_dir * vis * t.f_ndotl * brightness(Lcol);
-        } else if (L.type == 1) {
-            kv = t.f_dist * t.f_ndotl * vis;
-            fac = t.f_dist * vis * t.f_ndotl * brightness(Lcol);
-        } else {
-            kv = t.f_ndotl * vis;
-            fac = vis * t.f_ndotl * brightness(Lcol);
-        }
-        a.kval[w] = kv;
-        if (a.ndir && a.sinst[s] != 0 && fac > 0) a.ndir[w] = st4(t.dir * fac, 1.0f);
+        direct_pair(a, items[i], nq, nv, nt);
         c_traced += 1;
         c_nq += nq;
         c_nv += nv;
@@ -668,6 +676,19 @@ __device__ __forceinline__ unsigned long long warp_fetch(unsigned long long* ctr
 
 constexpr unsigned kAoChunk = 4;
 
+// Ray r of sample s (i = s * ns + r): closest-hit fraction along the AO segment.
+__device__ __forceinline__ void ao_ray(const AoArgs& a, float* __restrict__ hits, unsigned long long i)
+{
+    u32 s = (u32) (i / a.ns);
+    int r = (int) (i % a.ns);
+    V3 SP = ld3(a.spos[s]), SN = ld3(a.snrm[s]);
+    V3 ro = SP + SN * (kSmall * 2);
+    V3 rd = spiral_dir(SN, a.randoff[s], r, a.ns) * a.dist;
+    V3 B = ro + rd;
+    V3 dn = normalized(B - ro);
+    hits[i] = bvh_closest(a.bvh, ro + dn * kSmall, B - dn * kSmall, a.err, nullptr);
+}
+
 __global__ void k_ao_rays(AoArgs a, float* __restrict__ hits, unsigned long long n_rays, unsigned long long* next)
 {
     unsigned long long c_rays = 0;
@@ -676,18 +697,120 @@ __global__ void k_ao_rays(AoArgs a, float* __restrict__ hits, unsigned long long
         if (i0 >= n_rays) break;
         unsigned long long i1 = i0 + kAoChunk < n_rays ? i0 + kAoChunk : n_rays;
         for (unsigned long long i = i0; i < i1; ++i) {
-        u32 s = (u32) (i / a.ns);
-        int r = (int) (i % a.ns);
-        V3 SP = ld3(a.spos[s]), SN = ld3(a.snrm[s]);
-        V3 ro = SP + SN * (kSmall * 2);
-        V3 rd = spiral_dir(SN, a.randoff[s], r, a.ns) * a.dist;
-        V3 B = ro + rd;
-        V3 dn = normalized(B - ro);
-        hits[i] = bvh_closest(a.bvh, ro + dn * kSmall, B - dn * kSmall, a.err, nullptr);
-        ++c_rays;
+            ao_ray(a, hits, i);
+            ++c_rays;
         }
     }
     if (a.counters) warp_add(&a.counters->ao_rays, c_rays);
+}
+
+// ----------------------------------------------------------------------------- batches of scenes
+// A batch of scenes (ltrg_StartBatch) traces the direct-light pairs and the AO
+// rays of all its scenes in one persistent launch each: job k holds scene k's
+// arguments and work list, off[] the exclusive prefix sums of the jobs' item
+// counts; item g belongs to the job k with off[k] <= g < off[k + 1].
+
+struct DirectJob {
+    DirectArgs args;
+    const u32* items;   // traced pairs (light * n_samples + sample)
+    const u32* count;   // device: number of items (null: none)
+};
+
+struct AoJob {
+    AoArgs args;
+    float* hits;        // n_samples * ns hit fractions
+};
+
+__device__ __forceinline__ int find_job(const unsigned long long* __restrict__ off, int n, unsigned long long g)
+{
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (off[mid] <= g) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_direct_batch_offsets(const DirectJob* __restrict__ jobs, int n, unsigned long long* __restrict__ off)
+{
+    if (blockIdx.x || threadIdx.x) return;
+    unsigned long long acc = 0;
+    for (int k = 0; k < n; ++k) {
+        off[k] = acc;
+        acc += jobs[k].count ? *jobs[k].count : 0u;
+    }
+    off[n] = acc;
+}
+
+__device__ __forceinline__ void flush_direct(Counters* c, unsigned long long& tr, unsigned long long& nq,
+                                             unsigned long long& nv, unsigned long long& nt)
+{
+    if (c && tr) {
+        atomicAdd(&c->shadow_evals, tr);
+        atomicAdd(&c->distance_queries, nq);
+        atomicAdd(&c->node_visits, nv);
+        atomicAdd(&c->tri_tests, nt);
+    }
+    tr = nq = nv = nt = 0;
+}
+
+__global__ void k_direct_trace_batch(const DirectJob* __restrict__ jobs, int n, const unsigned long long* __restrict__ off,
+                                     unsigned long long* __restrict__ next)
+{
+    const unsigned long long total = off[n];
+    unsigned long long c_traced = 0, c_nq = 0, c_nv = 0, c_nt = 0;
+    int cur = -1;
+    DirectArgs a;
+    const u32* items = nullptr;
+    unsigned long long base = 0;
+    for (unsigned long long g = atomicAdd(next, 1ull); g < total; g = atomicAdd(next, 1ull)) {
+        const int k = find_job(off, n, g);
+        if (k != cur) {
+            if (cur >= 0) flush_direct(a.counters, c_traced, c_nq, c_nv, c_nt);
+            cur = k;
+            a = jobs[k].args;
+            items = jobs[k].items;
+            base = off[k];
+        }
+        u32 nq = 0, nv = 0, nt = 0;
+        direct_pair(a, items[g - base], nq, nv, nt);
+        c_traced += 1;
+        c_nq += nq;
+        c_nv += nv;
+        c_nt += nt;
+    }
+    if (cur >= 0) flush_direct(a.counters, c_traced, c_nq, c_nv, c_nt);
+}
+
+__global__ void k_ao_rays_batch(const AoJob* __restrict__ jobs, int n, const unsigned long long* __restrict__ off,
+                                unsigned long long* __restrict__ next)
+{
+    const unsigned long long total = off[n];
+    unsigned long long c_rays = 0;
+    int cur = -1;
+    AoArgs a;
+    float* hits = nullptr;
+    unsigned long long base = 0;
+    for (;;) {
+        unsigned long long i0 = warp_fetch(next, kAoChunk);
+        if (i0 >= total) break;
+        unsigned long long i1 = i0 + kAoChunk < total ? i0 + kAoChunk : total;
+        for (unsigned long long g = i0; g < i1; ++g) {
+            const int k = find_job(off, n, g);
+            if (k != cur) {
+                if (cur >= 0 && a.counters && c_rays) atomicAdd(&a.counters->ao_rays, c_rays);
+                c_rays = 0;
+                cur = k;
+                a = jobs[k].args;
+                hits = jobs[k].hits;
+                base = off[k];
+            }
+            ao_ray(a, hits, g - base);
+            ++c_rays;
+        }
+    }
+    if (cur >= 0 && a.counters && c_rays) atomicAdd(&a.counters->ao_rays, c_rays);
 }
 
 // Pass 2: per sample, the hit fractions summed in ray order like the
@@ -1118,6 +1241,265 @@ void build_refs_host(const std::vector<float>& xyz, std::vector<u32>& ref_tri, s
     build_refs(xyz, ref_tri, ref_box, cmin, cmax);
 }
 
+// ----------------------------------------------------------------------------- batches of scenes (host)
+//
+// The scenes of one ltrg_StartBatch run their bakes on their own host threads
+// and streams as usual. At the direct-light and the AO stage every scene
+// joins a rendezvous with its job; the last one to arrive (or to leave, when
+// a scene ends early) launches one trace kernel for all jobs on the batch's
+// stream, after events that mark each scene's inputs ready, and every scene's
+// stream waits on the launch's completion event. The per-sample rand() draws
+// of AO take turns in scene order, so a batch gives every scene the random
+// offsets it would get from bakes run one after another in that order.
+struct BatchCtx {
+    BatchCtx(int n_, int device_)
+        : n(n_), device(device_), rand_done(n_, 0), member(n_, 0), started(n_, 0), cv_turn(n_), cv_start(n_)
+    {
+        for (Phase& p : phase) p.expected = n_;
+        slots = std::max(2, std::min(16, (int) std::thread::hardware_concurrency()));
+        trace = getenv("LTRG_TRACE") != nullptr;
+        t0 = std::chrono::steady_clock::now();
+    }
+    ~BatchCtx()
+    {
+        for (Phase& p : phase) {
+            for (cudaEvent_t e : p.ready) cudaEventDestroy(e);
+            if (p.done) cudaEventDestroy(p.done);
+        }
+        if (bst) {
+            cudaStreamSynchronize(bst);
+            cudaStreamDestroy(bst);
+        }
+    }
+
+    struct Phase {
+        int expected = 0, arrived = 0;
+        bool launched = false;
+        std::string error;
+        std::vector<DirectJob> djobs;
+        std::vector<AoJob> ajobs;
+        std::vector<unsigned long long> rays;   // AO rays per job
+        std::vector<cudaEvent_t> ready;
+        cudaEvent_t done = nullptr;
+    };
+
+    const int n, device;
+    std::mutex mu;
+    std::vector<char> rand_done;   // per scene: its AO draws are over (or it draws none)
+    int rand_turn = 0;
+    std::vector<int> member;       // per scene: phases joined (bit p) or left
+    std::vector<char> started;     // per scene: took its first slot (or left before)
+    int next_start = 0;
+    // Each kind of wait has its own condition variable, and the per-scene turns
+    // one per scene, so a step of the ordered chains wakes one thread, not all.
+    std::vector<std::condition_variable> cv_turn;    // scene's turn to draw
+    std::vector<std::condition_variable> cv_start;   // scene's turn to start
+    std::condition_variable cv_slot;                 // a slot for a scene back from a wait
+    std::condition_variable cv_phase[2];             // the phase was launched
+    int slots = 16;                                  // scenes allowed to work at a time
+    int returners = 0;                               // scenes waiting in cv_slot
+    Phase phase[2];                                  // 0: direct light, 1: AO
+    cudaStream_t bst = nullptr;
+    bool trace = false;
+    std::chrono::steady_clock::time_point t0;
+    static constexpr auto kWait = std::chrono::seconds(900);
+
+    void note(const char* what, int p, int k)
+    {
+        if (trace)
+            fprintf(stderr, "[ltrg batch] %9.3f ms  phase %d %s %d\n",
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(), p, what, k);
+    }
+
+    // --- slots: at most `slots` scenes do host work (and issue CUDA calls) at a
+    // time; a scene gives its slot back while it waits at a rendezvous or for its
+    // turn to draw. Scenes take their first slot in batch order, so the chain of
+    // ordered AO draws can begin with scene 0 at once. Called with `mu` held:
+    void grant()
+    {
+        if (slots <= 0) return;
+        if (returners > 0) cv_slot.notify_one();
+        else if (next_start < n) cv_start[next_start].notify_one();
+    }
+    void advance_start()
+    {
+        while (next_start < n && started[next_start]) ++next_start;
+        grant();
+    }
+    void take_slot(std::unique_lock<std::mutex>& lk)
+    {
+        ++returners;
+        bool ok = cv_slot.wait_for(lk, kWait, [&] { return slots > 0; });
+        --returners;
+        if (!ok) throw std::runtime_error("batch: timed out waiting for a slot");
+        --slots;
+        grant();
+    }
+
+    void acquire_start(int idx)
+    {
+        std::unique_lock<std::mutex> lk(mu);
+        if (!cv_start[idx].wait_for(lk, kWait, [&] { return slots > 0 && next_start == idx && returners == 0; }))
+            throw std::runtime_error("batch: timed out waiting for a slot");
+        --slots;
+        started[idx] = 1;
+        advance_start();
+    }
+    void acquire()
+    {
+        std::unique_lock<std::mutex> lk(mu);
+        take_slot(lk);
+    }
+    void release()
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        ++slots;
+        grant();
+    }
+
+    // --- AO draw turns, in scene order
+    void advance_turn()
+    {
+        while (rand_turn < n && rand_done[rand_turn]) ++rand_turn;
+        if (rand_turn < n) cv_turn[rand_turn].notify_one();
+    }
+    void rand_begin(int idx)
+    {
+        std::unique_lock<std::mutex> lk(mu);
+        if (!cv_turn[idx].wait_for(lk, kWait, [&] { return rand_turn >= idx; }))
+            throw std::runtime_error("batch: timed out waiting for the random draws of earlier scenes");
+    }
+    void rand_end(int idx)
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (idx % 32 == 0 || idx == n - 1) note("draws done, scene", 9, idx);
+        rand_done[idx] = 1;
+        advance_turn();
+    }
+
+    // --- rendezvous. Joins phase p with scene idx's job; returns the event its
+    // stream waits on (the scene holds a slot again on return).
+    cudaEvent_t join(int p, int idx, cudaStream_t st, const DirectJob* dj, const AoJob* aj, unsigned long long rays)
+    {
+        cudaEvent_t ready;
+        CK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+        CK(cudaEventRecord(ready, st));
+        std::unique_lock<std::mutex> lk(mu);
+        Phase& ph = phase[p];
+        ph.ready.push_back(ready);
+        if (dj) ph.djobs.push_back(*dj);
+        if (aj) {
+            ph.ajobs.push_back(*aj);
+            ph.rays.push_back(rays);
+        }
+        ph.arrived++;
+        member[idx] |= 1 << p;
+        if (ph.arrived == 1 || ph.arrived == ph.expected) note("arrival", p, ph.arrived);
+        if (ph.arrived == ph.expected) {
+            launch(p);
+            if (trace && ph.done) {   // timeline only: wait for the kernel without holding the lock
+                lk.unlock();
+                cudaEventSynchronize(ph.done);
+                lk.lock();
+                note("kernel done", p, ph.arrived);
+            }
+        }
+        ++slots;   // the slot goes to scenes that still have to arrive
+        grant();
+        if (!cv_phase[p].wait_for(lk, kWait, [&] { return ph.launched; }))
+            throw std::runtime_error("batch: timed out waiting for the other scenes of the batch");
+        take_slot(lk);
+        if (!ph.error.empty()) throw std::runtime_error("batch launch failed: " + ph.error);
+        return ph.done;
+    }
+
+    // Scene idx has no work for phase p (it will not join it).
+    void skip(int p, int idx)
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (member[idx] & (1 << p)) return;
+        member[idx] |= 1 << p;
+        Phase& ph = phase[p];
+        ph.expected--;
+        if (!ph.launched && ph.arrived > 0 && ph.arrived == ph.expected) launch(p);
+    }
+
+    // Scene idx will join no further phase (its bake ended or failed).
+    void leave(int idx)
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        for (int p = 0; p < 2; ++p) {
+            if (member[idx] & (1 << p)) continue;
+            member[idx] |= 1 << p;
+            Phase& ph = phase[p];
+            ph.expected--;
+            if (!ph.launched && ph.arrived > 0 && ph.arrived == ph.expected) launch(p);
+        }
+        if (!rand_done[idx]) {
+            rand_done[idx] = 1;
+            advance_turn();
+        }
+        if (!started[idx]) {
+            started[idx] = 1;
+            advance_start();
+        }
+    }
+
+  private:
+    // Called with `mu` held, once per phase, when every remaining scene has joined.
+    void launch(int p)
+    {
+        Phase& ph = phase[p];
+        try {
+            CK(cudaSetDevice(device));
+            if (!bst) CK(cudaStreamCreateWithFlags(&bst, cudaStreamNonBlocking));
+            for (cudaEvent_t e : ph.ready) CK(cudaStreamWaitEvent(bst, e, 0));
+            int sms = 0;
+            CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+            const int nj = p == 0 ? (int) ph.djobs.size() : (int) ph.ajobs.size();
+            if (nj > 0) {
+                unsigned long long* d_off = nullptr;
+                unsigned long long* d_next = nullptr;
+                void* d_jobs = nullptr;
+                const size_t jb = p == 0 ? nj * sizeof(DirectJob) : nj * sizeof(AoJob);
+                CK(cudaMallocAsync(&d_jobs, jb, bst));
+                CK(cudaMallocAsync((void**) &d_off, (nj + 1) * sizeof(unsigned long long), bst));
+                CK(cudaMallocAsync((void**) &d_next, sizeof(unsigned long long), bst));
+                CK(cudaMemsetAsync(d_next, 0, sizeof(unsigned long long), bst));
+                if (p == 0) {
+                    CK(cudaMemcpyAsync(d_jobs, ph.djobs.data(), jb, cudaMemcpyHostToDevice, bst));
+                    k_direct_batch_offsets<<<1, 32, 0, bst>>>((const DirectJob*) d_jobs, nj, d_off); note_launch();
+                    k_direct_trace_batch<<<(unsigned) sms * 8, 128, 0, bst>>>((const DirectJob*) d_jobs, nj, d_off, d_next);
+                    note_launch();
+                } else {
+                    std::vector<unsigned long long> off(nj + 1, 0);
+                    for (int k = 0; k < nj; ++k) off[k + 1] = off[k] + ph.rays[k];
+                    CK(cudaMemcpyAsync(d_jobs, ph.ajobs.data(), jb, cudaMemcpyHostToDevice, bst));
+                    CK(cudaMemcpyAsync(d_off, off.data(), off.size() * sizeof(unsigned long long),
+                                       cudaMemcpyHostToDevice, bst));
+                    // the pageable copies above are staged before they return, so `off` may go
+                    k_ao_rays_batch<<<(unsigned) sms * 16, 128, 0, bst>>>((const AoJob*) d_jobs, nj, d_off, d_next);
+                    note_launch();
+                }
+                CK(cudaGetLastError());
+                cudaFreeAsync(d_jobs, bst);
+                cudaFreeAsync(d_off, bst);
+                cudaFreeAsync(d_next, bst);
+            }
+            CK(cudaEventCreateWithFlags(&ph.done, cudaEventDisableTiming));
+            CK(cudaEventRecord(ph.done, bst));
+            note("launched, jobs", p, nj);
+        } catch (const std::exception& e) {
+            ph.error = e.what();
+        }
+        ph.launched = true;
+        cv_phase[p].notify_all();
+    }
+};
+
+std::shared_ptr<BatchCtx> make_batch(int n, int device) { return std::make_shared<BatchCtx>(n, device); }
+void batch_leave(BatchCtx* b, int idx) { b->leave(idx); }
+
 // ----------------------------------------------------------------------------- the bake
 
 void run_bake(ltr_Scene* S)
@@ -1127,10 +1509,22 @@ void run_bake(ltr_Scene* S)
     host_counters() = HostCounters();
     S->rad_links = 0;
 
+    // member of a batch (ltrg_StartBatch): leaves it however the bake ends
+    BatchCtx* batch = S->batch.get();
+    const int bidx = S->batch_index;
+    struct BatchLeave {
+        BatchCtx* b; int i; bool slot = false;
+        ~BatchLeave() { if (b) { b->leave(i); if (slot) b->release(); } }
+    } batch_leave_end{batch, bidx};
+
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw std::runtime_error("no CUDA device available");
     if (S->opt.device >= ndev) throw std::runtime_error("ltrg_Options.device out of range");
     CK(cudaSetDevice(S->opt.device));
+    if (batch) {
+        batch->acquire_start(bidx);
+        batch_leave_end.slot = true;
+    }
 
     Arena A;
     CK(cudaStreamCreateWithFlags(&A.st, cudaStreamNonBlocking));
@@ -1199,7 +1593,7 @@ void run_bake(ltr_Scene* S)
     {
         std::vector<std::thread> pool;
         std::atomic<int> next(1);
-        int nth = std::max(1, std::min(8, (int) std::thread::hardware_concurrency()));
+        int nth = std::max(1, std::min({8, (int) std::thread::hardware_concurrency(), n_inst - 1}));
         for (int t = 0; t < nth; ++t)
             pool.emplace_back([&]() {
                 for (int i = next++; i < n_inst; i = next++)
@@ -1454,12 +1848,21 @@ void run_bake(ltr_Scene* S)
     std::vector<float> ao_randoff;
     std::thread ao_thread;
     const bool do_ao = cfg.ao_distance && n_samples && cfg.ao_num_samples > 0;
+    if (batch && !do_ao) batch->rand_end(bidx);   // draws nothing: the next scene's turn
     if (do_ao && (gpu_sample_fn || !cfg.bounce_count))
-        ao_thread = std::thread([&ao_randoff, n_samples]() {
+        ao_thread = std::thread([&ao_randoff, n_samples, batch, bidx]() {
+            if (batch) batch->rand_begin(bidx);
             ao_randoff.resize(n_samples);
             for (u32 s = 0; s < n_samples; ++s) ao_randoff[s] = randf_host();   // instance order, sample order
+            if (batch) batch->rand_end(bidx);
         });
     struct JoinGuard { std::thread& t; ~JoinGuard() { if (t.joinable()) t.join(); } } ao_guard{ao_thread};
+    // leaving the batch's rendezvous before the join above waits on a draw turn
+    // keeps a failed scene from holding the others
+    struct BatchLeaveEarly {
+        BatchCtx* b; int i;
+        ~BatchLeaveEarly() { if (b) b->leave(i); }
+    } batch_leave_early{batch, bidx};
 
     float4* d_spos = A.alloc<float4>(n_samples);
     float4* d_snrm = A.alloc<float4>(n_samples);
@@ -1552,9 +1955,16 @@ void run_bake(ltr_Scene* S)
         u32* d_next = A.zeros<u32>(1);
         int dev_sms = 0;
         CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, S->opt.device));
-        unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * 8, (items + 127) / 128);
-        k_direct_trace<<<grid, 128, 0, st>>>(da, d_items, d_dscan + items, d_next); note_launch();
-        CK(cudaGetLastError());
+        if (batch) {   // one trace launch for the whole batch
+            DirectJob job{da, d_items, d_dscan + items};
+            CK(cudaStreamWaitEvent(st, batch->join(0, bidx, st, &job, nullptr, 0), 0));
+        } else {
+            unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * 8, (items + 127) / 128);
+            k_direct_trace<<<grid, 128, 0, st>>>(da, d_items, d_dscan + items, d_next); note_launch();
+            CK(cudaGetLastError());
+        }
+    } else if (batch) {
+        batch->skip(0, bidx);
     }
     if (n_samples) {
         k_accumulate<<<(n_samples + kThreads - 1) / kThreads, kThreads, 0, st>>>(
@@ -1651,8 +2061,17 @@ void run_bake(ltr_Scene* S)
         // AO draws its per-sample random offsets after the last sample_fn call,
         // as the reference's AO stage comes after radiosity
         if (do_ao && !ao_thread.joinable()) {
+            // in a batch no slot is held while waiting for the turn (and drawing)
+            if (batch) {
+                batch->release();
+                batch->rand_begin(bidx);
+            }
             ao_randoff.resize(n_samples);
             for (u32 s = 0; s < n_samples; ++s) ao_randoff[s] = randf_host();
+            if (batch) {
+                batch->rand_end(bidx);
+                batch->acquire();
+            }
         }
         CK(cudaMemcpyAsync(d_diff, hdiff.data(), n_samples * sizeof(float4), cudaMemcpyHostToDevice, st2)); note_h2d(n_samples * sizeof(float4));
         CK(cudaMemcpyAsync(d_emis, hemis.data(), n_samples * sizeof(float4), cudaMemcpyHostToDevice, st2)); note_h2d(n_samples * sizeof(float4));
@@ -1756,7 +2175,11 @@ void run_bake(ltr_Scene* S)
         S->stage = "committing radiosity";
         e_rad_links = e_rad_bounce = clock.mark();
     }
-    if (ao_thread.joinable()) ao_thread.join();
+    if (ao_thread.joinable()) {   // the draws may wait for earlier scenes of a batch: no slot held meanwhile
+        if (batch) batch->release();
+        ao_thread.join();
+        if (batch) batch->acquire();
+    }
     check_abort(S);
 
     // ---- ambient occlusion (Job_AORender)
@@ -1785,12 +2208,20 @@ void run_bake(ltr_Scene* S)
             unsigned long long* d_next = A.zeros<unsigned long long>(1);
             int dev_sms = 0;
             CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, S->opt.device));
-            unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * 16, (n_rays + 127) / 128);
-            k_ao_rays<<<grid, 128, 0, st>>>(aa, d_hits, n_rays, d_next); note_launch();
-            CK(cudaGetLastError());
+            if (batch) {   // one trace launch for the whole batch
+                AoJob job{aa, d_hits};
+                CK(cudaStreamWaitEvent(st, batch->join(1, bidx, st, nullptr, &job, n_rays), 0));
+            } else {
+                unsigned grid =
+                    (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * 16, (n_rays + 127) / 128);
+                k_ao_rays<<<grid, 128, 0, st>>>(aa, d_hits, n_rays, d_next); note_launch();
+                CK(cudaGetLastError());
+            }
             k_ao<<<blocks_for(n_samples), kThreads, 0, st>>>(aa, d_hits); note_launch();
             CK(cudaGetLastError());
         }
+    } else if (batch) {
+        batch->skip(1, bidx);
     }
     TRACE("ao issued");
     cudaEvent_t e_ao1 = clock.mark();

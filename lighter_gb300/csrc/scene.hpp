@@ -5,6 +5,7 @@
 #pragma once
 
 #include <atomic>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -54,6 +55,11 @@ struct ltr_Mesh {
     std::vector<lg::HostPart> parts;
 };
 
+namespace lg {
+struct BatchCtx;   // bake.cu: the rendezvous of the scenes of one ltrg_StartBatch
+std::shared_ptr<BatchCtx> make_batch(int n, int device);
+}  // namespace lg
+
 struct ltr_Scene {
     ltr_Config cfg;
     ltrg_Options opt;
@@ -73,6 +79,8 @@ struct ltr_Scene {
     std::atomic<bool> abort_flag{false};
     std::atomic<bool> running{false};
     std::thread worker;
+    std::shared_ptr<lg::BatchCtx> batch;   // set for the bake started by ltrg_StartBatch
+    int batch_index = -1;
 
     ltr_Scene();
     ~ltr_Scene();

@@ -40,6 +40,7 @@ EXT_API = {
     "ltrg_GetStats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "ltrg_LastError": (C.c_char_p, [C.c_void_p]),
     "ltrg_Wait": (C.c_int, [C.c_void_p]),
+    "ltrg_StartBatch": (C.c_int, [C.POINTER(C.c_void_p), u32]),
 }
 
 

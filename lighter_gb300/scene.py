@@ -277,40 +277,81 @@ def bake(lib, desc: SceneDesc, threads: int = 1, debug: bool = True, poll_s: flo
                 from .ext import get_stats
                 stats.update(get_stats(lib, scene))
 
-        info = abi.WorkOutputInfo()
-        lib.ltr_GetWorkOutputInfo(scene, C.byref(info))
-        lms = []
-        for k in range(info.lightmap_count):
-            wo = abi.WorkOutput()
-            if not lib.ltr_GetWorkOutput(scene, k, C.byref(wo)):
-                raise RuntimeError("ltr_GetWorkOutput failed")
-            n = wo.width * wo.height
-            rgb = np.ctypeslib.as_array(wo.lightmap_rgb, shape=(n * 3,)).copy().reshape(wo.height, wo.width, 3)
-            nrm = None
-            if wo.normals_xyzf:
-                nrm = np.ctypeslib.as_array(wo.normals_xyzf, shape=(n * 4,)).copy().reshape(wo.height, wo.width, 4)
-            mid = C.string_at(wo.mesh_ident, wo.mesh_ident_size).decode() if wo.mesh_ident else ""
-            iid = C.string_at(wo.inst_ident, wo.inst_ident_size).decode() if wo.inst_ident else ""
-            lms.append((wo.uid, mid, iid, rgb, nrm))
-        colors = np.zeros((info.sample_count, 3), np.float32)
-        for k in range(info.sample_count):
-            colors[k] = info.samples[k].out_color[:]
-
-        dbg = []
-        if debug and hasattr(lib, "ltrdbg_InstanceCount"):
-            for i in range(lib.ltrdbg_InstanceCount(scene)):
-                n = lib.ltrdbg_SampleCount(scene, i)
-                d = {
-                    "pos": np.zeros((n, 3), np.float32),
-                    "nrm": np.zeros((n, 3), np.float32),
-                    "loc": np.zeros((n,), np.uint32),
-                    "radinfo": np.zeros((n, 4), np.float32),
-                    "color": np.zeros((n, 3), np.float32),
-                }
-                if n:
-                    lib.ltrdbg_GetSamples(scene, i, d["pos"].ctypes.data, d["nrm"].ctypes.data,
-                                          d["loc"].ctypes.data, d["radinfo"].ctypes.data, d["color"].ctypes.data)
-                dbg.append(d)
-        return BakeResult(lms, colors, stages, wall, dbg, final)
+        return _collect(lib, scene, debug, stages, wall, final)
     finally:
         lib.ltr_DestroyScene(scene)
+
+
+def _collect(lib, scene, debug, stages, wall, final) -> "BakeResult":
+    info = abi.WorkOutputInfo()
+    lib.ltr_GetWorkOutputInfo(scene, C.byref(info))
+    lms = []
+    for k in range(info.lightmap_count):
+        wo = abi.WorkOutput()
+        if not lib.ltr_GetWorkOutput(scene, k, C.byref(wo)):
+            raise RuntimeError("ltr_GetWorkOutput failed")
+        n = wo.width * wo.height
+        rgb = np.ctypeslib.as_array(wo.lightmap_rgb, shape=(n * 3,)).copy().reshape(wo.height, wo.width, 3)
+        nrm = None
+        if wo.normals_xyzf:
+            nrm = np.ctypeslib.as_array(wo.normals_xyzf, shape=(n * 4,)).copy().reshape(wo.height, wo.width, 4)
+        mid = C.string_at(wo.mesh_ident, wo.mesh_ident_size).decode() if wo.mesh_ident else ""
+        iid = C.string_at(wo.inst_ident, wo.inst_ident_size).decode() if wo.inst_ident else ""
+        lms.append((wo.uid, mid, iid, rgb, nrm))
+    colors = np.zeros((info.sample_count, 3), np.float32)
+    for k in range(info.sample_count):
+        colors[k] = info.samples[k].out_color[:]
+
+    dbg = []
+    if debug and hasattr(lib, "ltrdbg_InstanceCount"):
+        for i in range(lib.ltrdbg_InstanceCount(scene)):
+            n = lib.ltrdbg_SampleCount(scene, i)
+            d = {
+                "pos": np.zeros((n, 3), np.float32),
+                "nrm": np.zeros((n, 3), np.float32),
+                "loc": np.zeros((n,), np.uint32),
+                "radinfo": np.zeros((n, 4), np.float32),
+                "color": np.zeros((n, 3), np.float32),
+            }
+            if n:
+                lib.ltrdbg_GetSamples(scene, i, d["pos"].ctypes.data, d["nrm"].ctypes.data,
+                                      d["loc"].ctypes.data, d["radinfo"].ctypes.data, d["color"].ctypes.data)
+            dbg.append(d)
+    return BakeResult(lms, colors, stages, wall, dbg, final)
+
+
+def bake_batch(lib, descs, debug: bool = False, gpu_options: Optional[dict] = None, stats: Optional[list] = None,
+               abort: Optional[list] = None):
+    """Ingest every scene of `descs` in order, start them as one batch
+    (ltrg_StartBatch) and collect their outputs like bake(). Scenes whose
+    index is in `abort` get ltr_Abort right after the start; their result is
+    None. `stats` (a list) receives one ltrg_GetStats dict per scene."""
+    handles = [ingest(lib, d, 1, gpu_options, debug) for d in descs]
+    arr = (C.c_void_p * len(handles))(*[h for h, _ in handles])
+    try:
+        t0 = time.perf_counter()
+        if not lib.ltrg_StartBatch(arr, len(handles)):
+            raise RuntimeError("ltrg_StartBatch rejected the batch")
+        for k in abort or []:
+            lib.ltr_Abort(handles[k][0])
+        ok = [bool(lib.ltrg_Wait(h)) for h, _ in handles]
+        wall = time.perf_counter() - t0
+        out = []
+        for k, ((h, _), good) in enumerate(zip(handles, ok)):
+            st = abi.WorkStatus()
+            lib.ltr_GetStatus(h, C.byref(st))
+            final = st.stage.decode() if st.stage else ""
+            if not good:
+                if abort and k in abort:
+                    out.append(None)
+                    continue
+                msg = lib.ltrg_LastError(h)
+                raise RuntimeError(f"batch scene {k} ended with '{final}': {msg.decode() if msg else ''}")
+            if stats is not None:
+                from .ext import get_stats
+                stats.append(get_stats(lib, h))
+            out.append(_collect(lib, h, debug, [final], wall, final))
+        return out, wall
+    finally:
+        for h, _ in handles:
+            lib.ltr_DestroyScene(h)

@@ -103,6 +103,61 @@ def pack_faces(faces, lm_size: int, pad_texels: float = 2.0):
     return out
 
 
+def pack_faces_fast(faces, lm_size: int, pad_texels: float = 2.0):
+    """Vectorised pack_faces for faces of equal vertex count (same layout and
+    charts, evaluated with array operations; used by the generators of the
+    large and batch workloads)."""
+    F = np.asarray(faces, np.float64)                   # (k, m, 3)
+    k = len(F)
+    g = max(1, int(math.ceil(math.sqrt(k))))
+    cell = 1.0 / g
+    pad = min(pad_texels, 0.25 * cell * lm_size) / lm_size
+    inner = cell - 2 * pad
+    if inner <= 0:
+        raise ValueError(f"{k} faces do not fit a {lm_size}^2 lightmap")
+    n = np.cross(F[:, 1] - F[:, 0], F[:, 2] - F[:, 0])
+    ln = np.linalg.norm(n, axis=1, keepdims=True)
+    n = np.where(ln > 0, n / np.where(ln > 0, ln, 1), np.array([0, 0, 1.0]))
+    a = F[:, 1] - F[:, 0]
+    a = a / np.linalg.norm(a, axis=1, keepdims=True)
+    b = np.cross(n, a)
+    d = F - F[:, :1]
+    uv = np.stack([np.einsum("kmc,kc->km", d, a), np.einsum("kmc,kc->km", d, b)], -1)
+    uv -= uv.min(1, keepdims=True)
+    ext = np.maximum(uv.max((1, 2)), 1e-9)[:, None, None]
+    uv = uv / ext * inner
+    idx = np.arange(k)
+    uv += np.stack([(idx % g) * cell + pad, (idx // g) * cell + pad], 1)[:, None, :]
+    return uv, n
+
+
+def faces_to_part_fast(faces, lm_size, face_id0=0, shadow=1, pad_texels=2.0):
+    """faces_to_part for triangles and quads through pack_faces_fast; faces are
+    grouped by vertex count, each group packed into its own half of the map
+    when both kinds are present."""
+    tris = [f for f in faces if len(f) == 3]
+    quads = [f for f in faces if len(f) == 4]
+    groups = [(g_, m) for g_, m in ((tris, 3), (quads, 4)) if g_]
+    P, N, T1, T2, I = [], [], [], [], []
+    base, fid = 0, face_id0
+    for gi, (grp, m) in enumerate(groups):
+        uv, n = pack_faces_fast(grp, lm_size, pad_texels)
+        if len(groups) == 2:             # left or right half
+            uv = uv * np.array([0.5, 1.0]) + np.array([0.5 * gi, 0.0])
+        k = len(grp)
+        P.append(np.asarray(grp, np.float64).reshape(-1, 3))
+        N.append(np.repeat(n, m, 0))
+        T1.append(np.stack([np.repeat(fid + np.arange(k) + 0.5, m), np.zeros(k * m)], 1))
+        T2.append(uv.reshape(-1, 2))
+        fan = np.array([[0, j, j + 1] for j in range(1, m - 1)]).ravel()
+        I.append((base + np.arange(k)[:, None] * m + fan[None, :]).ravel())
+        base += k * m
+        fid += k
+    return Part(np.concatenate(P).astype(np.float32), np.concatenate(N).astype(np.float32),
+                np.concatenate(T1).astype(np.float32), np.concatenate(T2).astype(np.float32),
+                np.concatenate(I).astype(np.uint32), shadow)
+
+
 def faces_to_part(faces, lm_size, face_id0=0, shadow=1, pad_texels=2.0):
     """Flat-shaded part: each face has its own vertices, normal and chart; uv1.u
     carries the global face id (face_id0 + k) for table-driven albedo."""
@@ -439,4 +494,48 @@ def large(seed: int = 1, lm: int = 2048, grid=(1024, 512), tiles=(4, 4), n_rocks
                             light_radius=0.3, shadow_sample_count=16))
     cfg = {"bounce_count": bounces, "ao_distance": 2.0 if ao_rays else 0.0, "ao_num_samples": max(ao_rays, 1)}
     return SceneDesc(f"large{lm}", meshes, insts, lights, cfg, fixed_lm_size=(lm, lm),
+                     sample_table=(albedo, None), seed=seed)
+
+
+def batch_scene(seed: int) -> SceneDesc:
+    """One scene of the C4 batch: a ground quad with boxes and 80-triangle
+    icospheres up to a triangle count drawn lognormal (median 2k, clipped to
+    200..20k); one instance per object group; a square lightmap whose side is
+    log-uniform in [64, 512]; 1-8 point lights with 16-64 samples; AO 16 rays;
+    no radiosity."""
+    rng = np.random.default_rng(seed)
+    target = int(np.clip(np.exp(rng.normal(math.log(2000.0), 0.8)), 200, 20000))
+    lm = int(round(math.exp(rng.uniform(math.log(64), math.log(512)))))
+    H = 30.0
+    ground = [np.array([[-H, -H, 0], [H, -H, 0], [H, H, 0], [-H, H, 0]], float)]
+    boxes, spheres = [], []
+    unit = icosphere(1)
+    n_tris = 2
+    while n_tris < target:
+        if rng.uniform() < 0.5:
+            sx, sy, sz = rng.uniform(0.5, 5.0, 3)
+            cx, cy = rng.uniform(-H + 3, H - 3, 2)
+            boxes += box_faces(sx, sy, sz, rng.uniform(0, 2 * math.pi), cx, cy, 0.0)
+            n_tris += 12
+        else:
+            r = rng.uniform(0.5, 2.5)
+            c = np.array([*rng.uniform(-H + 3, H - 3, 2), r])
+            spheres += [tri * r + c for tri in unit]
+            n_tris += 80
+    groups = [("ground", ground), ("boxes", boxes), ("spheres", spheres)]
+    meshes, insts, fid = [], [], 0
+    for name, faces in groups:
+        if not faces:
+            continue
+        meshes.append(Mesh(name, [faces_to_part_fast(faces, lm, fid, pad_texels=1.0)]))
+        fid += len(faces)
+        insts.append(Instance(len(meshes) - 1, ident=name))
+    albedo = rng.uniform(0.3, 0.8, (fid, 3)).astype(np.float32)
+    lights = []
+    for _ in range(int(rng.integers(1, 9))):
+        lights.append(Light(LTR_LT_POINT, (*rng.uniform(-H, H, 2), rng.uniform(3, 10)),
+                            color=tuple(rng.uniform(0.5, 1.0, 3)), range=float(rng.uniform(15, 40)), power=1.0,
+                            light_radius=0.2, shadow_sample_count=int(rng.integers(16, 65))))
+    cfg = {"bounce_count": 0, "ao_distance": 2.0, "ao_num_samples": 16}
+    return SceneDesc(f"batch{seed}", meshes, insts, lights, cfg, fixed_lm_size=(lm, lm),
                      sample_table=(albedo, None), seed=seed)
