@@ -211,7 +211,11 @@ def run_ours(args, world, rank, local, dist):
     # ingest once through the C API; every step is ltr_Start .. finished
     from lighter_gb300.scene import ingest
     scene, keep = ingest(lib, desc, gpu_options=gpu_opts)
+    tuning = None
     try:
+        if not args.no_autotune:   # launch shapes of the trace kernels, tuned on this scene
+            from lighter_gb300.ext import autotune
+            tuning = autotune(lib, scene)
         for _ in range(args.warmup):
             _bake_once(lib, scene)
         _barrier(dist)
@@ -231,7 +235,7 @@ def run_ours(args, world, rank, local, dist):
     rays = sum(s["shadow_evals"] + s["ao_rays"] + s["rad_vis_rays"] for s in stats)
     dev_ms = sum(s["ms_device"] for s in stats)
     launches = sum(s["kernel_launches"] for s in stats)
-    return rays, dev_ms, wall, stats, clocks, stats[-1]["bytes_h2d"], stats[-1]["bytes_d2h"], launches
+    return rays, dev_ms, wall, stats, clocks, stats[-1]["bytes_h2d"], stats[-1]["bytes_d2h"], launches, tuning
 
 
 GATHER_WORKLOAD = ("multi-RHS radiosity: seeded room with furniture, {n} patches, {t} triangles, "
@@ -414,6 +418,7 @@ def main():
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-bake", action="store_true",
                     help="gather only (profiling of the gather kernels on a smaller patch set)")
     args = ap.parse_args()
@@ -429,7 +434,7 @@ def main():
             print(json.dumps({"gather": run_gather(args, local)}), flush=True)
         return 0
 
-    rays, dev_ms, wall, stats, clocks, h2d, d2h, launches = run_ours(args, world, rank, local, dist)
+    rays, dev_ms, wall, stats, clocks, h2d, d2h, launches, tuning = run_ours(args, world, rank, local, dist)
     if dist is not None:
         import torch.distributed as td
         rays_all, = _allreduce(dist, [float(rays)], td.ReduceOp.SUM)
@@ -465,6 +470,7 @@ def main():
             "l2": "inputs larger than L2: per-bake sample buffers of %.0f MB, scene re-uploaded every step"
                   % (s0["samples"] * 84 / 1e6),
             "parallelism": "replicas" if world > 1 else "single GPU",
+            "trace_launch_shapes": tuning or "defaults (autotuner off)",
         },
         "e2e": {"value": rays_all / wall_max, "unit": "rays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},

@@ -199,6 +199,26 @@ LTRAPI LTRBOOL ltrg_GatherSolveDevice(ltrg_Gather* g, const float* albedo_rgb, c
  * the reference, which bakes one scene per ltr_Start. */
 LTRAPI LTRBOOL ltrg_StartBatch(ltr_Scene** scenes, u32 count);
 
+/* Launch shapes of the persistent trace kernels, per CUDA device. Results do
+ * not depend on them (every pair and ray is traced by the same function
+ * whatever thread takes it); only the time does. */
+typedef struct ltrg_Tuning {
+    u32 direct_block;         /* threads per block of the shadow-trace kernel, default 128 */
+    u32 direct_blocks_per_sm; /* persistent blocks per SM, default 8 */
+    u32 ao_block;             /* threads per block of the AO-ray kernel, default 128 */
+    u32 ao_blocks_per_sm;     /* default 16 */
+    u32 reserved[8];
+} ltrg_Tuning;
+LTRAPI LTRBOOL ltrg_GetTuning(int device, ltrg_Tuning* out);
+/* Values outside 32..512 threads (multiples of 32) or 1..64 blocks per SM are rejected. */
+LTRAPI LTRBOOL ltrg_SetTuning(int device, const ltrg_Tuning* t);
+/* Autotuner: bakes `scene` (not running; its device) repeatedly, coordinate
+ * descent over the candidate shapes of each kernel, each timed by that
+ * kernel's stage time (the best of two bakes), and keeps the fastest as the
+ * device's tuning. `out` receives it (may be NULL); the scene keeps the outputs
+ * of its last bake. Returns 0 if a bake fails. */
+LTRAPI LTRBOOL ltrg_Autotune(ltr_Scene* scene, ltrg_Tuning* out);
+
 /* Read-only introspection of a finished bake (requires keep_samples = 1).
  * Instance 0 is the probe-sample container of ltr_SampleAdd, as in the
  * reference (lighter_int.hpp:975-980). */

@@ -5,9 +5,12 @@
 // ltr_GetStatus polls a bake running on a host thread of its own.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <mutex>
 #include <stdexcept>
+#include <vector>
 
 #include "scene.hpp"
 
@@ -38,6 +41,39 @@ ltr_Scene::~ltr_Scene()
     if (pinned) cudaFreeHost(pinned);
     for (HostInst* mi : insts) delete mi;
     for (ltr_Mesh* m : meshes) delete m;
+}
+
+// ---- launch shapes of the trace kernels, per device
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_tuning_mu;
+ltrg_Tuning g_tuning[kMaxDevices];
+bool g_tuning_set[kMaxDevices] = {};
+
+ltrg_Tuning default_tuning()
+{
+    ltrg_Tuning t;
+    memset(&t, 0, sizeof(t));
+    t.direct_block = 128;
+    t.direct_blocks_per_sm = 8;
+    t.ao_block = 128;
+    t.ao_blocks_per_sm = 16;
+    return t;
+}
+
+bool tuning_valid(const ltrg_Tuning& t)
+{
+    auto block_ok = [](u32 b) { return b >= 32 && b <= 512 && b % 32 == 0; };
+    auto bps_ok = [](u32 k) { return k >= 1 && k <= 64; };
+    return block_ok(t.direct_block) && block_ok(t.ao_block) && bps_ok(t.direct_blocks_per_sm) && bps_ok(t.ao_blocks_per_sm);
+}
+}  // namespace
+
+ltrg_Tuning lg::get_tuning(int device)
+{
+    std::lock_guard<std::mutex> lk(g_tuning_mu);
+    if (device < 0 || device >= kMaxDevices || !g_tuning_set[device]) return default_tuning();
+    return g_tuning[device];
 }
 
 static u32 next_pow2(u32 x)
@@ -295,6 +331,81 @@ LTRAPI const char* ltrg_LastError(ltr_Scene* scene)
 {
     if (scene->running.load()) return nullptr;
     return scene->error.empty() ? nullptr : scene->error.c_str();
+}
+
+LTRAPI LTRBOOL ltrg_GetTuning(int device, ltrg_Tuning* out)
+{
+    if (!out || device < 0 || device >= kMaxDevices) return 0;
+    *out = get_tuning(device);
+    return 1;
+}
+
+LTRAPI LTRBOOL ltrg_SetTuning(int device, const ltrg_Tuning* t)
+{
+    if (!t || device < 0 || device >= kMaxDevices || !tuning_valid(*t)) return 0;
+    std::lock_guard<std::mutex> lk(g_tuning_mu);
+    g_tuning[device] = *t;
+    g_tuning_set[device] = true;
+    return 1;
+}
+
+// Coordinate descent: each launch parameter in turn takes the candidate whose
+// bakes (best of two) give its kernel's stage the shortest device time.
+LTRAPI LTRBOOL ltrg_Autotune(ltr_Scene* scene, ltrg_Tuning* out)
+{
+    if (!scene || scene->running.load()) return 0;
+    const int dev = scene->opt.device;
+    if (dev < 0 || dev >= kMaxDevices) return 0;
+    ltrg_Tuning best = get_tuning(dev);
+    auto bake_once = [&](const ltrg_Tuning& t, double& ms_direct, double& ms_ao) {
+        ltrg_SetTuning(dev, &t);
+        ltr_Start(scene);
+        if (!ltrg_Wait(scene)) return false;
+        ms_direct = scene->stats.ms_direct;
+        ms_ao = scene->stats.ms_ao;
+        return true;
+    };
+    auto measure = [&](const ltrg_Tuning& t, double& ms_direct, double& ms_ao) {
+        double d0, a0, d1, a1;
+        if (!bake_once(t, d0, a0) || !bake_once(t, d1, a1)) return false;
+        ms_direct = std::min(d0, d1);
+        ms_ao = std::min(a0, a1);
+        return true;
+    };
+    double bd, ba;
+    if (!bake_once(best, bd, ba) || !measure(best, bd, ba)) {   // warm-up, then the baseline
+        ltrg_SetTuning(dev, &best);
+        return 0;
+    }
+    struct Param { u32 ltrg_Tuning::*field; bool direct; std::vector<u32> cand; };
+    const Param params[] = {
+        {&ltrg_Tuning::direct_blocks_per_sm, true, {2, 4, 8, 16, 32}},
+        {&ltrg_Tuning::direct_block, true, {64, 128, 256}},
+        {&ltrg_Tuning::ao_blocks_per_sm, false, {4, 8, 16, 32}},
+        {&ltrg_Tuning::ao_block, false, {64, 128, 256}},
+    };
+    for (const Param& p : params) {
+        for (u32 v : p.cand) {
+            if (best.*p.field == v) continue;
+            ltrg_Tuning t = best;
+            t.*p.field = v;
+            double d, a;
+            if (!measure(t, d, a)) {
+                ltrg_SetTuning(dev, &best);
+                return 0;
+            }
+            double& cur = p.direct ? bd : ba;
+            double got = p.direct ? d : a;
+            if (got < cur * 0.98) {   // a clear win only
+                best = t;
+                bd = p.direct ? d : bd;
+                ba = p.direct ? ba : a;
+            }
+        }
+    }
+    ltrg_SetTuning(dev, &best);
+    if (out) *out = best;
+    return 1;
 }
 
 LTRAPI LTRBOOL ltrg_Wait(ltr_Scene* scene)

@@ -1469,7 +1469,9 @@ struct BatchCtx {
                 if (p == 0) {
                     CK(cudaMemcpyAsync(d_jobs, ph.djobs.data(), jb, cudaMemcpyHostToDevice, bst));
                     k_direct_batch_offsets<<<1, 32, 0, bst>>>((const DirectJob*) d_jobs, nj, d_off); note_launch();
-                    k_direct_trace_batch<<<(unsigned) sms * 8, 128, 0, bst>>>((const DirectJob*) d_jobs, nj, d_off, d_next);
+                    const ltrg_Tuning tu = get_tuning(device);
+                    k_direct_trace_batch<<<(unsigned) sms * tu.direct_blocks_per_sm, tu.direct_block, 0, bst>>>(
+                        (const DirectJob*) d_jobs, nj, d_off, d_next);
                     note_launch();
                 } else {
                     std::vector<unsigned long long> off(nj + 1, 0);
@@ -1478,7 +1480,9 @@ struct BatchCtx {
                     CK(cudaMemcpyAsync(d_off, off.data(), off.size() * sizeof(unsigned long long),
                                        cudaMemcpyHostToDevice, bst));
                     // the pageable copies above are staged before they return, so `off` may go
-                    k_ao_rays_batch<<<(unsigned) sms * 16, 128, 0, bst>>>((const AoJob*) d_jobs, nj, d_off, d_next);
+                    const ltrg_Tuning tu = get_tuning(device);
+                    k_ao_rays_batch<<<(unsigned) sms * tu.ao_blocks_per_sm, tu.ao_block, 0, bst>>>((const AoJob*) d_jobs, nj,
+                                                                                                 d_off, d_next);
                     note_launch();
                 }
                 CK(cudaGetLastError());
@@ -1959,8 +1963,10 @@ void run_bake(ltr_Scene* S)
             DirectJob job{da, d_items, d_dscan + items};
             CK(cudaStreamWaitEvent(st, batch->join(0, bidx, st, &job, nullptr, 0), 0));
         } else {
-            unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * 8, (items + 127) / 128);
-            k_direct_trace<<<grid, 128, 0, st>>>(da, d_items, d_dscan + items, d_next); note_launch();
+            const ltrg_Tuning tu = get_tuning(S->opt.device);
+            unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * tu.direct_blocks_per_sm,
+                                                                    (items + tu.direct_block - 1) / tu.direct_block);
+            k_direct_trace<<<grid, tu.direct_block, 0, st>>>(da, d_items, d_dscan + items, d_next); note_launch();
             CK(cudaGetLastError());
         }
     } else if (batch) {
@@ -2212,9 +2218,10 @@ void run_bake(ltr_Scene* S)
                 AoJob job{aa, d_hits};
                 CK(cudaStreamWaitEvent(st, batch->join(1, bidx, st, nullptr, &job, n_rays), 0));
             } else {
-                unsigned grid =
-                    (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * 16, (n_rays + 127) / 128);
-                k_ao_rays<<<grid, 128, 0, st>>>(aa, d_hits, n_rays, d_next); note_launch();
+                const ltrg_Tuning tu = get_tuning(S->opt.device);
+                unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * tu.ao_blocks_per_sm,
+                                                                        (n_rays + tu.ao_block - 1) / tu.ao_block);
+                k_ao_rays<<<grid, tu.ao_block, 0, st>>>(aa, d_hits, n_rays, d_next); note_launch();
                 CK(cudaGetLastError());
             }
             k_ao<<<blocks_for(n_samples), kThreads, 0, st>>>(aa, d_hits); note_launch();

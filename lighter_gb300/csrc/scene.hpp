@@ -58,6 +58,8 @@ struct ltr_Mesh {
 namespace lg {
 struct BatchCtx;   // bake.cu: the rendezvous of the scenes of one ltrg_StartBatch
 std::shared_ptr<BatchCtx> make_batch(int n, int device);
+// Launch shapes of the trace kernels of one device (api.cpp).
+ltrg_Tuning get_tuning(int device);
 }  // namespace lg
 
 struct ltr_Scene {

@@ -44,6 +44,30 @@ EXT_API = {
 }
 
 
+class Tuning(C.Structure):
+    _fields_ = [("direct_block", u32), ("direct_blocks_per_sm", u32), ("ao_block", u32), ("ao_blocks_per_sm", u32),
+                ("reserved", u32 * 8)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
+
+
+EXT_API.update({
+    "ltrg_GetTuning": (C.c_int, [C.c_int, C.POINTER(Tuning)]),
+    "ltrg_SetTuning": (C.c_int, [C.c_int, C.POINTER(Tuning)]),
+    "ltrg_Autotune": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+})
+
+
+def autotune(lib, scene) -> dict:
+    """Runs ltrg_Autotune on an ingested scene and returns the chosen launch shapes."""
+    t = Tuning()
+    if not lib.ltrg_Autotune(scene, C.byref(t)):
+        msg = lib.ltrg_LastError(scene)
+        raise RuntimeError("autotune failed: " + (msg.decode() if msg else "unknown"))
+    return t.as_dict()
+
+
 def set_options(lib, scene, **kw):
     o = Options()
     lib.ltrg_GetOptions(scene, C.byref(o))

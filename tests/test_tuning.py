@@ -1,0 +1,74 @@
+"""Launch shapes of the trace kernels (ltrg_Tuning) and the autotuner."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from lighter_gb300 import ext, scenes
+from lighter_gb300.scene import bake, ingest
+
+
+def _get(lib, dev=0):
+    t = ext.Tuning()
+    assert lib.ltrg_GetTuning(dev, C.byref(t))
+    return t
+
+
+def test_tuning_defaults_and_validation(gpu):
+    lib = gpu
+    saved = _get(lib)
+    try:
+        t = _get(lib)
+        assert (t.direct_block, t.direct_blocks_per_sm, t.ao_block, t.ao_blocks_per_sm) != (0, 0, 0, 0)
+        bad = ext.Tuning()
+        C.memmove(C.byref(bad), C.byref(t), C.sizeof(t))
+        bad.direct_block = 100                       # not a multiple of 32
+        assert lib.ltrg_SetTuning(0, C.byref(bad)) == 0
+        bad.direct_block = 1024                      # above 512
+        assert lib.ltrg_SetTuning(0, C.byref(bad)) == 0
+        bad.direct_block, bad.ao_blocks_per_sm = 64, 0
+        assert lib.ltrg_SetTuning(0, C.byref(bad)) == 0
+        assert lib.ltrg_SetTuning(-1, C.byref(t)) == 0
+        ok = ext.Tuning()
+        C.memmove(C.byref(ok), C.byref(t), C.sizeof(t))
+        ok.direct_block, ok.direct_blocks_per_sm = 64, 4
+        assert lib.ltrg_SetTuning(0, C.byref(ok)) == 1
+        got = _get(lib)
+        assert (got.direct_block, got.direct_blocks_per_sm) == (64, 4)
+        assert lib.ltrg_GetTuning(0, None) == 0
+    finally:
+        lib.ltrg_SetTuning(0, C.byref(saved))
+
+
+@pytest.mark.gpu
+def test_results_do_not_depend_on_launch_shape(gpu):
+    lib = gpu
+    saved = _get(lib)
+    d = scenes.mid(5, lm=128, n_boxes=24, n_spheres=3, bounces=0, ao_rays=8)
+    try:
+        a = bake(lib, d, debug=False)
+        t = _get(lib)
+        t.direct_block, t.direct_blocks_per_sm, t.ao_block, t.ao_blocks_per_sm = 256, 2, 64, 32
+        assert lib.ltrg_SetTuning(0, C.byref(t))
+        b = bake(lib, d, debug=False)
+        for x, y in zip(a.lightmaps, b.lightmaps):
+            np.testing.assert_array_equal(x[3], y[3])
+    finally:
+        lib.ltrg_SetTuning(0, C.byref(saved))
+
+
+@pytest.mark.gpu
+def test_autotune_picks_valid_shapes(gpu):
+    lib = gpu
+    saved = _get(lib)
+    h, keep = ingest(lib, scenes.mid(6, lm=128, n_boxes=24, n_spheres=3, bounces=0, ao_rays=8))
+    try:
+        t = ext.autotune(lib, h)
+        assert t["direct_block"] in (64, 128, 256) and t["ao_block"] in (64, 128, 256)
+        assert 1 <= t["direct_blocks_per_sm"] <= 64 and 1 <= t["ao_blocks_per_sm"] <= 64
+        assert _get(lib).as_dict() == t
+        info = ext.Stats()
+        assert lib.ltrg_GetStats(h, C.byref(info)) and info.shadow_evals > 0
+    finally:
+        lib.ltr_DestroyScene(h)
+        lib.ltrg_SetTuning(0, C.byref(saved))
