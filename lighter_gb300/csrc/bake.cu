@@ -658,22 +658,8 @@ struct AoArgs {
 };
 
 // Job_AORender_Inner (lighter.cpp:799-841), pass 1: every (sample, ray) is an
-// independent closest-hit query; persistent threads take rays one at a time
-// (consecutive rays of a sample share an origin) and store the hit fraction.
-// Work fetch for persistent threads: the lanes of a warp that ask together
-// share one atomic; each gets `chunk` consecutive items.
-__device__ __forceinline__ unsigned long long warp_fetch(unsigned long long* ctr, unsigned chunk)
-{
-    unsigned mask = __activemask();
-    int lane = threadIdx.x & 31;
-    int leader = __ffs(mask) - 1;
-    unsigned rank = __popc(mask & ((1u << lane) - 1u));
-    unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(ctr, (unsigned long long) __popc(mask) * chunk);
-    base = __shfl_sync(mask, base, leader);
-    return base + (unsigned long long) rank * chunk;
-}
-
+// independent closest-hit query; persistent warps take 32 x kAoChunk rays at a
+// time (see ao_item for their order) and store the hit fractions.
 constexpr unsigned kAoChunk = 4;
 
 // Ray r of sample s (i = s * ns + r): closest-hit fraction along the AO segment.
@@ -689,16 +675,43 @@ __device__ __forceinline__ void ao_ray(const AoArgs& a, float* __restrict__ hits
     hits[i] = bvh_closest(a.bvh, ro + dn * kSmall, B - dn * kSmall, a.err, nullptr);
 }
 
-__global__ void k_ao_rays(AoArgs a, float* __restrict__ hits, unsigned long long n_rays, unsigned long long* next)
+// AO work items in sample-tile order: tiles of 32 consecutive samples, and in a
+// tile, ray r of the 32 samples are items 32 r .. 32 r + 31. A warp takes 32 x
+// kAoChunk items and lane l traces items base + l + 32 k, so at every step its
+// lanes trace the same spiral direction from 32 neighbouring samples (coherent
+// traversals). Only the assignment of rays to threads changes: each hit lands
+// in its own slot s * ns + r, which the ordered reduction reads.
+__host__ __device__ __forceinline__ unsigned long long ao_items(u32 n_samples, int ns)
 {
+    return ((unsigned long long) (n_samples + 31) / 32) * 32ull * (unsigned long long) ns;
+}
+
+__device__ __forceinline__ bool ao_item(unsigned long long g, u32 n_samples, int ns, unsigned long long& i)
+{
+    const unsigned long long per_tile = 32ull * (unsigned long long) ns;
+    const unsigned long long tile = g / per_tile, w = g % per_tile;
+    const unsigned long long s = tile * 32 + w % 32;
+    if (s >= n_samples) return false;
+    i = s * (unsigned long long) ns + w / 32;
+    return true;
+}
+
+__global__ void k_ao_rays(AoArgs a, float* __restrict__ hits, unsigned long long n_items, unsigned long long* next)
+{
+    const int lane = threadIdx.x & 31;
     unsigned long long c_rays = 0;
     for (;;) {
-        unsigned long long i0 = warp_fetch(next, kAoChunk);
-        if (i0 >= n_rays) break;
-        unsigned long long i1 = i0 + kAoChunk < n_rays ? i0 + kAoChunk : n_rays;
-        for (unsigned long long i = i0; i < i1; ++i) {
-            ao_ray(a, hits, i);
-            ++c_rays;
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(next, 32ull * kAoChunk);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n_items) break;
+        for (unsigned k = 0; k < kAoChunk; ++k) {
+            const unsigned long long g = base + 32ull * k + lane;
+            unsigned long long i;
+            if (g < n_items && ao_item(g, a.n_samples, a.ns, i)) {
+                ao_ray(a, hits, i);
+                ++c_rays;
+            }
         }
     }
     if (a.counters) warp_add(&a.counters->ao_rays, c_rays);
@@ -787,16 +800,20 @@ __global__ void k_ao_rays_batch(const AoJob* __restrict__ jobs, int n, const uns
                                 unsigned long long* __restrict__ next)
 {
     const unsigned long long total = off[n];
+    const int lane = threadIdx.x & 31;
     unsigned long long c_rays = 0;
     int cur = -1;
     AoArgs a;
     float* hits = nullptr;
-    unsigned long long base = 0;
+    unsigned long long job0 = 0;
     for (;;) {
-        unsigned long long i0 = warp_fetch(next, kAoChunk);
-        if (i0 >= total) break;
-        unsigned long long i1 = i0 + kAoChunk < total ? i0 + kAoChunk : total;
-        for (unsigned long long g = i0; g < i1; ++g) {
+        unsigned long long wb = 0;
+        if (lane == 0) wb = atomicAdd(next, 32ull * kAoChunk);
+        wb = __shfl_sync(0xffffffffu, wb, 0);
+        if (wb >= total) break;
+        for (unsigned kk = 0; kk < kAoChunk; ++kk) {
+            const unsigned long long g = wb + 32ull * kk + lane;
+            if (g >= total) continue;
             const int k = find_job(off, n, g);
             if (k != cur) {
                 if (cur >= 0 && a.counters && c_rays) atomicAdd(&a.counters->ao_rays, c_rays);
@@ -804,10 +821,13 @@ __global__ void k_ao_rays_batch(const AoJob* __restrict__ jobs, int n, const uns
                 cur = k;
                 a = jobs[k].args;
                 hits = jobs[k].hits;
-                base = off[k];
+                job0 = off[k];
             }
-            ao_ray(a, hits, g - base);
-            ++c_rays;
+            unsigned long long i;
+            if (ao_item(g - job0, a.n_samples, a.ns, i)) {
+                ao_ray(a, hits, i);
+                ++c_rays;
+            }
         }
     }
     if (cur >= 0 && a.counters && c_rays) atomicAdd(&a.counters->ao_rays, c_rays);
@@ -1278,7 +1298,7 @@ struct BatchCtx {
         std::string error;
         std::vector<DirectJob> djobs;
         std::vector<AoJob> ajobs;
-        std::vector<unsigned long long> rays;   // AO rays per job
+        std::vector<unsigned long long> rays;   // AO work items per job (ao_items)
         std::vector<cudaEvent_t> ready;
         cudaEvent_t done = nullptr;
     };
@@ -2214,14 +2234,15 @@ void run_bake(ltr_Scene* S)
             unsigned long long* d_next = A.zeros<unsigned long long>(1);
             int dev_sms = 0;
             CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, S->opt.device));
+            const unsigned long long n_items = ao_items(n_samples, aa.ns);
             if (batch) {   // one trace launch for the whole batch
                 AoJob job{aa, d_hits};
-                CK(cudaStreamWaitEvent(st, batch->join(1, bidx, st, nullptr, &job, n_rays), 0));
+                CK(cudaStreamWaitEvent(st, batch->join(1, bidx, st, nullptr, &job, n_items), 0));
             } else {
                 const ltrg_Tuning tu = get_tuning(S->opt.device);
                 unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * tu.ao_blocks_per_sm,
-                                                                        (n_rays + tu.ao_block - 1) / tu.ao_block);
-                k_ao_rays<<<grid, tu.ao_block, 0, st>>>(aa, d_hits, n_rays, d_next); note_launch();
+                                                                        (n_items + tu.ao_block - 1) / tu.ao_block);
+                k_ao_rays<<<grid, tu.ao_block, 0, st>>>(aa, d_hits, n_items, d_next); note_launch();
                 CK(cudaGetLastError());
             }
             k_ao<<<blocks_for(n_samples), kThreads, 0, st>>>(aa, d_hits); note_launch();
