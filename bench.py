@@ -130,29 +130,13 @@ class ClockSampler:
 
 
 def _dist():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        import torch.distributed as dist
-        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        dist.init_process_group("gloo")
-        return world, rank, local, dist
-    return 1, 0, 0, None
+    from lighter_gb300 import replicas
+    return replicas.init()
 
 
 def _barrier(dist):
-    if dist is not None:
-        dist.barrier()
-
-
-def _allreduce(dist, vals, op):
-    if dist is None:
-        return vals
-    import torch
-    t = torch.tensor(vals, dtype=torch.float64)
-    dist.all_reduce(t, op=op)
-    return t.tolist()
+    from lighter_gb300 import replicas
+    replicas.barrier(dist)
 
 
 def _oracle_bake(desc, threads):
@@ -435,12 +419,8 @@ def main():
         return 0
 
     rays, dev_ms, wall, stats, clocks, h2d, d2h, launches, tuning = run_ours(args, world, rank, local, dist)
-    if dist is not None:
-        import torch.distributed as td
-        rays_all, = _allreduce(dist, [float(rays)], td.ReduceOp.SUM)
-        dev_ms_max, wall_max = _allreduce(dist, [dev_ms, wall], td.ReduceOp.MAX)
-    else:
-        rays_all, dev_ms_max, wall_max = float(rays), dev_ms, wall
+    from lighter_gb300 import replicas
+    rays_all, dev_ms_max, wall_max = replicas.aggregate(dist, rays, dev_ms, wall)
     if rank != 0:
         return 0
 
