@@ -228,6 +228,11 @@ LTRAPI LTRBOOL ltrdbg_LightmapSize(ltr_Scene* scene, u32 inst, u32* wh);
 LTRAPI LTRBOOL ltrdbg_GetSamples(ltr_Scene* scene, u32 inst, float* pos3, float* nrm3, u32* loc, float* radinfo4,
                                  float* color3);
 LTRAPI u32 ltrdbg_RadLinkCount(ltr_Scene* scene);
+/* Per-ray records of instance `inst` (keep_samples = 1): vis receives
+ * n_lights x n samples shadow factors (CalcInvShadowFactor, -1 where the pair
+ * was not traced), ao receives n x ao_num_samples AO closest-hit fractions (2
+ * for a miss); either may be NULL. Returns 0 when the bake recorded none. */
+LTRAPI LTRBOOL ltrdbg_GetRayData(ltr_Scene* scene, u32 inst, float* vis, float* ao);
 
 #ifdef __cplusplus
 }

@@ -27,6 +27,7 @@ def load_library(path: str, with_debug: bool = True, extra: dict | None = None):
     abi.bind(lib, abi.LTR_API)
     if with_debug:
         abi.bind(lib, abi.LTRDBG_API)
+        abi.bind(lib, {k: v for k, v in abi.LTRDBG_OPTIONAL.items() if hasattr(lib, k)})
     if extra:
         abi.bind(lib, extra)
     return lib

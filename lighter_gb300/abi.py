@@ -189,6 +189,12 @@ LTRDBG_API = {
 }
 
 
+# Bound where the library has them (the GPU library and the oracle port; not the reference build).
+LTRDBG_OPTIONAL = {
+    "ltrdbg_GetRayData": (C.c_int, [C.c_void_p, u32, C.c_void_p, C.c_void_p]),
+}
+
+
 def bind(lib, table):
     for name, (res, args) in table.items():
         fn = getattr(lib, name)

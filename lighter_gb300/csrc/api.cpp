@@ -461,4 +461,19 @@ LTRAPI LTRBOOL ltrdbg_GetSamples(ltr_Scene* s, u32 inst, float* pos3, float* nrm
 
 LTRAPI u32 ltrdbg_RadLinkCount(ltr_Scene* s) { return s->rad_links; }
 
+LTRAPI LTRBOOL ltrdbg_GetRayData(ltr_Scene* scene, u32 inst, float* vis, float* ao)
+{
+    if (scene->running.load() || inst >= scene->dump.size()) return 0;
+    const SampleDump& d = scene->dump[inst];
+    if (vis) {
+        if (d.vis.size() != (size_t) scene->lights.size() * d.loc.size()) return 0;
+        if (!d.vis.empty()) memcpy(vis, d.vis.data(), d.vis.size() * sizeof(float));
+    }
+    if (ao) {
+        if (d.ao.empty() && !d.loc.empty()) return 0;
+        if (!d.ao.empty()) memcpy(ao, d.ao.data(), d.ao.size() * sizeof(float));
+    }
+    return 1;
+}
+
 }  // extern "C"

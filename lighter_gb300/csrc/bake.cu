@@ -344,6 +344,7 @@ struct DirectArgs {
     float* kval;                // [light][sample] colour multiplier, 0 when nothing is added
     float4* ndir;               // [light][sample] normal-map contribution, w = 1 when recorded (may be null)
     Counters* counters;
+    float* vis;                 // [light][sample] shadow factor, -1 when not traced (debug record, may be null)
 };
 
 // Unshadowed terms of one (light, sample) pair of
@@ -408,6 +409,7 @@ __global__ void k_direct_setup(DirectArgs a, u32* __restrict__ flags)
         }
         a.kval[w] = 0.0f;
         if (a.ndir) a.ndir[w] = make_float4(0, 0, 0, 0);
+        if (a.vis) a.vis[w] = -1.0f;
         flags[w] = go ? 1u : 0u;
     }
 }
@@ -434,6 +436,7 @@ __device__ __forceinline__ void direct_pair(const DirectArgs& a, u32 w, u32& nq,
     LightTerms t;
     light_terms(a, L, s, t);
     float vis = inv_shadow(a.bvh, t.from, t.to, L.radius, a.err, nq, nv, nt);
+    if (a.vis) a.vis[w] = vis;
     V3 Lcol = mk(L.color[0], L.color[1], L.color[2]);
     float kv, fac;
     if (L.type == 2) {
@@ -1960,8 +1963,11 @@ void run_bake(ltr_Scene* S)
     float4* d_ndir = nullptr;
     S->stage = "rendering lightmaps";
     const bool want_normals = cfg.generate_normalmap_data != 0;
+    float* d_vis = nullptr;       // debug records (keep_samples)
+    float* d_ao_hits = nullptr;
     if (n_lights && n_samples) {
         d_kval = A.alloc<float>((size_t) n_lights * n_samples);
+        if (S->opt.keep_samples) d_vis = A.alloc<float>((size_t) n_lights * n_samples);
         if (want_normals) d_ndir = A.alloc<float4>((size_t) n_lights * n_samples);
         DirectArgs da;
         da.bvh = bv;
@@ -1977,6 +1983,7 @@ void run_bake(ltr_Scene* S)
         da.kval = d_kval;
         da.ndir = d_ndir;
         da.counters = d_cnt;
+        da.vis = d_vis;
         unsigned long long items = (unsigned long long) n_lights * n_samples;
         if (items >= 0xffffffffull) throw std::runtime_error("too many (light, sample) pairs for one bake");
         u32* d_dflags = A.alloc<u32>(items + 1);
@@ -2248,6 +2255,7 @@ void run_bake(ltr_Scene* S)
         if (aa.ns > 0) {
             unsigned long long n_rays = (unsigned long long) n_samples * aa.ns;
             float* d_hits = A.alloc<float>(n_rays);
+            d_ao_hits = d_hits;
             unsigned long long* d_next = A.zeros<unsigned long long>(1);
             int dev_sms = 0;
             CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, S->opt.device));
@@ -2369,7 +2377,17 @@ void run_bake(ltr_Scene* S)
     if (n_probe) CK(cudaMemcpyAsync(probe_lm.data(), d_lm, n_probe * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_probe * sizeof(float4));
     std::vector<float4> dpos, dnrm, drad, dlm;
     std::vector<u32> dloc;
+    std::vector<float> dvis, dao;
+    const int ao_ns = d_ao_hits ? cfg.ao_num_samples : 0;
     if (S->opt.keep_samples && n_samples) {
+        if (d_vis) {
+            dvis.resize((size_t) n_lights * n_samples);
+            CK(cudaMemcpyAsync(dvis.data(), d_vis, dvis.size() * sizeof(float), cudaMemcpyDeviceToHost, st)); note_d2h(dvis.size() * sizeof(float));
+        }
+        if (d_ao_hits) {
+            dao.resize((size_t) n_samples * ao_ns);
+            CK(cudaMemcpyAsync(dao.data(), d_ao_hits, dao.size() * sizeof(float), cudaMemcpyDeviceToHost, st)); note_d2h(dao.size() * sizeof(float));
+        }
         dpos.resize(n_samples); dnrm.resize(n_samples); drad.resize(n_samples); dlm.resize(n_samples); dloc.resize(n_samples);
         CK(cudaMemcpyAsync(dpos.data(), d_spos, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(float4));
         CK(cudaMemcpyAsync(dnrm.data(), d_snrm, n_samples * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(float4));
@@ -2416,6 +2434,15 @@ void run_bake(ltr_Scene* S)
                 d.color.insert(d.color.end(), {dlm[s].x, dlm[s].y, dlm[s].z});
                 d.loc.push_back(dloc[s]);
             }
+            d.n_lights = (u32) n_lights;
+            d.ao_ns = (u32) ao_ns;
+            d.vis.assign((size_t) n_lights * scount[i], -1.0f);
+            if (!dvis.empty())
+                for (int l = 0; l < n_lights; ++l)
+                    for (u32 k = 0; k < scount[i]; ++k)
+                        d.vis[(size_t) l * scount[i] + k] = dvis[(size_t) l * n_samples + sbeg[i] + k];
+            if (!dao.empty())
+                d.ao.assign(dao.begin() + (size_t) sbeg[i] * ao_ns, dao.begin() + (size_t) (sbeg[i] + scount[i]) * ao_ns);
         }
     }
 

@@ -42,6 +42,9 @@ struct HostLight {
 struct SampleDump {
     std::vector<float> pos, nrm, radinfo, color;
     std::vector<u32> loc;
+    std::vector<float> vis;   // [light][sample] shadow factor, -1 when not traced
+    std::vector<float> ao;    // [sample][ray] AO closest-hit fraction
+    u32 n_lights = 0, ao_ns = 0;
 };
 
 }  // namespace lg

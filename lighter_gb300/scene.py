@@ -277,12 +277,15 @@ def bake(lib, desc: SceneDesc, threads: int = 1, debug: bool = True, poll_s: flo
                 from .ext import get_stats
                 stats.update(get_stats(lib, scene))
 
-        return _collect(lib, scene, debug, stages, wall, final)
+        cfg = abi.Config()
+        lib.ltr_GetConfig(C.byref(cfg), scene)
+        ao_ns = int(cfg.ao_num_samples) if cfg.ao_distance and cfg.ao_num_samples > 0 else 0
+        return _collect(lib, scene, debug, stages, wall, final, len(desc.lights), ao_ns)
     finally:
         lib.ltr_DestroyScene(scene)
 
 
-def _collect(lib, scene, debug, stages, wall, final) -> "BakeResult":
+def _collect(lib, scene, debug, stages, wall, final, n_lights: int = 0, ao_ns: int = 0) -> "BakeResult":
     info = abi.WorkOutputInfo()
     lib.ltr_GetWorkOutputInfo(scene, C.byref(info))
     lms = []
@@ -316,6 +319,13 @@ def _collect(lib, scene, debug, stages, wall, final) -> "BakeResult":
             if n:
                 lib.ltrdbg_GetSamples(scene, i, d["pos"].ctypes.data, d["nrm"].ctypes.data,
                                       d["loc"].ctypes.data, d["radinfo"].ctypes.data, d["color"].ctypes.data)
+            if hasattr(lib, "ltrdbg_GetRayData"):
+                vis = np.zeros((n_lights, n), np.float32)
+                ao = np.zeros((n, ao_ns), np.float32)
+                if lib.ltrdbg_GetRayData(scene, i, vis.ctypes.data, ao.ctypes.data if ao_ns else None):
+                    d["vis"] = vis
+                    if ao_ns:
+                        d["ao"] = ao
             dbg.append(d)
     return BakeResult(lms, colors, stages, wall, dbg, final)
 

@@ -674,6 +674,10 @@ struct OInst {
     std::vector<V4> srad;
     std::vector<V3> lm;
     std::vector<Contrib> contrib;
+    // per-ray records of the last bake, for the hit/miss comparison with the GPU:
+    // dbg_vis[light * n + i] = CalcInvShadowFactor of (light, sample i), -1 when not traced;
+    // dbg_ao[i * ao_num_samples + r] = closest-hit fraction of AO ray r of sample i
+    std::vector<float> dbg_vis, dbg_ao;
 };
 struct OLight {
     u32 type; V3 pos, dir, up, color; float range, power, radius; int nsamples; float out, in, curve;
@@ -796,7 +800,7 @@ struct ltr_Scene {
     void prexform(OInst* mi);
     void colinfo(OInst* mi);
     void make_samples(OInst* mi);
-    void render_light(const OLight& L, OInst* mi);
+    void render_light(const OLight& L, OInst* mi, size_t li);
     void rad_links();
     void rad_bounce();
     void ao(OInst* mi, const std::vector<float>& randoff);
@@ -973,9 +977,10 @@ void ltr_Scene::make_samples(OInst* mi)
 }
 
 // Point / spot / directional direct light per sample (lighter.cpp:485-600, 623-665).
-void ltr_Scene::render_light(const OLight& L, OInst* mi)
+void ltr_Scene::render_light(const OLight& L, OInst* mi, size_t li)
 {
     size_t n = mi->lm.size();
+    float* dvis = &mi->dbg_vis[li * n];
     bool want_n = cfg.generate_normalmap_data && !mi->container;
     std::vector<Contrib> contribs;
     if (cfg.generate_normalmap_data) { Contrib z = {mk(0, 0, 0), -1}; contribs.assign(n, z); }
@@ -1004,6 +1009,7 @@ void ltr_Scene::render_light(const OLight& L, OInst* mi)
                 return;
             }
             float vis = inv_shadow(SP + SN * kShadowOffset, L.pos, L.radius);
+            dvis[i] = vis;
             float k = L.type == 2 ? f_dist * f_ndotl * f_dir * vis : f_dist * f_ndotl * vis;
             mi->lm[i] += L.color * k;
             if (want_n) {
@@ -1014,6 +1020,7 @@ void ltr_Scene::render_light(const OLight& L, OInst* mi)
         } else {
             float f_ndotl = fmax_(0.0f, dot(L.dir, SN));
             float vis = inv_shadow(SP + SN * kShadowOffset, SP + L.dir * L.range, L.radius);
+            dvis[i] = vis;
             mi->lm[i] += L.color * (f_ndotl * vis);
             if (want_n) {
                 float fac = vis * f_ndotl * brightness(L.color);
@@ -1110,6 +1117,7 @@ void ltr_Scene::ao(OInst* mi, const std::vector<float>& randoff)
     float dist = cfg.ao_distance, falloff = cfg.ao_falloff, mult = cfg.ao_multiplier, effect = cfg.ao_effect;
     int ns = cfg.ao_num_samples;
     V3 aoc = mk(cfg.ao_color_rgb[0], cfg.ao_color_rgb[1], cfg.ao_color_rgb[2]);
+    mi->dbg_ao.assign(mi->lm.size() * (size_t) (ns > 0 ? ns : 0), 2.0f);
     parallel_for(threads(), mi->lm.size(), [&](size_t i) {
         V3 SP = mi->spos[i], SN = mi->snrm[i];
         V3& out = mi->lm[i];
@@ -1118,6 +1126,7 @@ void ltr_Scene::ao(OInst* mi, const std::vector<float>& randoff)
         for (int s = 0; s < ns; ++s) {
             V3 rd = spiral_dir(SN, randoff[i], s, ns) * dist;
             float hit = closest_tree(ro, ro + rd);
+            mi->dbg_ao[i * ns + s] = hit;
             g_ao_rays.fetch_add(1, std::memory_order_relaxed);
             if (hit < 1.0f) f += 1.0f - hit;
         }
@@ -1275,6 +1284,7 @@ void ltr_Scene::run()
     parallel_for(nt, insts.size(), [&](size_t i) { make_samples(insts[i]); });
     if (!lights.empty()) {
         stage = "rendering lightmaps"; completion = 0;
+        for (OInst* mi : insts) mi->dbg_vis.assign(lights.size() * mi->lm.size(), -1.0f);
         for (size_t li = 0; li < lights.size(); ++li) {
             const OLight& L = lights[li];
             std::vector<i32> ids(1, 0);
@@ -1290,7 +1300,7 @@ void ltr_Scene::run()
             for (size_t k = 0; k < ids.size(); ++k) {
                 if (k > 0 && ids[k] == prev) continue;
                 prev = ids[k];
-                render_light(L, insts[prev]);
+                render_light(L, insts[prev], li);
             }
             completion = (li + 1) / float(lights.size());
         }
@@ -1494,6 +1504,23 @@ API int ltrdbg_GetSamples(ltr_Scene* s, u32 inst, float* pos3, float* nrm3, u32*
     return 1;
 }
 API u32 ltrdbg_RadLinkCount(ltr_Scene* s) { return (u32) s->links.size(); }
+
+// Per-ray records of instance `inst`: vis (n_lights x n samples) and ao (n x ao_num_samples),
+// either may be NULL; 0 when the bake recorded none.
+API int ltrdbg_GetRayData(ltr_Scene* s, u32 inst, float* vis, float* ao)
+{
+    if (inst >= s->insts.size()) return 0;
+    const OInst* mi = s->insts[inst];
+    if (vis) {
+        if (mi->dbg_vis.size() != s->lights.size() * mi->lm.size()) return 0;
+        memcpy(vis, mi->dbg_vis.data(), mi->dbg_vis.size() * sizeof(float));
+    }
+    if (ao) {
+        if (mi->dbg_ao.empty() && !mi->lm.empty()) return 0;
+        memcpy(ao, mi->dbg_ao.data(), mi->dbg_ao.size() * sizeof(float));
+    }
+    return 1;
+}
 
 // out[0..3] = shadow evaluations, sphere-trace steps, AO rays, radiosity visibility tests
 API void orc_GetCounters(unsigned long long* out)

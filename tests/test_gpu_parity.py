@@ -188,3 +188,44 @@ def test_abort_between_stages(gpu):
     finally:
         gpu.ltr_DestroyScene(scene)
         del keep
+
+
+RAY_FLIP_FRAC = 1e-3   # fewer than 0.1% of shadow / AO rays may flip hit/miss (grazing-edge cases only)
+
+
+def _ray_flips(rg, ro):
+    """(AO rays, AO flips, traced shadow pairs, blocked/unblocked flips, pairs traced by the GPU only).
+    The GPU skips pairs whose unshadowed term is zero (a directional light facing away), which
+    the reference and the oracle trace and then multiply by zero; those are not mismatches."""
+    ao_tot = ao_flip = sh_tot = sh_flip = traced_mismatch = 0
+    for a, b in zip(rg.debug, ro.debug):
+        if "ao" in a and "ao" in b and a["ao"].size:
+            ha, hb = a["ao"] < 1.0, b["ao"] < 1.0
+            ao_tot += ha.size
+            ao_flip += int((ha != hb).sum())
+        if "vis" in a and "vis" in b and a["vis"].size:
+            ta, tb = a["vis"] >= 0, b["vis"] >= 0
+            traced_mismatch += int((ta & ~tb).sum())
+            both = ta & tb
+            sh_tot += int(both.sum())
+            sh_flip += int(((a["vis"] == 0) != (b["vis"] == 0))[both].sum())
+    return ao_tot, ao_flip, sh_tot, sh_flip, traced_mismatch
+
+
+@pytest.mark.parametrize("name", ["cornell32_ao", "mid128", "large64"])
+def test_shadow_and_ao_rays_flip_below_a_thousandth(gpu, oracle, name):
+    import os
+    if name == "cornell32_ao":
+        d = scenes.cornell(4, lm=32, bounces=0, ao=True)
+    elif name == "mid128":
+        d = scenes.mid(4, lm=128, n_boxes=24, n_spheres=3, bounces=0, ao_rays=8)
+    else:
+        d = scenes.large(3, lm=64, grid=(64, 32), n_rocks=40, n_points=4, ao_rays=4, bounces=0)
+    rg = bake(gpu, d)
+    ro = bake(oracle, d, threads=os.cpu_count() or 1)
+    ao_tot, ao_flip, sh_tot, sh_flip, mism = _ray_flips(rg, ro)
+    assert ao_tot > 0 and sh_tot > 0
+    assert ao_flip <= RAY_FLIP_FRAC * ao_tot, f"{name}: {ao_flip} of {ao_tot} AO rays flip"
+    assert sh_flip <= RAY_FLIP_FRAC * sh_tot, f"{name}: {sh_flip} of {sh_tot} shadow pairs flip"
+    assert mism <= RAY_FLIP_FRAC * sh_tot, f"{name}: {mism} pairs traced by the GPU only"
+    print(f"{name}: AO {ao_flip}/{ao_tot} flips, shadow {sh_flip}/{sh_tot} flips, traced-set mismatch {mism}")
