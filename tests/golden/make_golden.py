@@ -60,10 +60,10 @@ def result_arrays(res, samples: bool):
             out[f"nrm_{uid}"] = nrm
     out["probes"] = res.sample_colors
     out["counts"] = np.array([len(d["loc"]) for d in res.debug], np.int64)
-    if samples:
+    if samples:   # the per-sample arrays the reference harness exports (not the per-ray records)
         for i, d in enumerate(res.debug):
-            for k, v in d.items():
-                out[f"s{i}_{k}"] = v
+            for k in ("pos", "nrm", "loc", "radinfo", "color"):
+                out[f"s{i}_{k}"] = d[k]
     return out
 
 
