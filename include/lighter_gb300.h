@@ -233,6 +233,10 @@ LTRAPI u32 ltrdbg_RadLinkCount(ltr_Scene* scene);
  * was not traced), ao receives n x ao_num_samples AO closest-hit fractions (2
  * for a miss); either may be NULL. Returns 0 when the bake recorded none. */
 LTRAPI LTRBOOL ltrdbg_GetRayData(ltr_Scene* scene, u32 inst, float* vis, float* ao);
+/* n values of (float) rand() / RAND_MAX exactly as n rand() calls would give
+ * them, leaving the C library's generator where those calls would (the AO
+ * stage's bulk draw, exposed for testing). */
+LTRAPI void ltrdbg_DrawRandFloats(float* out, u32 n);
 
 #ifdef __cplusplus
 }

@@ -39,6 +39,7 @@ ltr_Scene::~ltr_Scene()
     if (worker.joinable()) worker.join();
     clear_outputs();
     if (pinned) cudaFreeHost(pinned);
+    if (ao_pinned) cudaFreeHost(ao_pinned);
     for (HostInst* mi : insts) delete mi;
     for (ltr_Mesh* m : meshes) delete m;
 }

@@ -1093,7 +1093,6 @@ struct StageClock {
     }
 };
 
-inline float randf_host() { return (float) rand() / (float) RAND_MAX; }   // lighter_int.hpp:271
 
 void check_abort(ltr_Scene* s)
 {
@@ -1546,6 +1545,25 @@ void batch_leave(BatchCtx* b, int idx) { b->leave(idx); }
 
 // ----------------------------------------------------------------------------- the bake
 
+// The default stream-ordered memory pool returns its memory to the driver at
+// every synchronisation (release threshold 0), so each bake's few dozen
+// cudaMallocAsync calls would map fresh memory. Keeping up to 8 GiB cached
+// per device makes a repeated bake's allocations pool hits.
+void keep_pool_memory(int device)
+{
+    static std::mutex mu;
+    static std::vector<char> done;
+    std::lock_guard<std::mutex> lk(mu);
+    if ((int) done.size() <= device) done.resize(device + 1, 0);
+    if (done[device]) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = 8ull << 30;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    done[device] = 1;
+}
+
 void run_bake(ltr_Scene* S)
 {
     const ltr_Config& cfg = S->cfg;
@@ -1565,6 +1583,7 @@ void run_bake(ltr_Scene* S)
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw std::runtime_error("no CUDA device available");
     if (S->opt.device >= ndev) throw std::runtime_error("ltrg_Options.device out of range");
     CK(cudaSetDevice(S->opt.device));
+    keep_pool_memory(S->opt.device);
     if (batch) {
         batch->acquire_start(bidx);
         batch_leave_end.slot = true;
@@ -1889,15 +1908,26 @@ void run_bake(ltr_Scene* S)
     // AO's per-sample rand() draws (lighter.cpp:819) come after every user
     // callback that could call rand() itself: here unless a host sample_fn
     // still has to run, in which case they follow its calls.
-    std::vector<float> ao_randoff;
+    // drawn into page-locked memory the scene keeps, so their upload does not wait
+    // for the kernels queued before it
+    float* ao_randoff = nullptr;
+    if (n_samples && cfg.ao_distance && cfg.ao_num_samples > 0) {
+        if (S->ao_pinned_n < n_samples) {
+            if (S->ao_pinned) cudaFreeHost(S->ao_pinned);
+            S->ao_pinned = nullptr;
+            S->ao_pinned_n = 0;
+            CK(cudaHostAlloc((void**) &S->ao_pinned, (size_t) n_samples * sizeof(float), cudaHostAllocDefault));
+            S->ao_pinned_n = n_samples;
+        }
+        ao_randoff = S->ao_pinned;
+    }
     std::thread ao_thread;
     const bool do_ao = cfg.ao_distance && n_samples && cfg.ao_num_samples > 0;
     if (batch && !do_ao) batch->rand_end(bidx);   // draws nothing: the next scene's turn
     if (do_ao && (gpu_sample_fn || !cfg.bounce_count))
-        ao_thread = std::thread([&ao_randoff, n_samples, batch, bidx]() {
+        ao_thread = std::thread([ao_randoff, n_samples, batch, bidx]() {
             if (batch) batch->rand_begin(bidx);
-            ao_randoff.resize(n_samples);
-            for (u32 s = 0; s < n_samples; ++s) ao_randoff[s] = randf_host();   // instance order, sample order
+            rand_floats(ao_randoff, n_samples);   // instance order, sample order
             if (batch) batch->rand_end(bidx);
         });
     struct JoinGuard { std::thread& t; ~JoinGuard() { if (t.joinable()) t.join(); } } ao_guard{ao_thread};
@@ -2116,8 +2146,7 @@ void run_bake(ltr_Scene* S)
                 batch->release();
                 batch->rand_begin(bidx);
             }
-            ao_randoff.resize(n_samples);
-            for (u32 s = 0; s < n_samples; ++s) ao_randoff[s] = randf_host();
+            rand_floats(ao_randoff, n_samples);
             if (batch) {
                 batch->rand_end(bidx);
                 batch->acquire();
@@ -2230,13 +2259,16 @@ void run_bake(ltr_Scene* S)
         ao_thread.join();
         if (batch) batch->acquire();
     }
+    TRACE("ao draws joined");
     check_abort(S);
 
     // ---- ambient occlusion (Job_AORender)
     cudaEvent_t e_ao0 = clock.mark();
     if (do_ao) {
         S->stage = "rendering ambient occlusion";
-        float* d_ro = A.upload(ao_randoff);
+        float* d_ro = A.alloc<float>(n_samples);
+        CK(cudaMemcpyAsync(d_ro, ao_randoff, (size_t) n_samples * sizeof(float), cudaMemcpyHostToDevice, st));
+        note_h2d((size_t) n_samples * sizeof(float));
         AoArgs aa;
         aa.bvh = bv;
         aa.err = err_ao;

@@ -63,6 +63,8 @@ struct BatchCtx;   // bake.cu: the rendezvous of the scenes of one ltrg_StartBat
 std::shared_ptr<BatchCtx> make_batch(int n, int device);
 // Launch shapes of the trace kernels of one device (api.cpp).
 ltrg_Tuning get_tuning(int device);
+// n values of (float) rand() / RAND_MAX, as n rand() calls would give and leave the state (rng.cpp).
+void rand_floats(float* out, size_t n);
 }  // namespace lg
 
 struct ltr_Scene {
@@ -75,6 +77,8 @@ struct ltr_Scene {
     std::vector<ltr_WorkOutput> outputs;   // buffers point into `pinned`
     void* pinned = nullptr;                 // page-locked output storage, reused across bakes
     size_t pinned_bytes = 0;
+    float* ao_pinned = nullptr;             // page-locked AO random offsets, reused across bakes
+    lg::u32 ao_pinned_n = 0;
     std::vector<lg::SampleDump> dump;
     lg::u32 rad_links = 0;
     ltrg_Stats stats;
