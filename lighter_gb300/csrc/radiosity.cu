@@ -3,6 +3,7 @@
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <stdexcept>
 #include <string>
 
@@ -28,47 +29,58 @@ __device__ __forceinline__ float to_f(float v) { return v; }
 __device__ __forceinline__ float to_f(__half v) { return __half2float(v); }
 __device__ __forceinline__ float to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
 
-// Link factor of the pair (i, j), i < j (lighter.cpp:733-757): facing tests on
-// the unnormalised offset, f = dotA dotB / (|d|^4 pi) >= SMALL_FLOAT, then the
-// predicate on the segment between the two samples.
-__device__ __forceinline__ float pair_factor(const BvhView& bvh, ErrFlag err, int links, V3 AP, V3 AN, V3 BP, V3 BN,
-                                             unsigned& vis)
+// Form factors in two passes, with the reference's pair test and factor
+// (lighter.cpp:733-757) and its link predicate:
+//  1. k_ff_pretest: every pair (i, j), i < j, of a 32 x 32 tile gets the
+//     facing tests on the unnormalised offset and f = dA dB / (|d|^4 pi) >= SMALL_FLOAT;
+//     F receives f (both (i, j) and (j, i), through a shared-memory transpose) or
+//     0, and the pairs that passed are appended to a list.
+//  2. k_ff_visibility: persistent warps take 32 listed pairs at a time and trace
+//     ltr_Scene::VisibilityTest (lighter.cpp:138-147: segment shrunk by
+//     SMALL_FLOAT at both ends, any occluder hit); a pair the predicate rejects
+//     gets F = 0 back in both entries.
+// The dense pair loop so runs at tile speed and the divergent rays run apart
+// from it; F and the link count are those of one combined pass.
+struct PairRef {
+    u32 i, j;
+};
+
+__device__ __forceinline__ float pair_pretest(V3 AP, V3 AN, V3 BP, V3 BN)
 {
     V3 pd = BP - AP;
     float dA = dot(AN, pd), dB = dot(BN, -pd);
     if (dA <= kSmall || dB <= kSmall) return 0.0f;
     float l2 = lensq(pd);
     float f = dA * dB / (l2 * l2 * 3.14159265358979323846f);
-    if (f < kSmall) return 0.0f;
-    ++vis;
-    // ltr_Scene::VisibilityTest (lighter.cpp:138-147): segment shrunk by
-    // SMALL_FLOAT at both ends, any occluder hit
-    V3 dn = normalized(BP - AP);
-    bool occluded = bvh_any_hit(bvh, AP + dn * kSmall, BP - dn * kSmall, err);
-    bool keep = links == 0 ? occluded : !occluded;
-    return keep ? f : 0.0f;
+    return f < kSmall ? 0.0f : f;
 }
 
-// 32x32 tile of F per block (upper-triangle tiles only); entries written to
-// both (i, j) and (j, i) through a shared-memory transpose.
+// counts[0]: pairs that passed (appended; entries past `cap` are dropped and
+// the host runs the pass again with room for all of them)
 template <class T>
-__global__ void k_form_factors(u32 n, const float4* __restrict__ pos, const float4* __restrict__ nrm, BvhView bvh,
-                               ErrFlag err, int links, T* __restrict__ F, unsigned long long* counts)
+__global__ void k_ff_pretest(u32 n, const float4* __restrict__ pos, const float4* __restrict__ nrm, T* __restrict__ F,
+                             PairRef* __restrict__ cand, unsigned long long cap, unsigned long long* counts)
 {
     __shared__ float tile[32][33];
     const u32 bi = blockIdx.y, bj = blockIdx.x;
     if (bj < bi) return;
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    unsigned nlinks = 0, nvis = 0;
+    const int tx = threadIdx.x, ty = threadIdx.y;   // a warp is one tile row ty (lanes tx)
     for (int k = 0; k < 4; ++k) {
         int r = ty + 8 * k;
         u32 i = bi * 32 + r, j = bj * 32 + tx;
         float f = 0.0f;
-        if (i < j && j < n) {
-            f = pair_factor(bvh, err, links, ld3(pos[i]), ld3(nrm[i]), ld3(pos[j]), ld3(nrm[j]), nvis);
-            nlinks += f != 0.0f;
-        }
+        if (i < j && j < n) f = pair_pretest(ld3(pos[i]), ld3(nrm[i]), ld3(pos[j]), ld3(nrm[j]));
         tile[r][tx] = f;
+        const unsigned m = __ballot_sync(0xffffffffu, f != 0.0f);
+        if (m) {
+            unsigned long long base = 0;
+            if (tx == 0) base = atomicAdd(&counts[0], (unsigned long long) __popc(m));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (f != 0.0f) {
+                unsigned long long at = base + __popc(m & ((1u << tx) - 1u));
+                if (at < cap) cand[at] = PairRef{i, j};
+            }
+        }
     }
     __syncthreads();
     for (int k = 0; k < 4; ++k) {
@@ -83,15 +95,38 @@ __global__ void k_form_factors(u32 n, const float4* __restrict__ pos, const floa
             if (i2 < n && j2 < n) F[(size_t) i2 * n + j2] = to_store<T>(tile[tx][r]);
         }
     }
-    // block totals
-    for (int o = 16; o > 0; o >>= 1) {
-        nlinks += __shfl_down_sync(0xffffffffu, nlinks, o);
-        nvis += __shfl_down_sync(0xffffffffu, nvis, o);
+}
+
+// counts[1]: links kept
+template <class T>
+__global__ void k_ff_visibility(u32 n, const float4* __restrict__ pos, BvhView bvh, ErrFlag err, int links,
+                                T* __restrict__ F, const PairRef* __restrict__ cand, unsigned long long n_cand,
+                                unsigned long long* next, unsigned long long* counts)
+{
+    const int lane = threadIdx.x & 31;
+    unsigned long long kept = 0;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(next, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n_cand) break;
+        const unsigned long long k = base + lane;
+        if (k < n_cand) {
+            const PairRef pr = cand[k];
+            V3 AP = ld3(pos[pr.i]), BP = ld3(pos[pr.j]);
+            V3 dn = normalized(BP - AP);
+            bool occluded = bvh_any_hit(bvh, AP + dn * kSmall, BP - dn * kSmall, err);
+            bool keep = links == 0 ? occluded : !occluded;
+            if (keep) {
+                ++kept;
+            } else {
+                F[(size_t) pr.i * n + pr.j] = to_store<T>(0.0f);
+                F[(size_t) pr.j * n + pr.i] = to_store<T>(0.0f);
+            }
+        }
     }
-    if (tx == 0) {
-        atomicAdd(&counts[0], (unsigned long long) nlinks);
-        atomicAdd(&counts[1], (unsigned long long) nvis);
-    }
+    for (int o = 16; o > 0; o >>= 1) kept += __shfl_down_sync(0xffffffffu, kept, o);
+    if (lane == 0 && kept) atomicAdd(&counts[1], kept);
 }
 
 // X_j = (out_j * diffuse_j) * area_j (lighter.cpp:781-782 without the factor).
@@ -138,6 +173,56 @@ __global__ void k_rad_update(u32 n, const float4* __restrict__ Y, float4* __rest
     out[j] = y;
 }
 
+// Both passes on `st`; returns the link and visibility-ray counts (synchronises
+// the stream once after the first pass, to size the pair list).
+template <class T>
+RadFormFactors build_ff(u32 n, const float4* pos, const float4* nrm, const BvhView& bvh, ErrFlag err, int links, T* F,
+                        cudaStream_t st)
+{
+    RadFormFactors out;
+    if (n == 0) return out;
+    const u32 nb = (n + 31) / 32;
+    if (nb > 65535) throw std::runtime_error("radiosity: too many elements for the tile grid");
+    const unsigned long long pairs = (unsigned long long) n * (n - 1) / 2;
+    unsigned long long cap = std::min<unsigned long long>(pairs, std::max<unsigned long long>(1ull << 24, pairs / 16));
+    unsigned long long* counts = nullptr;   // [0] pairs that passed, [1] links kept, [2] work counter
+    PairRef* cand = nullptr;
+    RCK(cudaMallocAsync(&counts, 3 * sizeof(unsigned long long), st));
+    struct Free {
+        cudaStream_t st; void** p[2];
+        ~Free() { for (void** q : p) if (*q) cudaFreeAsync(*q, st); }
+    } guard{st, {(void**) &counts, (void**) &cand}};
+    unsigned long long n_cand = 0;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        RCK(cudaMallocAsync(&cand, std::max<unsigned long long>(cap, 1) * sizeof(PairRef), st));
+        RCK(cudaMemsetAsync(counts, 0, 3 * sizeof(unsigned long long), st));
+        k_ff_pretest<T><<<dim3(nb, nb), dim3(32, 8), 0, st>>>(n, pos, nrm, F, cand, cap, counts); note_launch();
+        RCK(cudaGetLastError());
+        RCK(cudaMemcpyAsync(&n_cand, counts, sizeof(n_cand), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(n_cand));
+        RCK(cudaStreamSynchronize(st));
+        if (n_cand <= cap) break;
+        RCK(cudaFreeAsync(cand, st));   // again, with room for every pair that passed
+        cand = nullptr;
+        cap = n_cand;
+    }
+    if (n_cand > cap) throw std::runtime_error("radiosity: pair list overflow");
+    if (n_cand) {
+        int dev = 0, sms = 0;
+        RCK(cudaGetDevice(&dev));
+        RCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) sms * 8, (n_cand + 127) / 128);
+        k_ff_visibility<T><<<grid, 128, 0, st>>>(n, pos, bvh, err, links, F, cand, n_cand, counts + 2, counts);
+        note_launch();
+        RCK(cudaGetLastError());
+    }
+    unsigned long long hc[2] = {0, 0};
+    RCK(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(hc));
+    RCK(cudaStreamSynchronize(st));
+    out.vis_rays = n_cand;
+    out.links = hc[1];
+    return out;
+}
+
 template <class T>
 RadResult solve_t(const RadDevInputs& in, const RadSettings& rs, const BvhView& bvh, ErrFlag err, cudaStream_t st,
                   float4* total_out, std::atomic<bool>* abort_flag)
@@ -152,29 +237,22 @@ RadResult solve_t(const RadDevInputs& in, const RadSettings& rs, const BvhView& 
                                  std::to_string(fbytes >> 20) + " MiB, more than the free device memory");
     T* F = nullptr;
     float4 *out, *X, *Y;
-    unsigned long long* counts;
     RCK(cudaMallocAsync(&F, fbytes ? fbytes : 1, st));
     RCK(cudaMallocAsync(&out, n * sizeof(float4), st));
     RCK(cudaMallocAsync(&X, n * sizeof(float4), st));
     RCK(cudaMallocAsync(&Y, n * sizeof(float4), st));
-    RCK(cudaMallocAsync(&counts, 2 * sizeof(unsigned long long), st));
     struct Free {
-        cudaStream_t st; void* p[5];
+        cudaStream_t st; void* p[4];
         ~Free() { for (void* q : p) if (q) cudaFreeAsync(q, st); }
-    } guard{st, {F, out, X, Y, counts}};
+    } guard{st, {F, out, X, Y}};
     float4* total = total_out;
     RCK(cudaMemcpyAsync(out, in.emit, n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
     if (total != in.emit) RCK(cudaMemcpyAsync(total, in.emit, n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
-    RCK(cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned long long), st));
 
     cudaEvent_t e0, e1, e2;
     RCK(cudaEventCreate(&e0)); RCK(cudaEventCreate(&e1)); RCK(cudaEventCreate(&e2));
     RCK(cudaEventRecord(e0, st));
-    u32 nb = (n + 31) / 32;
-    if (nb > 65535) throw std::runtime_error("radiosity: too many elements for the tile grid");
-    dim3 grid(nb, nb), block(32, 8);
-    k_form_factors<T><<<grid, block, 0, st>>>(n, in.pos, in.nrm, bvh, err, rs.links, F, counts); note_launch();
-    RCK(cudaGetLastError());
+    RadFormFactors ff = build_ff<T>(n, in.pos, in.nrm, bvh, err, rs.links, F, st);
     RCK(cudaEventRecord(e1, st));
     for (int b = 0; b < rs.bounces; ++b) {
         if (abort_flag && abort_flag->load()) break;
@@ -184,15 +262,13 @@ RadResult solve_t(const RadDevInputs& in, const RadSettings& rs, const BvhView& 
         RCK(cudaGetLastError());
     }
     RCK(cudaEventRecord(e2, st));
-    unsigned long long hc[2];
-    RCK(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(hc));
     RCK(cudaStreamSynchronize(st));
     float m1 = 0, m2 = 0;
     cudaEventElapsedTime(&m1, e0, e1);
     cudaEventElapsedTime(&m2, e1, e2);
     cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
-    rr.links = hc[0];
-    rr.vis_rays = hc[1];
+    rr.links = ff.links;
+    rr.vis_rays = ff.vis_rays;
     rr.pairs = (uint64_t) n * (n - 1) / 2;
     rr.ms_links = m1;
     rr.ms_bounce = m2;
@@ -213,24 +289,7 @@ RadResult radiosity_solve_dev(const RadDevInputs& in, const RadSettings& rs, con
 RadFormFactors radiosity_form_factors_f32(uint32_t n, const float4* pos, const float4* nrm, const BvhView& bvh,
                                           ErrFlag err, int links, float* F, cudaStream_t st)
 {
-    RadFormFactors out;
-    if (n == 0) return out;
-    u32 nb = (n + 31) / 32;
-    if (nb > 65535) throw std::runtime_error("radiosity: too many elements for the tile grid");
-    unsigned long long* counts = nullptr;
-    RCK(cudaMallocAsync(&counts, 2 * sizeof(unsigned long long), st));
-    RCK(cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned long long), st));
-    dim3 grid(nb, nb), block(32, 8);
-    k_form_factors<float><<<grid, block, 0, st>>>(n, pos, nrm, bvh, err, links, F, counts); note_launch();
-    cudaError_t le = cudaGetLastError();
-    unsigned long long hc[2] = {0, 0};
-    if (le == cudaSuccess) le = cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st);
-    cudaFreeAsync(counts, st);
-    RCK(le);
-    RCK(cudaStreamSynchronize(st));
-    out.links = hc[0];
-    out.vis_rays = hc[1];
-    return out;
+    return build_ff<float>(n, pos, nrm, bvh, err, links, F, st);
 }
 
 RadResult radiosity_solve(const RadInputs& in, const RadSettings& rs, const BvhView& bvh, ErrFlag err, cudaStream_t st,

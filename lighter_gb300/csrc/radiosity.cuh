@@ -51,7 +51,8 @@ RadResult radiosity_solve_dev(const RadDevInputs& in, const RadSettings& rs, con
                               cudaStream_t st, float4* total_out, std::atomic<bool>* abort_flag);
 
 // Only the form factors: F (n x n FP32, row-major) with the pair test and the
-// `links` predicate; returns the link and visibility-ray counts (synchronises
+// `links` predicate, in two passes (pair tests, then the visibility rays of the
+// pairs that passed); returns the link and visibility-ray counts (synchronises
 // the stream).
 struct RadFormFactors {
     uint64_t links = 0, vis_rays = 0;
