@@ -178,8 +178,7 @@ LTRAPI LTRBOOL ltrg_GatherGetG(ltrg_Gather* g, float* out);
 LTRAPI const char* ltrg_GatherLastError(ltrg_Gather* g);
 /* B after `bounces` sweeps for R right-hand sides; host buffers:
  *   albedo_rgb n x 3, emission n x R, out n x R (row-major).
- * precision LTRG_F_*, refine LTRG_REFINE_*; for FP16/BF16 R <= 256 (R <= 192
- * with LTRG_REFINE_FULL).
+ * precision LTRG_F_*, refine LTRG_REFINE_*; for FP16/BF16 R <= 256.
  * Returns 1, or 0 with ltrg_GatherLastError set. */
 LTRAPI LTRBOOL ltrg_GatherSolve(ltrg_Gather* g, const float* albedo_rgb, const float* emission, u32 R, int bounces,
                                 int precision, int refine, float* out, ltrg_GatherStats* stats);

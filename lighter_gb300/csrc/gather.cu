@@ -59,9 +59,8 @@ void gck(cudaError_t e, const char* what, int line)
 
 constexpr int BM = 128;                  // rows per tcgen05.mma (M)
 constexpr int ROWS = 2 * BM;             // rows of G per work unit
-constexpr int BK = 64;                   // k per stage: 64 x 2 B = one 128-byte swizzle row
+constexpr int BK = 64;                   // k per work unit (and the padding of a row of G)
 constexpr int UK = 16;                   // k per tcgen05.mma (kind::f16)
-constexpr int A_BYTES = ROWS * BK * 2;   // 32 KiB
 constexpr int MAX_BN = 256;
 constexpr int TMEM_COLS = 512;           // two accumulators of up to 256 columns
 constexpr int kThreads = 192;
@@ -128,17 +127,20 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
         : "memory");
 }
 
-// Matrix descriptor of a K-major operand tile written by TMA with the 128-byte
-// swizzle: rows of 128 bytes, groups of 8 rows 1024 bytes apart. Advancing K
-// by 16 elements inside the swizzle row adds 32 bytes to the start address.
+// Matrix descriptor of a K-major operand tile written by TMA with the swizzle
+// of its row length KB x 2 bytes: 128-byte rows (KB = 64, 128-byte swizzle) or
+// 64-byte rows (KB = 32, 64-byte swizzle), groups of 8 rows 8 x row bytes
+// apart. Advancing K by 16 elements inside a row adds 32 bytes to the start.
+template <int KB>
 __device__ __forceinline__ uint64_t sdesc(uint32_t addr)
 {
+    static_assert(KB == 64 || KB == 32, "stage k must be 64 or 32");
     uint64_t d = 0;
-    d |= (uint64_t) ((addr >> 4) & 0x3FFFu);   // start address >> 4
-    d |= (uint64_t) 1u << 16;                   // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t) (1024u >> 4) << 32;         // stride byte offset
-    d |= (uint64_t) 1u << 46;                   // descriptor version
-    d |= (uint64_t) 2u << 61;                   // 128-byte swizzle
+    d |= (uint64_t) ((addr >> 4) & 0x3FFFu);          // start address >> 4
+    d |= (uint64_t) 1u << 16;                          // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t) ((8u * KB * 2) >> 4) << 32;        // stride byte offset: 8 rows
+    d |= (uint64_t) 1u << 46;                          // descriptor version
+    d |= (uint64_t) (KB == 64 ? 2u : 4u) << 61;        // 128-byte or 64-byte swizzle
     return d;
 }
 
@@ -199,10 +201,14 @@ struct UmmaArgs {
     u32* err;
 };
 
+// KB: k per pipeline stage (a 64-wide work unit takes 64 / KB stages).
+template <int KB>
 __global__ void __launch_bounds__(kThreads, 1)
     k_umma_gather(const __grid_constant__ CUtensorMap tmG, const __grid_constant__ CUtensorMap tmGl,
                   const __grid_constant__ CUtensorMap tmXh, const __grid_constant__ CUtensorMap tmXl, UmmaArgs a)
 {
+    constexpr int SPU = BK / KB;                 // stages per work unit
+    constexpr u32 A_BYTES = ROWS * KB * 2;       // one 256-row tile of G per stage
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = (unsigned char*) ((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t) 1023);
     uint64_t* bars = reinterpret_cast<uint64_t*>(base + (size_t) a.stages * a.stage_bytes);
@@ -217,7 +223,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint64_t total = (uint64_t) a.n_rp * a.nkb;
     const uint64_t lo = (uint64_t) blockIdx.x * total / gridDim.x;
     const uint64_t hi = (uint64_t) (blockIdx.x + 1) * total / gridDim.x;
-    const u32 b_bytes = a.BN * BK * 2;
+    const u32 b_bytes = a.BN * KB * 2;
     const u32 off_gl = A_BYTES;
     const u32 off_xh = a.mode == LTRG_REFINE_FULL ? 2 * A_BYTES : A_BYTES;
     const u32 off_xl = off_xh + b_bytes;
@@ -243,18 +249,24 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     if (warp == 0) {
         if (lane == 0) {
-            // producer
+            // producer: stage counter i runs over the units' stages
             uint64_t i = 0;
-            for (uint64_t u = lo; u < hi; ++u, ++i) {
-                const u32 s = (u32) (i % a.stages);
-                if (i >= a.stages && !mbar_wait(&empty[s], (u32) ((i / a.stages) - 1) & 1u, a.err, kErrProducer)) break;
-                const int kx = (int) ((u % a.nkb) * BK), ry = (int) ((u / a.nkb) * ROWS);
-                unsigned char* st = base + (size_t) s * a.stage_bytes;
-                mbar_expect_tx(&full[s], tx_bytes);
-                tma_load_2d(st, &tmG, &full[s], kx, ry);
-                if (a.mode == LTRG_REFINE_FULL) tma_load_2d(st + off_gl, &tmGl, &full[s], kx, ry);
-                tma_load_2d(st + off_xh, &tmXh, &full[s], kx, 0);
-                if (a.mode >= LTRG_REFINE_RHS) tma_load_2d(st + off_xl, &tmXl, &full[s], kx, 0);
+            bool ok = true;
+            for (uint64_t u = lo; u < hi && ok; ++u) {
+                for (int q = 0; q < SPU; ++q, ++i) {
+                    const u32 s = (u32) (i % a.stages);
+                    if (i >= a.stages && !mbar_wait(&empty[s], (u32) ((i / a.stages) - 1) & 1u, a.err, kErrProducer)) {
+                        ok = false;
+                        break;
+                    }
+                    const int kx = (int) ((u % a.nkb) * BK + q * KB), ry = (int) ((u / a.nkb) * ROWS);
+                    unsigned char* st = base + (size_t) s * a.stage_bytes;
+                    mbar_expect_tx(&full[s], tx_bytes);
+                    tma_load_2d(st, &tmG, &full[s], kx, ry);
+                    if (a.mode == LTRG_REFINE_FULL) tma_load_2d(st + off_gl, &tmGl, &full[s], kx, ry);
+                    tma_load_2d(st + off_xh, &tmXh, &full[s], kx, 0);
+                    if (a.mode >= LTRG_REFINE_RHS) tma_load_2d(st + off_xl, &tmXl, &full[s], kx, 0);
+                }
             }
             // wait for the copies still in flight (complete already unless a wait above expired)
             const uint64_t issued = i;
@@ -266,29 +278,35 @@ __global__ void __launch_bounds__(kThreads, 1)
             // MMA issuer
             uint64_t i = 0;
             u32 seg = 0;
-            for (uint64_t u = lo; u < hi; ++u, ++i) {
+            bool ok = true;
+            for (uint64_t u = lo; u < hi && ok; ++u) {
                 const u32 kb = (u32) (u % a.nkb);
                 const bool first = u == lo || kb == 0 || (a.kchunk && kb % a.kchunk == 0);
                 const bool last = u + 1 == hi || kb + 1 == a.nkb || (a.kchunk && (kb + 1) % a.kchunk == 0);
                 if (first && seg > 0 && !mbar_wait(acce, (seg - 1) & 1u, a.err, kErrMma)) break;
-                const u32 s = (u32) (i % a.stages);
-                if (!mbar_wait(&full[s], (u32) (i / a.stages) & 1u, a.err, kErrMma)) break;
-                tc_fence_after();
-                const uint32_t st = saddr(base + (size_t) s * a.stage_bytes);
-                for (int k = 0; k < BK / UK; ++k) {
-                    const uint64_t bh = sdesc(st + off_xh + k * UK * 2);
-                    const uint64_t bl = sdesc(st + off_xl + k * UK * 2);
-                    for (int h = 0; h < 2; ++h) {
-                        const uint32_t d = tmem + h * 256;
-                        const uint32_t ao = h * (BM * 128) + k * UK * 2;
-                        const uint64_t ad = sdesc(st + ao);
-                        umma(d, ad, bh, a.idesc, (first && k == 0) ? 0u : 1u);
-                        if (a.mode >= LTRG_REFINE_RHS) umma(d, ad, bl, a.idesc, 1u);
-                        if (a.mode == LTRG_REFINE_FULL) umma(d, sdesc(st + off_gl + ao), bh, a.idesc, 1u);
+                for (int q = 0; q < SPU; ++q, ++i) {
+                    const u32 s = (u32) (i % a.stages);
+                    if (!mbar_wait(&full[s], (u32) (i / a.stages) & 1u, a.err, kErrMma)) {
+                        ok = false;
+                        break;
                     }
+                    tc_fence_after();
+                    const uint32_t st = saddr(base + (size_t) s * a.stage_bytes);
+                    for (int k = 0; k < KB / UK; ++k) {
+                        const uint64_t bh = sdesc<KB>(st + off_xh + k * UK * 2);
+                        const uint64_t bl = sdesc<KB>(st + off_xl + k * UK * 2);
+                        for (int h = 0; h < 2; ++h) {
+                            const uint32_t d = tmem + h * 256;
+                            const uint32_t ao = h * (BM * KB * 2) + k * UK * 2;
+                            const uint64_t ad = sdesc<KB>(st + ao);
+                            umma(d, ad, bh, a.idesc, (first && q == 0 && k == 0) ? 0u : 1u);
+                            if (a.mode >= LTRG_REFINE_RHS) umma(d, ad, bl, a.idesc, 1u);
+                            if (a.mode == LTRG_REFINE_FULL) umma(d, sdesc<KB>(st + off_gl + ao), bh, a.idesc, 1u);
+                        }
+                    }
+                    umma_commit(&empty[s]);
                 }
-                umma_commit(&empty[s]);
-                if (last) { umma_commit(accf); ++seg; }
+                if (ok && last) { umma_commit(accf); ++seg; }
             }
             umma_commit(done);
             mbar_wait(done, 0, a.err, kErrDrain);
@@ -578,21 +596,29 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 // 2-D map over `rows` rows of `ld` 16-bit elements (row stride ld * 2 bytes,
 // a multiple of 128), box of 64 elements (128 bytes) x box_rows, 128-byte
 // swizzle; rows past the end read as zero.
-CUtensorMap make_map(const void* ptr, CUtensorMapDataType dt, u32 ld, u32 rows, u32 box_rows)
+CUtensorMap make_map(const void* ptr, CUtensorMapDataType dt, u32 ld, u32 rows, u32 box_rows, u32 box_k)
 {
-    if ((reinterpret_cast<uintptr_t>(ptr) & 127) || (ld % BK) || box_rows == 0 || box_rows > 256)
+    if ((reinterpret_cast<uintptr_t>(ptr) & 127) || (ld % BK) || box_rows == 0 || box_rows > 256 ||
+        (box_k != 64 && box_k != 32))
         throw std::runtime_error("tensor map: misaligned base, row length or box");
     CUtensorMap m;
     cuuint64_t dims[2] = {ld, rows};
     cuuint64_t strides[1] = {(cuuint64_t) ld * 2};
-    cuuint32_t box[2] = {(cuuint32_t) BK, box_rows};
+    cuuint32_t box[2] = {(cuuint32_t) box_k, box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = encode_fn()(&m, dt, 2, const_cast<void*>(ptr), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                             box_k == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed with " + std::to_string((int) r));
     return m;
 }
+
+// k per pipeline stage of the tensor-core gather for a refine level. Measured
+// on GB300 (32,768 patches, R = 192): 64 for one and two products (0.388 and
+// 0.606 ms per contraction against 0.463 and 0.652 with 32); 32 for three
+// products, whose stages hold two G tiles and two X tiles (0.719 against
+// 0.738 ms; it also lets that mode take R = 256).
+u32 stage_k(int refine) { return refine == LTRG_REFINE_FULL ? 32u : 64u; }
 
 struct DevBuf {
     void* p = nullptr;
@@ -758,8 +784,9 @@ void ltrg_Gather::solve(const float* alb, const float* E, u32 R, int bounces, in
             g16_has_lo = need_lo;
         }
         const u32 BN = std::max<u32>(32, (R + 31) / 32 * 32);
-        const u32 b_bytes = BN * BK * 2;
-        const u32 stage_bytes = (need_lo ? 2 : 1) * A_BYTES + (refine >= LTRG_REFINE_RHS ? 2 : 1) * b_bytes;
+        const u32 KB = stage_k(refine);
+        const u32 b_bytes = BN * KB * 2, a_bytes = ROWS * KB * 2;
+        const u32 stage_bytes = (need_lo ? 2 : 1) * a_bytes + (refine >= LTRG_REFINE_RHS ? 2 : 1) * b_bytes;
         stages = std::min<int>(kMaxStages, (kSmemLimit - kSmemExtra) / (int) stage_bytes);
         if (stages < 2) throw std::runtime_error("tensor-core gather: stage does not fit in shared memory");
         const size_t smem = (size_t) stages * stage_bytes + kSmemExtra;
@@ -770,11 +797,12 @@ void ltrg_Gather::solve(const float* alb, const float* E, u32 R, int bounces, in
         partial.ensure((size_t) n_rp * max_slots * R * ROWS * 4);
         const CUtensorMapDataType dt =
             precision == LTRG_F_FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
-        const CUtensorMap mG = make_map(G16.p, dt, ld, n, ROWS);
-        const CUtensorMap mGl = make_map(need_lo ? G16lo.p : G16.p, dt, ld, n, ROWS);
-        const CUtensorMap mXh = make_map(xh.p, dt, ld, BN, BN);
-        const CUtensorMap mXl = make_map(xl.p, dt, ld, BN, BN);
-        GCK(cudaFuncSetAttribute(k_umma_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+        const CUtensorMap mG = make_map(G16.p, dt, ld, n, ROWS, KB);
+        const CUtensorMap mGl = make_map(need_lo ? G16lo.p : G16.p, dt, ld, n, ROWS, KB);
+        const CUtensorMap mXh = make_map(xh.p, dt, ld, BN, BN, KB);
+        const CUtensorMap mXl = make_map(xl.p, dt, ld, BN, BN, KB);
+        auto kern = KB == 64 ? k_umma_gather<64> : k_umma_gather<32>;
+        GCK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
         UmmaArgs ua;
         ua.nkb = nkb; ua.n_rp = n_rp; ua.R = R; ua.BN = BN;
         ua.stages = (u32) stages; ua.stage_bytes = stage_bytes; ua.mode = (u32) refine;
@@ -809,7 +837,7 @@ void ltrg_Gather::solve(const float* alb, const float* E, u32 R, int bounces, in
         std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ge;
         for (int b = 0; b < bounces; ++b) {
             cudaEvent_t g0 = event();
-            k_umma_gather<<<n_cta, kThreads, smem, s>>>(mG, mGl, mXh, mXl, ua); note_launch();
+            kern<<<n_cta, kThreads, smem, s>>>(mG, mGl, mXh, mXl, ua); note_launch();
             cudaEvent_t g1 = event();
             ge.push_back({g0, g1});
             GCK(cudaGetLastError());
