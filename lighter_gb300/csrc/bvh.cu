@@ -17,6 +17,7 @@
 // whole triangle, so every query still tests the original triangle.
 #include <cuda_runtime.h>
 #include <cub/cub.cuh>
+#include <cfloat>
 
 #include <cstring>
 #include <stdexcept>
@@ -149,6 +150,58 @@ __global__ void k_pack_nodes(int n_int, const int* left, const int* right, const
     o[3] = make_float4(__int_as_float(l), __int_as_float(r), 0.0f, 0.0f);
 }
 
+// ---- 4-wide nodes: the binary nodes at even depth, with their grandchildren as children
+
+// flag[i] = 1 when internal node i lies at even depth (the root at depth 0).
+__global__ void k_even_depth(int n_int, const int* __restrict__ parent_int, int* __restrict__ flag)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n_int) return;
+    if (i == n_int) { flag[i] = 0; return; }
+    int d = 0;
+    for (int p = parent_int[i]; p >= 0 && d < 4096; p = parent_int[p]) ++d;
+    flag[i] = (d & 1) == 0;
+}
+
+__device__ __forceinline__ void put_slot(float4* o, int k, const float* box, int child)
+{
+    reinterpret_cast<float*>(&o[0])[k] = box[0];
+    reinterpret_cast<float*>(&o[1])[k] = box[3];
+    reinterpret_cast<float*>(&o[2])[k] = box[1];
+    reinterpret_cast<float*>(&o[3])[k] = box[4];
+    reinterpret_cast<float*>(&o[4])[k] = box[2];
+    reinterpret_cast<float*>(&o[5])[k] = box[5];
+    reinterpret_cast<int*>(&o[6])[k] = child;
+}
+
+// Node layout in bvh.cuh (8 float4). Child boxes are the binary tree's, which
+// are already inflated; a grandchild that is internal is referenced by its
+// 4-wide index (it lies at even depth too), a leaf by ~leaf.
+__global__ void k_pack4(int n_int, const int* __restrict__ flag, const int* __restrict__ idx4, const int* __restrict__ left,
+                        const int* __restrict__ right, const float* __restrict__ leaf_box, const float* __restrict__ int_box,
+                        float4* __restrict__ nodes4)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_int || !flag[i]) return;
+    float4* o = nodes4 + 8 * (size_t) idx4[i];
+    const float empty_box[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+    int k = 0;
+    const int kids[2] = {left[i], right[i]};
+    for (int c : kids) {
+        if (c < 0) {
+            put_slot(o, k++, leaf_box + 6 * (size_t) (~c), c);
+        } else {
+            const int gk[2] = {left[c], right[c]};
+            for (int g : gk) {
+                const float* box = g < 0 ? leaf_box + 6 * (size_t) (~g) : int_box + 6 * (size_t) g;
+                put_slot(o, k++, box, g < 0 ? g : idx4[g]);
+            }
+        }
+    }
+    for (; k < 4; ++k) put_slot(o, k, empty_box, kNoChild);
+    o[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
 __global__ void k_pack_tris(int n, const u32* ids, const u32* ref_tri, const float* xyz, const u32* meta, const u32* local,
                             float4* tris)
 {
@@ -255,6 +308,25 @@ void bvh_build(const BvhBuildInput& in, BvhStorage& out, void* stream)
         k_pack_nodes<<<(n_int + B - 1) / B, B, 0, st>>>(n_int, left, right, leaf_box, int_box, out.nodes); note_launch();
         BVH_CHECK(cudaGetLastError());
     }
+    // 4-wide nodes (at most one per binary node)
+    out.nodes4 = alloc<float4>(8 * (size_t) (n_int > 0 ? n_int : 1), st, out.bytes);
+    out.root4 = n_int > 0 ? 0 : ~0;   // Karras' root is binary node 0, at depth 0: 4-wide node 0
+    if (n_int > 0) {
+        int* flag = alloc<int>(n_int + 1, st, scratch_bytes);
+        int* idx4 = alloc<int>(n_int + 1, st, scratch_bytes);
+        k_even_depth<<<(n_int + 1 + B - 1) / B, B, 0, st>>>(n_int, parent_int, flag); note_launch();
+        BVH_CHECK(cudaGetLastError());
+        size_t tb4 = 0;
+        BVH_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, tb4, flag, idx4, n_int + 1, st));
+        void* t4 = alloc<char>(tb4, st, scratch_bytes);
+        BVH_CHECK(cub::DeviceScan::ExclusiveSum(t4, tb4, flag, idx4, n_int + 1, st));
+        k_pack4<<<(n_int + B - 1) / B, B, 0, st>>>(n_int, flag, idx4, left, right, leaf_box, int_box, out.nodes4);
+        note_launch();
+        BVH_CHECK(cudaGetLastError());
+        BVH_CHECK(cudaFreeAsync(flag, st));
+        BVH_CHECK(cudaFreeAsync(idx4, st));
+        BVH_CHECK(cudaFreeAsync(t4, st));
+    }
     k_pack_tris<<<(n + B - 1) / B, B, 0, st>>>(n, ids2, in.ref_tri, in.tri_xyz, in.tri_meta, in.tri_local,
                                                 out.tris); note_launch();
     BVH_CHECK(cudaGetLastError());
@@ -308,6 +380,8 @@ void bvh_free(BvhStorage& s, void* stream)
 {
     cudaStream_t st = (cudaStream_t) stream;
     if (s.nodes) cudaFreeAsync(s.nodes, st);
+    if (s.nodes4) cudaFreeAsync(s.nodes4, st);
+    s.nodes4 = nullptr;
     if (s.tris) cudaFreeAsync(s.tris, st);
     if (s.srec) cudaFreeAsync(s.srec, st);
     if (s.drec) cudaFreeAsync(s.drec, st);

@@ -98,7 +98,7 @@ __global__ void k_ff_pretest(u32 n, const float4* __restrict__ pos, const float4
 }
 
 // counts[1]: links kept
-template <class T>
+template <class T, bool kWide>
 __global__ void k_ff_visibility(u32 n, const float4* __restrict__ pos, BvhView bvh, ErrFlag err, int links,
                                 T* __restrict__ F, const PairRef* __restrict__ cand, unsigned long long n_cand,
                                 unsigned long long* next, unsigned long long* counts)
@@ -115,7 +115,7 @@ __global__ void k_ff_visibility(u32 n, const float4* __restrict__ pos, BvhView b
             const PairRef pr = cand[k];
             V3 AP = ld3(pos[pr.i]), BP = ld3(pos[pr.j]);
             V3 dn = normalized(BP - AP);
-            bool occluded = bvh_any_hit(bvh, AP + dn * kSmall, BP - dn * kSmall, err);
+            bool occluded = bvh_any_hit<kWide>(bvh, AP + dn * kSmall, BP - dn * kSmall, err);
             bool keep = links == 0 ? occluded : !occluded;
             if (keep) {
                 ++kept;
@@ -211,7 +211,11 @@ RadFormFactors build_ff(u32 n, const float4* pos, const float4* nrm, const BvhVi
         RCK(cudaGetDevice(&dev));
         RCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) sms * 8, (n_cand + 127) / 128);
-        k_ff_visibility<T><<<grid, 128, 0, st>>>(n, pos, bvh, err, links, F, cand, n_cand, counts + 2, counts);
+        // the 4-wide walk for trees of 256k references and more (see walk_segment4)
+        if (bvh.n_tris >= (1 << 18))
+            k_ff_visibility<T, true><<<grid, 128, 0, st>>>(n, pos, bvh, err, links, F, cand, n_cand, counts + 2, counts);
+        else
+            k_ff_visibility<T, false><<<grid, 128, 0, st>>>(n, pos, bvh, err, links, F, cand, n_cand, counts + 2, counts);
         note_launch();
         RCK(cudaGetLastError());
     }
