@@ -222,6 +222,39 @@ def run_ours(args, world, rank, local, dist):
     return rays, dev_ms, wall, stats, clocks, stats[-1]["bytes_h2d"], stats[-1]["bytes_d2h"], launches, tuning
 
 
+# bake radiosity precisions: (name, LTRG_F_*, refine_steps)
+RAD_MODES = (("fp32", 0, 0), ("fp16", 1, 0), ("fp16_refine1", 1, 1), ("bf16", 2, 0), ("bf16_refine1", 2, 1))
+
+
+def run_rad_precisions(args, lib, desc, gpu_opts, bounces):
+    """One bake of the scene per form-factor precision (after one warm-up bake):
+    seconds per radiosity bounce and the largest lightmap difference from the FP32
+    bake, relative to each lightmap's peak."""
+    import numpy as np
+    from lighter_gb300.ext import get_stats
+    from lighter_gb300.scene import _collect, ingest
+    out, base = {}, None
+    for name, prec, refine in RAD_MODES:
+        scene, keep = ingest(lib, desc, gpu_options=dict(gpu_opts, radiosity_precision=prec, refine_steps=refine))
+        try:
+            _bake_once(lib, scene)
+            _bake_once(lib, scene)
+            st = get_stats(lib, scene)
+            lms = [x[3] for x in _collect(lib, scene, False, [], 0.0, "finished").lightmaps]
+        finally:
+            lib.ltr_DestroyScene(scene)
+            del keep
+        if base is None:
+            base = lms
+        err = max(float(np.abs(a - b).max()) / max(float(np.abs(b).max()), 1e-12) for a, b in zip(lms, base))
+        n = st["rad_elements"]
+        f_bytes = n * ((n + 7) // 8 * 8) * (4 if prec == 0 else 2)   # F rows padded to 8 entries
+        spb = st["ms_rad_bounce"] / bounces / 1000.0
+        out[name] = {"s_per_bounce": spb, "ms_rad_links": st["ms_rad_links"], "max_rel_err_vs_fp32": err,
+                     "elements": n, "f_bytes": f_bytes, "f_gbs": f_bytes / spb / 1e9 if spb > 0 else 0.0}
+    return out
+
+
 GATHER_WORKLOAD = ("multi-RHS radiosity: seeded room with furniture, {n} patches, {t} triangles, "
                    "{c} light configurations (R = {r} RGB right-hand sides), {b} bounces")
 # (name, precision, refine, TMEM accumulation length in k blocks)
@@ -403,6 +436,8 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-rad-precisions", action="store_true",
+                    help="skip the per-precision bakes (FP32 / FP16 / BF16 form factors, with and without refinement)")
     ap.add_argument("--no-bake", action="store_true",
                     help="gather only (profiling of the gather kernels on a smaller patch set)")
     args = ap.parse_args()
@@ -468,6 +503,11 @@ def main():
                                                     "ms_rad_bounce", "ms_ao", "ms_finalize", "ms_download",
                                                     "ms_device", "ms_total")},
     }
+    if not args.no_rad_precisions:
+        from lighter_gb300 import library, scenes
+        desc = scenes.large(seed=1, lm=args.lm) if args.scene == "large" else scenes.mid(seed=1, lm=args.lm)
+        line["bake_radiosity_precisions"] = run_rad_precisions(
+            args, library(), desc, {"device": local, "radiosity_patches": args.patches, "radiosity_links": 1}, bounces)
     if not args.no_batch:
         line["batch"] = run_batch(args, 0)
     if not args.no_gather:

@@ -31,7 +31,9 @@ typedef struct ltrg_Options {
     int keep_samples;         /* keep per-sample arrays for ltrdbg_* after the bake, default 0 */
     int radiosity_links;      /* LTRG_LINKS_*, default LTRG_LINKS_REFERENCE */
     int radiosity_precision;  /* LTRG_F_*, default LTRG_F_FP32 */
-    int refine_steps;         /* FP32 residual-refinement sweeps for FP16/BF16 F, default 1 */
+    int refine_steps;         /* FP16/BF16 F: the last refine_steps bounces use F only as the link
+                                 mask and recompute each factor in FP32 (the FP32 result of those
+                                 bounces, bit for bit); default 1, 0..16 */
     uint32_t radiosity_patches; /* 0: one radiosity element per sample (reference, lighter.cpp:673-719);
                                    N > 0: group samples into about N patches by (instance, lightmap
                                    tile, dominant normal axis); each texel then receives its patch's

@@ -546,11 +546,12 @@ __global__ void k_table_samples(u32 n, const float4* __restrict__ srad, const u3
 }
 
 // Patch slot of a sample: (instance, lightmap tile, dominant axis of its
-// unit normal); marks the slot occupied.
+// unit normal); marks the slot occupied. With n_occ set, counts the occupied
+// slots instead (a trial of a tile size).
 __global__ void k_patch_slots(u32 n, const float4* __restrict__ snrm, const u32* __restrict__ sloc,
                               const u32* __restrict__ sinst, const u32* __restrict__ inst_w,
                               const u32* __restrict__ slot_base, const u32* __restrict__ ntx, u32 tile,
-                              u32* __restrict__ slot_of, u32* __restrict__ occ)
+                              u32* __restrict__ slot_of, u32* __restrict__ occ, u32* __restrict__ n_occ)
 {
     u32 s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
@@ -562,6 +563,10 @@ __global__ void k_patch_slots(u32 n, const float4* __restrict__ snrm, const u32*
     float ax = fabsf(nn.x), ay = fabsf(nn.y), az = fabsf(nn.z);
     u32 axis = (ax >= ay && ax >= az) ? (nn.x >= 0 ? 0 : 1) : (ay >= az ? (nn.y >= 0 ? 2 : 3) : (nn.z >= 0 ? 4 : 5));
     u32 slot = slot_base[inst] + (ty * ntx[inst] + tx) * 6 + axis;
+    if (n_occ) {
+        if (occ[slot] == 0 && atomicExch(&occ[slot], 1u) == 0) atomicAdd(n_occ, 1u);
+        return;
+    }
     slot_of[s] = slot;
     occ[slot] = 1;
 }
@@ -2183,24 +2188,61 @@ void run_bake(ltr_Scene* S)
             // Patch mode: group samples by (instance, lightmap tile, dominant
             // normal axis) on the device. Patches are numbered in slot order;
             // each patch's samples are listed in sample order (stable sort).
+            // The tile side (texels) is chosen so the patch count comes closest to
+            // the requested one: the first guess sqrt(covered texels / target)
+            // ignores partly covered tiles and the split by normal axis, so a
+            // few trials count the occupied slots of neighbouring sides.
             u32 target = S->opt.radiosity_patches;
-            double per = std::max(1.0, (double) n_cov / (double) target);
-            u32 tile = (u32) std::max(1.0, std::floor(std::sqrt(per) + 0.5));
             std::vector<u32> slot_base(n_inst + 1, 0), ntx(n_inst, 0);
-            for (int i = 0; i < n_inst; ++i) {
-                HostInst* mi = S->insts[i];
-                ntx[i] = mi->container ? 0 : (mi->w + tile - 1) / tile;
-                u32 nslots = mi->container ? 0 : ntx[i] * ((mi->h + tile - 1) / tile) * 6;
-                slot_base[i + 1] = slot_base[i] + nslots;
+            auto layout = [&](u32 t) {
+                for (int i = 0; i < n_inst; ++i) {
+                    HostInst* mi = S->insts[i];
+                    ntx[i] = mi->container ? 0 : (mi->w + t - 1) / t;
+                    u32 ns = mi->container ? 0 : ntx[i] * ((mi->h + t - 1) / t) * 6;
+                    slot_base[i + 1] = slot_base[i] + ns;
+                }
+                return slot_base[n_inst];
+            };
+            u32* d_slot_of = A.alloc<u32>(n_samples);
+            u32* d_count = A.alloc<u32>(1);
+            auto trial = [&](u32 t) -> u32 {
+                const u32 ns = layout(t);
+                u32* d_sb = A.upload(slot_base);
+                u32* d_nt = A.upload(ntx);
+                u32* d_o = A.zeros<u32>(ns + 1);
+                CK(cudaMemsetAsync(d_count, 0, sizeof(u32), st));
+                k_patch_slots<<<(n_samples + kThreads - 1) / kThreads, kThreads, 0, st>>>(
+                    n_samples, d_snrm, d_sloc, d_sinst, d_inst_w, d_sb, d_nt, t, d_slot_of, d_o, d_count); note_launch();
+                CK(cudaGetLastError());
+                u32 c = 0;
+                CK(cudaMemcpyAsync(&c, d_count, sizeof(u32), cudaMemcpyDeviceToHost, st)); note_d2h(4);
+                CK(cudaStreamSynchronize(st));
+                return c;
+            };
+            u32 tile = (u32) std::max(1.0, std::floor(std::sqrt(std::max(1.0, (double) n_cov / target)) + 0.5));
+            {
+                auto off = [&](u32 c) { return std::fabs(std::log(std::max(1.0, (double) c) / target)); };
+                u32 c = trial(tile), best = tile;
+                double best_off = off(c);
+                const int dir = c > target ? 1 : -1;
+                for (int k = 0; k < 8; ++k) {
+                    if ((dir > 0 && c <= target) || (dir < 0 && (c >= target || tile == 1))) break;
+                    // next side from the area scaling, at least one texel on
+                    u32 t2 = (u32) std::floor(tile * std::sqrt((double) c / target) + 0.5);
+                    t2 = dir > 0 ? std::max(t2, tile + 1) : std::max(1u, std::min(t2, tile - 1));
+                    tile = t2;
+                    c = trial(tile);
+                    if (off(c) < best_off) { best_off = off(c); best = tile; }
+                }
+                tile = best;
             }
-            const u32 nslots = slot_base[n_inst];
+            const u32 nslots = layout(tile);
             u32* d_slot_base = A.upload(slot_base);
             u32* d_ntx = A.upload(ntx);
-            u32* d_slot_of = A.alloc<u32>(n_samples);
             u32* d_occ = A.zeros<u32>(nslots + 1);
             u32* d_slot_scan = A.alloc<u32>(nslots + 1);
             k_patch_slots<<<(n_samples + kThreads - 1) / kThreads, kThreads, 0, st>>>(
-                n_samples, d_snrm, d_sloc, d_sinst, d_inst_w, d_slot_base, d_ntx, tile, d_slot_of, d_occ); note_launch();
+                n_samples, d_snrm, d_sloc, d_sinst, d_inst_w, d_slot_base, d_ntx, tile, d_slot_of, d_occ, nullptr); note_launch();
             CK(cudaGetLastError());
             {
                 size_t tb = 0;

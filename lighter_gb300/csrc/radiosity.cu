@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 
 #include "radiosity.cuh"
 
@@ -58,8 +59,9 @@ __device__ __forceinline__ float pair_pretest(V3 AP, V3 AN, V3 BP, V3 BN)
 // counts[0]: pairs that passed (appended; entries past `cap` are dropped and
 // the host runs the pass again with room for all of them)
 template <class T>
-__global__ void k_ff_pretest(u32 n, const float4* __restrict__ pos, const float4* __restrict__ nrm, T* __restrict__ F,
-                             PairRef* __restrict__ cand, unsigned long long cap, unsigned long long* counts)
+__global__ void k_ff_pretest(u32 n, size_t ld, const float4* __restrict__ pos, const float4* __restrict__ nrm,
+                             T* __restrict__ F, PairRef* __restrict__ cand, unsigned long long cap,
+                             unsigned long long* counts)
 {
     __shared__ float tile[32][33];
     const u32 bi = blockIdx.y, bj = blockIdx.x;
@@ -83,23 +85,24 @@ __global__ void k_ff_pretest(u32 n, const float4* __restrict__ pos, const float4
         }
     }
     __syncthreads();
+    // columns n .. ld-1 (row padding, ld <= 32 * tiles) receive zeros
     for (int k = 0; k < 4; ++k) {
         int r = ty + 8 * k;
         if (bi == bj) {
             u32 i = bi * 32 + r, j = bj * 32 + tx;
-            if (i < n && j < n) F[(size_t) i * n + j] = to_store<T>(tile[r][tx] + tile[tx][r]);
+            if (i < n && j < ld) F[(size_t) i * ld + j] = to_store<T>(tile[r][tx] + tile[tx][r]);
         } else {
             u32 i = bi * 32 + r, j = bj * 32 + tx;
-            if (i < n && j < n) F[(size_t) i * n + j] = to_store<T>(tile[r][tx]);
+            if (i < n && j < ld) F[(size_t) i * ld + j] = to_store<T>(tile[r][tx]);
             u32 i2 = bj * 32 + r, j2 = bi * 32 + tx;
-            if (i2 < n && j2 < n) F[(size_t) i2 * n + j2] = to_store<T>(tile[tx][r]);
+            if (i2 < n && j2 < ld) F[(size_t) i2 * ld + j2] = to_store<T>(tile[tx][r]);
         }
     }
 }
 
 // counts[1]: links kept
 template <class T, bool kWide>
-__global__ void k_ff_visibility(u32 n, const float4* __restrict__ pos, BvhView bvh, ErrFlag err, int links,
+__global__ void k_ff_visibility(size_t ld, const float4* __restrict__ pos, BvhView bvh, ErrFlag err, int links,
                                 T* __restrict__ F, const PairRef* __restrict__ cand, unsigned long long n_cand,
                                 unsigned long long* next, unsigned long long* counts)
 {
@@ -120,8 +123,8 @@ __global__ void k_ff_visibility(u32 n, const float4* __restrict__ pos, BvhView b
             if (keep) {
                 ++kept;
             } else {
-                F[(size_t) pr.i * n + pr.j] = to_store<T>(0.0f);
-                F[(size_t) pr.j * n + pr.i] = to_store<T>(0.0f);
+                F[(size_t) pr.i * ld + pr.j] = to_store<T>(0.0f);
+                F[(size_t) pr.j * ld + pr.i] = to_store<T>(0.0f);
             }
         }
     }
@@ -139,28 +142,120 @@ __global__ void k_rad_x(u32 n, const float4* __restrict__ out, const float4* __r
     X[j] = st4(x, 0.0f);
 }
 
-// Y = F X, one warp per row; F streamed once per bounce (HBM-bound).
-template <class T>
-__global__ void k_rad_gemv(u32 n, const T* __restrict__ F, const float4* __restrict__ X, float4* __restrict__ Y)
+// One vector load of V entries of F (16 or 8 bytes), and its entries as floats.
+template <int B> struct RawF;
+template <> struct RawF<16> {
+    uint4 u;
+    __device__ __forceinline__ void load(const void* p) { u = __ldcs(reinterpret_cast<const uint4*>(p)); }
+};
+template <> struct RawF<8> {
+    uint2 u;
+    __device__ __forceinline__ void load(const void* p) { u = __ldcs(reinterpret_cast<const uint2*>(p)); }
+};
+template <class T, int V> __device__ __forceinline__ void unpack(const void* raw, float* v)
 {
-    const int lane = threadIdx.x & 31;
-    u32 row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (row >= n) return;
-    const T* fr = F + (size_t) row * n;
-    float ax = 0, ay = 0, az = 0;
-    for (u32 j = lane; j < n; j += 32) {
-        float f = to_f(fr[j]);
-        if (f != 0.0f) {
-            float4 x = __ldg(&X[j]);
-            ax += x.x * f; ay += x.y * f; az += x.z * f;
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int k = 0; k < V; ++k) v[k] = reinterpret_cast<const float*>(raw)[k];
+    } else {
+#pragma unroll
+        for (int k = 0; k < V / 2; ++k) {
+            float2 f;
+            if constexpr (std::is_same<T, __half>::value) f = __half22float2(reinterpret_cast<const __half2*>(raw)[k]);
+            else f = __bfloat1622float2(reinterpret_cast<const __nv_bfloat162*>(raw)[k]);
+            v[2 * k] = f.x; v[2 * k + 1] = f.y;
         }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        ax += __shfl_down_sync(0xffffffffu, ax, o);
-        ay += __shfl_down_sync(0xffffffffu, ay, o);
-        az += __shfl_down_sync(0xffffffffu, az, o);
+}
+
+constexpr int kRadRows = 4;   // rows of F per warp in the bounce product
+
+// Y = F X (one bounce's gather). F is streamed once per bounce, so the kernel is
+// HBM-bound: a warp takes kRadRows rows and reads them V entries per lane per
+// row (16 bytes; the next step's loads issued before this step's arithmetic),
+// and each X_j it loads serves all its rows. A zero entry (no link) skips its X
+// load. Rows are ld entries apart, ld a multiple of 8 with zeros past n, so
+// every row starts on a 16-byte boundary.
+// kExact: F serves only as the link mask and the factor of every linked pair is
+// recomputed in FP32 with pair_pretest, lower index first as k_ff_pretest
+// computes it, i.e. bit-for-bit the value an FP32 F holds. A linked factor is
+// >= SMALL_FLOAT, which neither FP16 nor BF16 rounds to 0, so a 16-bit mask is
+// the FP32 one. kExact reads 4 entries per lane (8-byte loads of a 16-bit F),
+// the FP32 kernel's split of columns over lanes, so both sum in the same order:
+// the kExact product of a 16-bit F is the FP32 product.
+template <class T, bool kExact>
+__global__ void __launch_bounds__(256) k_rad_gemv(u32 n, size_t ld, const T* __restrict__ F,
+                                                  const float4* __restrict__ pos, const float4* __restrict__ nrm,
+                                                  const float4* __restrict__ X, float4* __restrict__ Y)
+{
+    constexpr int V = kExact ? 4 : 16 / (int) sizeof(T);
+    using Raw = RawF<V * sizeof(T)>;
+    const int lane = threadIdx.x & 31;
+    const u32 r0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kRadRows;
+    if (r0 >= n) return;
+    const T* rows[kRadRows];
+    V3 ap[kRadRows], an[kRadRows];
+    u32 ri[kRadRows];
+#pragma unroll
+    for (int r = 0; r < kRadRows; ++r) {
+        ri[r] = min(r0 + r, n - 1);   // rows past n repeat the last row and are not written
+        rows[r] = F + (size_t) ri[r] * ld;
+        if (kExact) { ap[r] = ld3(pos[ri[r]]); an[r] = ld3(nrm[ri[r]]); }
     }
-    if (lane == 0) Y[row] = make_float4(ax, ay, az, 0.0f);
+    float acc[kRadRows][3];
+#pragma unroll
+    for (int r = 0; r < kRadRows; ++r) acc[r][0] = acc[r][1] = acc[r][2] = 0.0f;
+    const u32 nv = (u32) (ld / V);
+    Raw cur[kRadRows];
+    u32 c = lane;
+    if (c < nv) {
+#pragma unroll
+        for (int r = 0; r < kRadRows; ++r) cur[r].load(rows[r] + (size_t) c * V);
+    }
+    while (c < nv) {
+        const u32 cn = c + 32;
+        Raw nxt[kRadRows];
+        if (cn < nv) {
+#pragma unroll
+            for (int r = 0; r < kRadRows; ++r) nxt[r].load(rows[r] + (size_t) cn * V);
+        }
+        float f[kRadRows][V];
+#pragma unroll
+        for (int r = 0; r < kRadRows; ++r) unpack<T, V>(&cur[r].u, f[r]);
+#pragma unroll
+        for (int k = 0; k < V; ++k) {
+            bool any = false;
+#pragma unroll
+            for (int r = 0; r < kRadRows; ++r) any |= f[r][k] != 0.0f;
+            if (any) {
+                const u32 j = c * V + k;
+                const float4 x = __ldg(&X[j]);
+                V3 bp, bn;
+                if (kExact) { bp = ld3(pos[j]); bn = ld3(nrm[j]); }
+#pragma unroll
+                for (int r = 0; r < kRadRows; ++r) {
+                    if (f[r][k] != 0.0f) {
+                        float fv = f[r][k];
+                        if (kExact) fv = ri[r] < j ? pair_pretest(ap[r], an[r], bp, bn) : pair_pretest(bp, bn, ap[r], an[r]);
+                        acc[r][0] += x.x * fv; acc[r][1] += x.y * fv; acc[r][2] += x.z * fv;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < kRadRows; ++r) cur[r] = nxt[r];
+        c = cn;
+    }
+#pragma unroll
+    for (int r = 0; r < kRadRows; ++r)
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+            for (int o = 16; o > 0; o >>= 1) acc[r][q] += __shfl_down_sync(0xffffffffu, acc[r][q], o);
+    if (lane == 0) {
+#pragma unroll
+        for (int r = 0; r < kRadRows; ++r)
+            if (r0 + r < n) Y[r0 + r] = make_float4(acc[r][0], acc[r][1], acc[r][2], 0.0f);
+    }
 }
 
 // total += Y, out = Y (lighter.cpp:784-796).
@@ -176,13 +271,14 @@ __global__ void k_rad_update(u32 n, const float4* __restrict__ Y, float4* __rest
 // Both passes on `st`; returns the link and visibility-ray counts (synchronises
 // the stream once after the first pass, to size the pair list).
 template <class T>
-RadFormFactors build_ff(u32 n, const float4* pos, const float4* nrm, const BvhView& bvh, ErrFlag err, int links, T* F,
-                        cudaStream_t st)
+RadFormFactors build_ff(u32 n, size_t ld, const float4* pos, const float4* nrm, const BvhView& bvh, ErrFlag err,
+                        int links, T* F, cudaStream_t st)
 {
     RadFormFactors out;
     if (n == 0) return out;
     const u32 nb = (n + 31) / 32;
     if (nb > 65535) throw std::runtime_error("radiosity: too many elements for the tile grid");
+    if (ld < n || ld > (size_t) nb * 32) throw std::runtime_error("radiosity: bad leading dimension");
     const unsigned long long pairs = (unsigned long long) n * (n - 1) / 2;
     unsigned long long cap = std::min<unsigned long long>(pairs, std::max<unsigned long long>(1ull << 24, pairs / 16));
     unsigned long long* counts = nullptr;   // [0] pairs that passed, [1] links kept, [2] work counter
@@ -196,7 +292,7 @@ RadFormFactors build_ff(u32 n, const float4* pos, const float4* nrm, const BvhVi
     for (int attempt = 0; attempt < 2; ++attempt) {
         RCK(cudaMallocAsync(&cand, std::max<unsigned long long>(cap, 1) * sizeof(PairRef), st));
         RCK(cudaMemsetAsync(counts, 0, 3 * sizeof(unsigned long long), st));
-        k_ff_pretest<T><<<dim3(nb, nb), dim3(32, 8), 0, st>>>(n, pos, nrm, F, cand, cap, counts); note_launch();
+        k_ff_pretest<T><<<dim3(nb, nb), dim3(32, 8), 0, st>>>(n, ld, pos, nrm, F, cand, cap, counts); note_launch();
         RCK(cudaGetLastError());
         RCK(cudaMemcpyAsync(&n_cand, counts, sizeof(n_cand), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(n_cand));
         RCK(cudaStreamSynchronize(st));
@@ -213,9 +309,9 @@ RadFormFactors build_ff(u32 n, const float4* pos, const float4* nrm, const BvhVi
         unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) sms * 8, (n_cand + 127) / 128);
         // the 4-wide walk for trees of 256k references and more (see walk_segment4)
         if (bvh.n_tris >= (1 << 18))
-            k_ff_visibility<T, true><<<grid, 128, 0, st>>>(n, pos, bvh, err, links, F, cand, n_cand, counts + 2, counts);
+            k_ff_visibility<T, true><<<grid, 128, 0, st>>>(ld, pos, bvh, err, links, F, cand, n_cand, counts + 2, counts);
         else
-            k_ff_visibility<T, false><<<grid, 128, 0, st>>>(n, pos, bvh, err, links, F, cand, n_cand, counts + 2, counts);
+            k_ff_visibility<T, false><<<grid, 128, 0, st>>>(ld, pos, bvh, err, links, F, cand, n_cand, counts + 2, counts);
         note_launch();
         RCK(cudaGetLastError());
     }
@@ -235,7 +331,8 @@ RadResult solve_t(const RadDevInputs& in, const RadSettings& rs, const BvhView& 
     const u32 n = in.n;
     size_t free_b = 0, total_b = 0;
     RCK(cudaMemGetInfo(&free_b, &total_b));
-    size_t fbytes = (size_t) n * n * sizeof(T);
+    const size_t ld = ((size_t) n + 7) / 8 * 8;   // rows on 16-byte boundaries
+    size_t fbytes = (size_t) n * ld * sizeof(T);
     if (fbytes > free_b / 10 * 9)
         throw std::runtime_error("radiosity: dense form factors for " + std::to_string(n) + " elements need " +
                                  std::to_string(fbytes >> 20) + " MiB, more than the free device memory");
@@ -256,12 +353,19 @@ RadResult solve_t(const RadDevInputs& in, const RadSettings& rs, const BvhView& 
     cudaEvent_t e0, e1, e2;
     RCK(cudaEventCreate(&e0)); RCK(cudaEventCreate(&e1)); RCK(cudaEventCreate(&e2));
     RCK(cudaEventRecord(e0, st));
-    RadFormFactors ff = build_ff<T>(n, in.pos, in.nrm, bvh, err, rs.links, F, st);
+    RadFormFactors ff = build_ff<T>(n, ld, in.pos, in.nrm, bvh, err, rs.links, F, st);
     RCK(cudaEventRecord(e1, st));
     for (int b = 0; b < rs.bounces; ++b) {
         if (abort_flag && abort_flag->load()) break;
         k_rad_x<<<(n + 255) / 256, 256, 0, st>>>(n, out, in.diff_area, X); note_launch();
-        k_rad_gemv<T><<<(unsigned) (((size_t) n * 32 + 255) / 256), 256, 0, st>>>(n, F, X, Y); note_launch();
+        // the last refine_steps bounces of a 16-bit F recompute the factors in FP32
+        const bool exact = sizeof(T) < 4 && b >= rs.bounces - rs.refine_steps;
+        const unsigned grid = (unsigned) ((((size_t) n + kRadRows - 1) / kRadRows * 32 + 255) / 256);
+        if (exact)
+            k_rad_gemv<T, true><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, X, Y);
+        else
+            k_rad_gemv<T, false><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, X, Y);
+        note_launch();
         k_rad_update<<<(n + 255) / 256, 256, 0, st>>>(n, Y, total, out); note_launch();
         RCK(cudaGetLastError());
     }
@@ -293,7 +397,7 @@ RadResult radiosity_solve_dev(const RadDevInputs& in, const RadSettings& rs, con
 RadFormFactors radiosity_form_factors_f32(uint32_t n, const float4* pos, const float4* nrm, const BvhView& bvh,
                                           ErrFlag err, int links, float* F, cudaStream_t st)
 {
-    return build_ff<float>(n, pos, nrm, bvh, err, links, F, st);
+    return build_ff<float>(n, n, pos, nrm, bvh, err, links, F, st);
 }
 
 RadResult radiosity_solve(const RadInputs& in, const RadSettings& rs, const BvhView& bvh, ErrFlag err, cudaStream_t st,

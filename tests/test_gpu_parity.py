@@ -142,9 +142,24 @@ def test_patch_radiosity_runs_and_adds_light(gpu):
     with_rad = bake(gpu, d, stats=st, gpu_options={"radiosity_patches": 256, "radiosity_links": 1})
     d0 = scenes.cornell(2, lm=32, bounces=0, ao=False)
     no_rad = bake(gpu, d0)
-    assert 0 < st["rad_elements"] <= 2 * 256 + 64
+    assert 128 <= st["rad_elements"] <= 512   # the tile side is picked for the count closest to 256
     gain = sum(float(x[3].sum()) for x in with_rad.lightmaps) - sum(float(x[3].sum()) for x in no_rad.lightmaps)
     assert gain > 0
+
+
+@pytest.mark.parametrize("precision,tol", [(1, 1e-3), (2, 4e-3)])
+def test_half_precision_form_factors_and_refinement(gpu, precision, tol):
+    # 16-bit F: with refine_steps = bounces every bounce recomputes its factors in FP32 (F is
+    # only the link mask), which is the FP32 bake bit for bit; without refinement the
+    # lightmaps stay within `tol` of the peak (FP16 rounds a factor by <= 2^-11, BF16 2^-8)
+    d = scenes.cornell(3, lm=32, bounces=2, ao=False)
+    f32 = bake(gpu, d, gpu_options={"radiosity_precision": 0})
+    refined = bake(gpu, d, gpu_options={"radiosity_precision": precision, "refine_steps": 2})
+    raw = bake(gpu, d, gpu_options={"radiosity_precision": precision, "refine_steps": 0})
+    for a, b, c in zip(f32.lightmaps, refined.lightmaps, raw.lightmaps):
+        np.testing.assert_array_equal(a[3], b[3])
+        peak = float(np.abs(a[3]).max())
+        assert float(np.abs(c[3] - a[3]).max()) <= tol * peak
 
 
 def test_invalid_option_rejected_and_error_reported(gpu):
