@@ -234,6 +234,16 @@ LTRAPI u32 ltrdbg_RadLinkCount(ltr_Scene* scene);
  * was not traced), ao receives n x ao_num_samples AO closest-hit fractions (2
  * for a miss); either may be NULL. Returns 0 when the bake recorded none. */
 LTRAPI LTRBOOL ltrdbg_GetRayData(ltr_Scene* scene, u32 inst, float* vis, float* ao);
+/* The radiosity elements of the last bake (keep_samples = 1): *n receives
+ * their count (samples, or patches in patch mode); each non-NULL array
+ * receives n float4: position, unit normal, (diffuse rgb, area), emitted rgb
+ * (the light the bounces start from) and the radiosity total (sum over
+ * m <= bounces of K^m E); F, when not NULL, receives the form factors as
+ * n x n floats (the stored FP32/FP16/BF16 values, widened; kept for
+ * n <= 24576). Returns 0 when the bake ran no radiosity or F was asked for
+ * and not kept. */
+LTRAPI LTRBOOL ltrdbg_GetRadiosity(ltr_Scene* scene, u32* n, float* pos4, float* nrm4, float* diff_area4, float* emit4,
+                                   float* total4, float* F);
 /* n values of (float) rand() / RAND_MAX exactly as n rand() calls would give
  * them, leaving the C library's generator where those calls would (the AO
  * stage's bulk draw, exposed for testing). */

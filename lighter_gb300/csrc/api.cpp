@@ -32,6 +32,7 @@ void ltr_Scene::clear_outputs()
 {
     outputs.clear();   // the buffers live in `pinned`, which the next bake reuses
     dump.clear();
+    rad_dump = lg::RadDump();
 }
 
 ltr_Scene::~ltr_Scene()
@@ -461,6 +462,21 @@ LTRAPI LTRBOOL ltrdbg_GetSamples(ltr_Scene* s, u32 inst, float* pos3, float* nrm
 }
 
 LTRAPI u32 ltrdbg_RadLinkCount(ltr_Scene* s) { return s->rad_links; }
+
+LTRAPI LTRBOOL ltrdbg_GetRadiosity(ltr_Scene* scene, u32* n, float* pos4, float* nrm4, float* diff_area4, float* emit4,
+                                   float* total4, float* F)
+{
+    if (scene->running.load()) return 0;
+    const lg::RadDump& d = scene->rad_dump;
+    if (n) *n = d.n;
+    if (!d.n || d.total.size() != 4 * (size_t) d.n || (F && d.F.empty())) return 0;
+    const std::vector<float>* src[5] = {&d.pos, &d.nrm, &d.diff_area, &d.emit, &d.total};
+    float* dst[5] = {pos4, nrm4, diff_area4, emit4, total4};
+    for (int k = 0; k < 5; ++k)
+        if (dst[k]) memcpy(dst[k], src[k]->data(), src[k]->size() * sizeof(float));
+    if (F) memcpy(F, d.F.data(), d.F.size() * sizeof(float));
+    return 1;
+}
 
 LTRAPI LTRBOOL ltrdbg_GetRayData(ltr_Scene* scene, u32 inst, float* vis, float* ao)
 {

@@ -2172,6 +2172,27 @@ void run_bake(ltr_Scene* S)
         rs.refine_steps = S->opt.refine_steps;
         rs.bounces = cfg.bounce_count;
         RadResult rr;
+        // debug records of the radiosity elements (keep_samples)
+        auto rad_dump_begin = [&](u32 n) {
+            if (!S->opt.keep_samples) return;
+            S->rad_dump.n = n;
+            if (n <= RadDump::kRadDumpMaxF) {
+                S->rad_dump.F.resize((size_t) n * n);
+                rs.f_host = S->rad_dump.F.data();
+            }
+        };
+        auto rad_dump_end = [&](u32 n, const float4* pos, const float4* nrm, const float4* da, const float4* emit,
+                                const float4* total) {
+            if (!S->opt.keep_samples) return;
+            RadDump& d = S->rad_dump;
+            std::vector<float>* dst[5] = {&d.pos, &d.nrm, &d.diff_area, &d.emit, &d.total};
+            const float4* src[5] = {pos, nrm, da, emit, total};
+            for (int k = 0; k < 5; ++k) {
+                dst[k]->resize(4 * (size_t) n);
+                CK(cudaMemcpyAsync(dst[k]->data(), src[k], n * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n * sizeof(float4));
+            }
+            CK(cudaStreamSynchronize(st));
+        };
         if (S->opt.radiosity_patches == 0) {
             cudaEvent_t up = nullptr;
             CK(cudaEventCreateWithFlags(&up, cudaEventDisableTiming));
@@ -2182,7 +2203,9 @@ void run_bake(ltr_Scene* S)
             CK(cudaGetLastError());
             cudaEventDestroy(up);
             RadDevInputs ri{n_samples, d_rpos, d_rnrm, d_rda, d_remit};
+            rad_dump_begin(n_samples);
             rr = radiosity_solve_dev(ri, rs, bv, err_rad, st, d_lm, &S->abort_flag);
+            rad_dump_end(n_samples, d_rpos, d_rnrm, d_rda, d_remit, d_lm);
             S->stats.rad_elements = n_samples;
         } else {
             // Patch mode: group samples by (instance, lightmap tile, dominant
@@ -2280,7 +2303,9 @@ void run_bake(ltr_Scene* S)
                                                                  d_emis, d_lm, d_ppos, d_pnrm, d_pda, d_pemit); note_launch();
                 CK(cudaGetLastError());
                 RadDevInputs pi{np, d_ppos, d_pnrm, d_pda, d_pemit};
+                rad_dump_begin(np);
                 rr = radiosity_solve_dev(pi, rs, bv, err_rad, st, d_ptot, &S->abort_flag);
+                rad_dump_end(np, d_ppos, d_pnrm, d_pda, d_pemit, d_ptot);
                 k_patch_apply<<<(n_samples + kThreads - 1) / kThreads, kThreads, 0, st>>>(
                     n_samples, d_patch_of, d_emis, d_ptot, d_pemit, d_lm); note_launch();
                 CK(cudaGetLastError());

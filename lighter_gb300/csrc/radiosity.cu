@@ -56,12 +56,71 @@ __device__ __forceinline__ float pair_pretest(V3 AP, V3 AN, V3 BP, V3 BN)
     return f < kSmall ? 0.0f : f;
 }
 
+// FP16 range. A factor grows as 1 / (pi |d|^2) for close elements, past FP16's
+// largest value (65504) for elements a few millimetres apart, so an FP16 F is
+// stored per row scaled by a power of two: row i holds f * 2^-e_i with e_i in
+// [0, 14] chosen from the row's largest factor (k_ff_rowmax, k_row_scale) so
+// that it stays below 2^15, and values past 65504 (rows that would need
+// e_i > 14) saturate. With e_i <= 14 the smallest linked factor, SMALL_FLOAT,
+// stays above FP16's smallest subnormal (0.001 * 2^-14 > 2^-24), so a factor
+// is zero in FP16 exactly where it is zero in FP32. The bounce multiplies each
+// row's sum by 2^e_i, which is exact: rounding happens only where F is stored.
+constexpr int kF16MaxExp = 14;
+constexpr float kF16Max = 65504.0f;
+
+// rowmax[i] = float bits of max_j f_ij (f >= 0, so unsigned order is float order)
+__global__ void k_ff_rowmax(u32 n, const float4* __restrict__ pos, const float4* __restrict__ nrm,
+                            unsigned* __restrict__ rowmax)
+{
+    __shared__ float tile[32][33];
+    const u32 bi = blockIdx.y, bj = blockIdx.x;
+    if (bj < bi) return;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    for (int k = 0; k < 4; ++k) {
+        int r = ty + 8 * k;
+        u32 i = bi * 32 + r, j = bj * 32 + tx;
+        float f = 0.0f;
+        if (i < j && j < n) f = pair_pretest(ld3(pos[i]), ld3(nrm[i]), ld3(pos[j]), ld3(nrm[j]));
+        tile[r][tx] = f;
+        float m = f;
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+        if (tx == 0 && m > 0.0f && i < n) atomicMax(&rowmax[i], __float_as_uint(m));
+    }
+    __syncthreads();
+    for (int k = 0; k < 4; ++k) {   // column maxima: row j of the mirrored entries
+        int c = ty + 8 * k;
+        u32 j = bj * 32 + c;
+        float m = tile[tx][c];
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+        if (tx == 0 && m > 0.0f && j < n) atomicMax(&rowmax[j], __float_as_uint(m));
+    }
+}
+
+// up[i] = 2^e_i, e_i = clamp(k - 15, 0, 14) where rowmax < 2^k
+__global__ void k_row_scale(u32 n, const unsigned* __restrict__ rowmax, float* __restrict__ up)
+{
+    u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int k = 0;
+    frexpf(__uint_as_float(rowmax[i]), &k);
+    int e = min(max(k - 15, 0), kF16MaxExp);
+    up[i] = __uint_as_float((u32) (127 + e) << 23);
+}
+
+template <class T> __device__ __forceinline__ T store_f(float f, const float* up, u32 row)
+{
+    if constexpr (std::is_same<T, __half>::value) {
+        if (up) f = fminf(f / up[row], kF16Max);   // division by a power of two: exact
+    }
+    return to_store<T>(f);
+}
+
 // counts[0]: pairs that passed (appended; entries past `cap` are dropped and
 // the host runs the pass again with room for all of them)
 template <class T>
 __global__ void k_ff_pretest(u32 n, size_t ld, const float4* __restrict__ pos, const float4* __restrict__ nrm,
-                             T* __restrict__ F, PairRef* __restrict__ cand, unsigned long long cap,
-                             unsigned long long* counts)
+                             const float* __restrict__ up, T* __restrict__ F, PairRef* __restrict__ cand,
+                             unsigned long long cap, unsigned long long* counts)
 {
     __shared__ float tile[32][33];
     const u32 bi = blockIdx.y, bj = blockIdx.x;
@@ -90,12 +149,12 @@ __global__ void k_ff_pretest(u32 n, size_t ld, const float4* __restrict__ pos, c
         int r = ty + 8 * k;
         if (bi == bj) {
             u32 i = bi * 32 + r, j = bj * 32 + tx;
-            if (i < n && j < ld) F[(size_t) i * ld + j] = to_store<T>(tile[r][tx] + tile[tx][r]);
+            if (i < n && j < ld) F[(size_t) i * ld + j] = store_f<T>(tile[r][tx] + tile[tx][r], up, i);
         } else {
             u32 i = bi * 32 + r, j = bj * 32 + tx;
-            if (i < n && j < ld) F[(size_t) i * ld + j] = to_store<T>(tile[r][tx]);
+            if (i < n && j < ld) F[(size_t) i * ld + j] = store_f<T>(tile[r][tx], up, i);
             u32 i2 = bj * 32 + r, j2 = bi * 32 + tx;
-            if (i2 < n && j2 < ld) F[(size_t) i2 * ld + j2] = to_store<T>(tile[tx][r]);
+            if (i2 < n && j2 < ld) F[(size_t) i2 * ld + j2] = store_f<T>(tile[tx][r], up, i2);
         }
     }
 }
@@ -186,7 +245,8 @@ constexpr int kRadRows = 4;   // rows of F per warp in the bounce product
 template <class T, bool kExact>
 __global__ void __launch_bounds__(256) k_rad_gemv(u32 n, size_t ld, const T* __restrict__ F,
                                                   const float4* __restrict__ pos, const float4* __restrict__ nrm,
-                                                  const float4* __restrict__ X, float4* __restrict__ Y)
+                                                  const float* __restrict__ up, const float4* __restrict__ X,
+                                                  float4* __restrict__ Y)
 {
     constexpr int V = kExact ? 4 : 16 / (int) sizeof(T);
     using Raw = RawF<V * sizeof(T)>;
@@ -253,9 +313,22 @@ __global__ void __launch_bounds__(256) k_rad_gemv(u32 n, size_t ld, const T* __r
             for (int o = 16; o > 0; o >>= 1) acc[r][q] += __shfl_down_sync(0xffffffffu, acc[r][q], o);
     if (lane == 0) {
 #pragma unroll
-        for (int r = 0; r < kRadRows; ++r)
-            if (r0 + r < n) Y[r0 + r] = make_float4(acc[r][0], acc[r][1], acc[r][2], 0.0f);
+        for (int r = 0; r < kRadRows; ++r) {
+            if (r0 + r >= n) continue;
+            const float s = (!kExact && up) ? up[r0 + r] : 1.0f;   // row scale of an FP16 F (exact)
+            Y[r0 + r] = make_float4(acc[r][0] * s, acc[r][1] * s, acc[r][2] * s, 0.0f);
+        }
     }
+}
+
+// F (n x ld, stored type) widened to n x n floats (debug copy).
+template <class T>
+__global__ void k_f_widen(u32 n, size_t ld, const T* __restrict__ F, const float* __restrict__ up,
+                          float* __restrict__ out)
+{
+    size_t k = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (size_t) n * n) return;
+    out[k] = to_f(F[(k / n) * ld + k % n]) * (up ? up[k / n] : 1.0f);
 }
 
 // total += Y, out = Y (lighter.cpp:784-796).
@@ -272,7 +345,7 @@ __global__ void k_rad_update(u32 n, const float4* __restrict__ Y, float4* __rest
 // the stream once after the first pass, to size the pair list).
 template <class T>
 RadFormFactors build_ff(u32 n, size_t ld, const float4* pos, const float4* nrm, const BvhView& bvh, ErrFlag err,
-                        int links, T* F, cudaStream_t st)
+                        int links, T* F, const float* up, cudaStream_t st)
 {
     RadFormFactors out;
     if (n == 0) return out;
@@ -292,7 +365,7 @@ RadFormFactors build_ff(u32 n, size_t ld, const float4* pos, const float4* nrm, 
     for (int attempt = 0; attempt < 2; ++attempt) {
         RCK(cudaMallocAsync(&cand, std::max<unsigned long long>(cap, 1) * sizeof(PairRef), st));
         RCK(cudaMemsetAsync(counts, 0, 3 * sizeof(unsigned long long), st));
-        k_ff_pretest<T><<<dim3(nb, nb), dim3(32, 8), 0, st>>>(n, ld, pos, nrm, F, cand, cap, counts); note_launch();
+        k_ff_pretest<T><<<dim3(nb, nb), dim3(32, 8), 0, st>>>(n, ld, pos, nrm, up, F, cand, cap, counts); note_launch();
         RCK(cudaGetLastError());
         RCK(cudaMemcpyAsync(&n_cand, counts, sizeof(n_cand), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(n_cand));
         RCK(cudaStreamSynchronize(st));
@@ -353,8 +426,32 @@ RadResult solve_t(const RadDevInputs& in, const RadSettings& rs, const BvhView& 
     cudaEvent_t e0, e1, e2;
     RCK(cudaEventCreate(&e0)); RCK(cudaEventCreate(&e1)); RCK(cudaEventCreate(&e2));
     RCK(cudaEventRecord(e0, st));
-    RadFormFactors ff = build_ff<T>(n, ld, in.pos, in.nrm, bvh, err, rs.links, F, st);
+    float* up = nullptr;   // row scales of an FP16 F
+    unsigned* rowmax = nullptr;
+    struct FreeScale {
+        cudaStream_t st; void** p[2];
+        ~FreeScale() { for (void** q : p) if (*q) cudaFreeAsync(*q, st); }
+    } guard_scale{st, {(void**) &up, (void**) &rowmax}};
+    if (std::is_same<T, __half>::value) {
+        const u32 nb = (n + 31) / 32;
+        RCK(cudaMallocAsync(&up, n * sizeof(float), st));
+        RCK(cudaMallocAsync(&rowmax, n * sizeof(unsigned), st));
+        RCK(cudaMemsetAsync(rowmax, 0, n * sizeof(unsigned), st));
+        k_ff_rowmax<<<dim3(nb, nb), dim3(32, 8), 0, st>>>(n, in.pos, in.nrm, rowmax); note_launch();
+        k_row_scale<<<(n + 255) / 256, 256, 0, st>>>(n, rowmax, up); note_launch();
+        RCK(cudaGetLastError());
+    }
+    RadFormFactors ff = build_ff<T>(n, ld, in.pos, in.nrm, bvh, err, rs.links, F, up, st);
     RCK(cudaEventRecord(e1, st));
+    if (rs.f_host) {
+        const size_t nn = (size_t) n * n;
+        float* wide = nullptr;
+        RCK(cudaMallocAsync(&wide, nn * sizeof(float), st));
+        k_f_widen<T><<<(unsigned) ((nn + 255) / 256), 256, 0, st>>>(n, ld, F, up, wide); note_launch();
+        RCK(cudaGetLastError());
+        RCK(cudaMemcpyAsync(rs.f_host, wide, nn * sizeof(float), cudaMemcpyDeviceToHost, st)); note_d2h(nn * sizeof(float));
+        RCK(cudaFreeAsync(wide, st));
+    }
     for (int b = 0; b < rs.bounces; ++b) {
         if (abort_flag && abort_flag->load()) break;
         k_rad_x<<<(n + 255) / 256, 256, 0, st>>>(n, out, in.diff_area, X); note_launch();
@@ -362,9 +459,9 @@ RadResult solve_t(const RadDevInputs& in, const RadSettings& rs, const BvhView& 
         const bool exact = sizeof(T) < 4 && b >= rs.bounces - rs.refine_steps;
         const unsigned grid = (unsigned) ((((size_t) n + kRadRows - 1) / kRadRows * 32 + 255) / 256);
         if (exact)
-            k_rad_gemv<T, true><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, X, Y);
+            k_rad_gemv<T, true><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, up, X, Y);
         else
-            k_rad_gemv<T, false><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, X, Y);
+            k_rad_gemv<T, false><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, up, X, Y);
         note_launch();
         k_rad_update<<<(n + 255) / 256, 256, 0, st>>>(n, Y, total, out); note_launch();
         RCK(cudaGetLastError());
@@ -397,7 +494,7 @@ RadResult radiosity_solve_dev(const RadDevInputs& in, const RadSettings& rs, con
 RadFormFactors radiosity_form_factors_f32(uint32_t n, const float4* pos, const float4* nrm, const BvhView& bvh,
                                           ErrFlag err, int links, float* F, cudaStream_t st)
 {
-    return build_ff<float>(n, n, pos, nrm, bvh, err, links, F, st);
+    return build_ff<float>(n, n, pos, nrm, bvh, err, links, F, nullptr, st);
 }
 
 RadResult radiosity_solve(const RadInputs& in, const RadSettings& rs, const BvhView& bvh, ErrFlag err, cudaStream_t st,

@@ -27,8 +27,9 @@ struct RadInputs {
 struct RadSettings {
     int links = 0;        // LTRG_LINKS_*
     int precision = 0;    // LTRG_F_*
-    int refine_steps = 1;
+    int refine_steps = 1;  // 16-bit F: the last refine_steps bounces recompute the factors in FP32
     int bounces = 1;
+    float* f_host = nullptr;   // debug: receives F as n x n floats (the stored values, widened)
 };
 
 struct RadResult {

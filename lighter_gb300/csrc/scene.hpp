@@ -47,6 +47,15 @@ struct SampleDump {
     u32 n_lights = 0, ao_ns = 0;
 };
 
+// The radiosity elements of the last bake (samples, or patches in patch mode),
+// kept when keep_samples is set: float4 per element, and F as n x n floats
+// when n <= kRadDumpMaxF.
+struct RadDump {
+    static constexpr u32 kRadDumpMaxF = 24576;
+    u32 n = 0;
+    std::vector<float> pos, nrm, diff_area, emit, total, F;
+};
+
 }  // namespace lg
 
 struct ltr_Mesh {
@@ -80,6 +89,7 @@ struct ltr_Scene {
     float* ao_pinned = nullptr;             // page-locked AO random offsets, reused across bakes
     lg::u32 ao_pinned_n = 0;
     std::vector<lg::SampleDump> dump;
+    lg::RadDump rad_dump;
     lg::u32 rad_links = 0;
     ltrg_Stats stats;
     std::string error;

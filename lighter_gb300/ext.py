@@ -1,6 +1,8 @@
 """ctypes mirror of include/lighter_gb300.h (the GPU extensions)."""
 import ctypes as C
 
+import numpy as np
+
 from .abi import Config, SampleRequest, u32
 
 LTRG_LINKS_REFERENCE = 0
@@ -56,7 +58,29 @@ EXT_API.update({
     "ltrg_GetTuning": (C.c_int, [C.c_int, C.POINTER(Tuning)]),
     "ltrg_SetTuning": (C.c_int, [C.c_int, C.POINTER(Tuning)]),
     "ltrg_Autotune": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+    "ltrdbg_GetRadiosity": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)] + [C.c_void_p] * 6),
 })
+
+
+def get_radiosity(lib, scene, with_F: bool = True):
+    """The radiosity elements of the scene's last bake (baked with keep_samples = 1):
+    dict of n and (n, 4) float32 arrays pos, nrm, diff_area, emit, total, plus the
+    (n, n) form factors F (widened from the stored type) when `with_F`. None when
+    the bake ran no radiosity."""
+    n = C.c_uint32(0)
+    lib.ltrdbg_GetRadiosity(scene, C.byref(n), None, None, None, None, None, None)
+    if n.value == 0:
+        return None
+    out = {k: np.zeros((n.value, 4), np.float32) for k in ("pos", "nrm", "diff_area", "emit", "total")}
+    F = np.zeros((n.value, n.value), np.float32) if with_F else None
+    ok = lib.ltrdbg_GetRadiosity(scene, C.byref(n), *(out[k].ctypes.data for k in
+                                                     ("pos", "nrm", "diff_area", "emit", "total")),
+                                 F.ctypes.data if F is not None else None)
+    if not ok:
+        raise RuntimeError("ltrdbg_GetRadiosity: no radiosity records (F kept only up to 24576 elements)")
+    out["n"] = n.value
+    out["F"] = F
+    return out
 
 
 def autotune(lib, scene) -> dict:
