@@ -408,6 +408,57 @@ def run_batch(args, local):
     }
 
 
+HEADLINE_WORKLOAD = ("{n} mid scenes (seeds 1..{n}, as the single-scene workload) in one ltrg_StartBatch, FP16 form "
+                     "factors with per-row scales, the last of 2 bounces refined in FP32")
+
+
+def run_headline(args, local, single):
+    """The batched mixed-precision bake against the plain FP32 single-scene bake:
+    `--headline-scenes` mid scenes baked as one batch with FP16 F (one refinement
+    bounce), host wall clock through the C API, against the single FP32 bake's
+    end-to-end and device figures of the same line."""
+    import ctypes as C
+
+    from lighter_gb300 import library, scenes
+    from lighter_gb300.ext import get_stats
+    from lighter_gb300.scene import ingest
+
+    lib = library()
+    n = args.headline_scenes
+    opts = {"device": local, "radiosity_patches": args.patches, "radiosity_links": 1, "radiosity_precision": 1,
+            "refine_steps": 1}
+    handles = [ingest(lib, scenes.mid(seed=s, lm=args.lm), gpu_options=opts) for s in range(1, n + 1)]
+    arr = (C.c_void_p * n)(*[h for h, _ in handles])
+    try:
+        def batched():
+            t0 = time.perf_counter()
+            if not lib.ltrg_StartBatch(arr, n):
+                raise RuntimeError("ltrg_StartBatch rejected the batch")
+            for h, _ in handles:
+                if not lib.ltrg_Wait(h):
+                    raise RuntimeError("batch bake failed: " + (lib.ltrg_LastError(h) or b"").decode())
+            return time.perf_counter() - t0
+
+        batched()
+        times = [batched() for _ in range(max(1, args.batch_steps))]
+        st = [get_stats(lib, h) for h, _ in handles]
+    finally:
+        for h, _ in handles:
+            lib.ltr_DestroyScene(h)
+    t = statistics.median(times)
+    rays = sum(x["shadow_evals"] + x["ao_rays"] + x["rad_vis_rays"] for x in st)
+    spb = statistics.median(x["ms_rad_bounce"] / 2 / 1000.0 for x in st)
+    return {
+        "workload": HEADLINE_WORKLOAD.format(n=n), "wall_s": t, "rays": rays, "rays_per_s": rays / t,
+        "s_per_bounce": spb,
+        "s_per_bounce_note": "per-scene CUDA-event time of the bounces while the batch's scenes share the GPU",
+        "plain_fp32_single_scene": {"rays_per_s_e2e": single["e2e"]["value"], "rays_per_s_device": single["value"],
+                                    "s_per_bounce": single["s_per_bounce"]},
+        "rays_per_s_vs_plain_e2e": rays / t / single["e2e"]["value"],
+        "timing": "host wall clock, median of %d batches after one warm-up" % len(times),
+    }
+
+
 def _bake_once(lib, scene):
     lib.ltr_Start(scene)
     if not lib.ltrg_Wait(scene):
@@ -436,6 +487,9 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--headline-scenes", type=int, default=4)
+    ap.add_argument("--no-headline", action="store_true",
+                    help="skip the batched FP16 mid-scene bake compared with the plain FP32 one")
     ap.add_argument("--no-rad-precisions", action="store_true",
                     help="skip the per-precision bakes (FP32 / FP16 / BF16 form factors, with and without refinement)")
     ap.add_argument("--no-bake", action="store_true",
@@ -508,6 +562,8 @@ def main():
         desc = scenes.large(seed=1, lm=args.lm) if args.scene == "large" else scenes.mid(seed=1, lm=args.lm)
         line["bake_radiosity_precisions"] = run_rad_precisions(
             args, library(), desc, {"device": local, "radiosity_patches": args.patches, "radiosity_links": 1}, bounces)
+    if not args.no_headline and args.scene == "mid":
+        line["batched_fp16_vs_plain_fp32"] = run_headline(args, local, line)
     if not args.no_batch:
         line["batch"] = run_batch(args, 0)
     if not args.no_gather:
