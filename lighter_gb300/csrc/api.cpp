@@ -367,13 +367,18 @@ LTRAPI LTRBOOL ltrg_Autotune(ltr_Scene* scene, ltrg_Tuning* out)
         ms_ao = scene->stats.ms_ao;
         return true;
     };
+    // a stage's time varies from bake to bake by a few per cent: the least of three bakes
     auto measure = [&](const ltrg_Tuning& t, double& ms_direct, double& ms_ao) {
-        double d0, a0, d1, a1;
-        if (!bake_once(t, d0, a0) || !bake_once(t, d1, a1)) return false;
-        ms_direct = std::min(d0, d1);
-        ms_ao = std::min(a0, a1);
+        ms_direct = ms_ao = 1e300;
+        for (int r = 0; r < 3; ++r) {
+            double d, a;
+            if (!bake_once(t, d, a)) return false;
+            ms_direct = std::min(ms_direct, d);
+            ms_ao = std::min(ms_ao, a);
+        }
         return true;
     };
+    const ltrg_Tuning start = best;
     double bd, ba;
     if (!bake_once(best, bd, ba) || !measure(best, bd, ba)) {   // warm-up, then the baseline
         ltrg_SetTuning(dev, &best);
@@ -404,6 +409,19 @@ LTRAPI LTRBOOL ltrg_Autotune(ltr_Scene* scene, ltrg_Tuning* out)
                 ba = p.direct ? ba : a;
             }
         }
+    }
+    // confirm each kernel's choice against the starting shapes, timed alternately
+    if (memcmp(&best, &start, sizeof(best)) != 0) {
+        double sd = 1e300, sa = 1e300, nd = 1e300, na = 1e300;
+        for (int r = 0; r < 2; ++r) {
+            double d, a;
+            if (!measure(start, d, a)) { ltrg_SetTuning(dev, &start); return 0; }
+            sd = std::min(sd, d); sa = std::min(sa, a);
+            if (!measure(best, d, a)) { ltrg_SetTuning(dev, &start); return 0; }
+            nd = std::min(nd, d); na = std::min(na, a);
+        }
+        if (!(nd < sd * 0.98)) { best.direct_block = start.direct_block; best.direct_blocks_per_sm = start.direct_blocks_per_sm; }
+        if (!(na < sa * 0.98)) { best.ao_block = start.ao_block; best.ao_blocks_per_sm = start.ao_blocks_per_sm; }
     }
     ltrg_SetTuning(dev, &best);
     if (out) *out = best;

@@ -200,6 +200,7 @@ struct FixupArgs {
     const float4* ref_nodes;   // 2 per node: (mn.xyz, mx.x), (mx.yz, ch, ido)
     const int* ref_items;      // <count, ids...> lists
     const int4* ref_inst;      // per instance: node offset, item offset, triangle offset, node count
+    const float4* inst_box;    // per instance: (root mn.xyz, 0), (root mx.xyz, 0); inverted when empty
     const float* tri_xyz;      // shadow-part triangles, instance by instance in local order
     int n_inst;
     u32 n_probe, n_samples;
@@ -232,45 +233,113 @@ __device__ __forceinline__ void offset_one(const FixupArgs& a, V3 P1, V3 P2, V3 
     if (r >= 0.9f || hit_local == local) P = Pnew;
 }
 
-__global__ void k_fixup(FixupArgs a)
+// One instance of the concave-edge pass: a depth-first walk (node items, left
+// subtree, right subtree) of its reference-shaped tree with the query box
+// P +- dist fixed at the start, while P moves.
+__device__ __forceinline__ void fixup_instance(const FixupArgs& a, int k, V3& P, V3 N, float dist)
 {
-    u32 s = a.n_probe + blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= a.n_samples) return;
-    V3 P = ld3(a.spos[s]);
-    V3 N = ld3(a.snrm[s]);
-    float dist = sqrtf(a.srad[s].w);
-    // every instance's tree in instance order (lighter.cpp:445-446): a
-    // depth-first walk (node items, left subtree, right subtree) of the
-    // reference-shaped tree with a query box fixed at the start, while P moves
-    for (int k = 1; k < a.n_inst; ++k) {
-        int4 ri = a.ref_inst[k];
-        if (ri.w == 0) continue;
-        V3 qmn = P - splat(dist), qmx = P + splat(dist);
-        int stack[40];
-        int sp = 0;
-        stack[sp++] = 0;
-        while (sp > 0) {
-            int node = stack[--sp];
-            float4 n0 = __ldg(&a.ref_nodes[2 * (ri.x + node)]);
-            float4 n1 = __ldg(&a.ref_nodes[2 * (ri.x + node) + 1]);
-            if (qmn.x > n0.w || qmx.x < n0.x || qmn.y > n1.x || qmx.y < n0.y || qmn.z > n1.y || qmx.z < n0.z) continue;
-            int ch = __float_as_int(n1.z), ido = __float_as_int(n1.w);
-            if (ido != -1) {
-                const int* it = a.ref_items + ri.y + ido;
-                int cnt = it[0];
-                for (int i = 0; i < cnt; ++i) {
-                    int id = it[1 + i];
-                    const float* p = a.tri_xyz + 9 * (size_t) (ri.z + id);
-                    offset_one(a, mk(p[0], p[1], p[2]), mk(p[3], p[4], p[5]), mk(p[6], p[7], p[8]), id, (u32) k, P, N,
-                               dist);
-                }
-            }
-            if (ch != -1) {
-                if (sp + 2 <= 40) { stack[sp++] = ch; stack[sp++] = node + 1; }
-                else raise_err(a.err, 1u);
+    int4 ri = a.ref_inst[k];
+    if (ri.w == 0) return;
+    V3 qmn = P - splat(dist), qmx = P + splat(dist);
+    int stack[40];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        int node = stack[--sp];
+        float4 n0 = __ldg(&a.ref_nodes[2 * (ri.x + node)]);
+        float4 n1 = __ldg(&a.ref_nodes[2 * (ri.x + node) + 1]);
+        if (qmn.x > n0.w || qmx.x < n0.x || qmn.y > n1.x || qmx.y < n0.y || qmn.z > n1.y || qmx.z < n0.z) continue;
+        int ch = __float_as_int(n1.z), ido = __float_as_int(n1.w);
+        if (ido != -1) {
+            const int* it = a.ref_items + ri.y + ido;
+            int cnt = it[0];
+            for (int i = 0; i < cnt; ++i) {
+                int id = it[1 + i];
+                const float* p = a.tri_xyz + 9 * (size_t) (ri.z + id);
+                offset_one(a, mk(p[0], p[1], p[2]), mk(p[3], p[4], p[5]), mk(p[6], p[7], p[8]), id, (u32) k, P, N,
+                           dist);
             }
         }
+        if (ch != -1) {
+            if (sp + 2 <= 40) { stack[sp++] = ch; stack[sp++] = node + 1; }
+            else raise_err(a.err, 1u);
+        }
     }
+}
+
+constexpr int kFixupThreads = 128;
+constexpr int kFixupCand = 256;   // candidate instances listed per warp
+
+// The concave-edge pass tests every instance's tree, in instance order
+// (lighter.cpp:445-446); an instance whose root box misses the query box
+// leaves P unchanged. A warp (32 consecutive samples) first lists, in order,
+// the instances whose root box meets the union of its query boxes grown by
+// G > M, and its lanes walk only those. A lane whose P has moved more than M
+// (per axis) from its start could meet an unlisted instance, so once any lane
+// has, the warp walks every remaining instance. Either way each lane visits
+// every instance its query box meets, in order: the reference's result.
+__global__ void __launch_bounds__(kFixupThreads) k_fixup(FixupArgs a)
+{
+    __shared__ int cand[kFixupThreads / 32][kFixupCand];
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const u32 s = a.n_probe + blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = s < a.n_samples;
+    if (!__any_sync(full, active)) return;
+    V3 P = mk(0, 0, 0), N = mk(0, 0, 0);
+    float dist = 0.0f;
+    if (active) {
+        P = ld3(a.spos[s]);
+        N = ld3(a.snrm[s]);
+        dist = sqrtf(a.srad[s].w);
+    }
+    const V3 P0 = P;
+    float lo[3] = {active ? P.x - dist : 3.0e38f, active ? P.y - dist : 3.0e38f, active ? P.z - dist : 3.0e38f};
+    float hi[3] = {active ? P.x + dist : -3.0e38f, active ? P.y + dist : -3.0e38f, active ? P.z + dist : -3.0e38f};
+    float dmax = dist;
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = fminf(lo[c], __shfl_xor_sync(full, lo[c], o));
+            hi[c] = fmaxf(hi[c], __shfl_xor_sync(full, hi[c], o));
+        }
+        dmax = fmaxf(dmax, __shfl_xor_sync(full, dmax, o));
+    }
+    const float M = 4.0f * dmax + 0.05f;
+    const float G = 1.5f * M + 1e-3f;   // the extra covers rounding of the box arithmetic
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { lo[c] -= G; hi[c] += G; }
+    int ncand = 0;
+    for (int base = 1; base < a.n_inst; base += 32) {
+        const int k = base + lane;
+        bool hit = false;
+        if (k < a.n_inst) {
+            const float4 b0 = __ldg(&a.inst_box[2 * k]), b1 = __ldg(&a.inst_box[2 * k + 1]);
+            hit = !(lo[0] > b1.x || hi[0] < b0.x || lo[1] > b1.y || hi[1] < b0.y || lo[2] > b1.z || hi[2] < b0.z);
+        }
+        const unsigned m = __ballot_sync(full, hit);
+        if (hit) {
+            const int at = ncand + __popc(m & ((1u << lane) - 1u));
+            if (at < kFixupCand) cand[w][at] = k;
+        }
+        ncand += __popc(m);
+    }
+    __syncwarp();
+    bool slow = ncand > kFixupCand;   // list overflow: every instance
+    int ci = 0, k = 1;
+    for (;;) {
+        if (!slow) {
+            if (ci >= ncand) break;
+            k = cand[w][ci++];
+        } else if (k >= a.n_inst) {
+            break;
+        }
+        if (active) fixup_instance(a, k, P, N, dist);
+        const bool far = fabsf(P.x - P0.x) > M || fabsf(P.y - P0.y) > M || fabsf(P.z - P0.z) > M;
+        if (!slow && __any_sync(full, far)) slow = true;
+        ++k;
+    }
+    if (!active) return;
     // push in front of overlapping faces (lighter.cpp:449-465); the
     // reference's BSP query is replaced by the closest hit over occluders
     if (a.max_correct_dist != 0.0f) {
@@ -605,10 +674,13 @@ __global__ void k_patch_inputs(u32 np, const u32* __restrict__ off, const u32* _
                                const float4* __restrict__ emis, const float4* __restrict__ lm, float4* __restrict__ ppos,
                                float4* __restrict__ pnrm, float4* __restrict__ pda, float4* __restrict__ pemit)
 {
-    u32 p = blockIdx.x * blockDim.x + threadIdx.x;
+    // one warp per patch: lanes take every 32nd sample of the patch's list, then
+    // a fixed shuffle tree sums the lanes (deterministic order)
+    const int lane = threadIdx.x & 31;
+    const u32 p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (p >= np) return;
     double q[13] = {0};
-    for (u32 k = off[p]; k < off[p + 1]; ++k) {
+    for (u32 k = off[p] + lane; k < off[p + 1]; k += 32) {
         u32 s = idx[k];
         double a = srad[s].w;
         V3 n = normalized(ld3(snrm[s]));
@@ -621,6 +693,10 @@ __global__ void k_patch_inputs(u32 np, const u32* __restrict__ off, const u32* _
         q[7] += a * D.x; q[8] += a * D.y; q[9] += a * D.z;
         q[10] += a * e.x; q[11] += a * e.y; q[12] += a * e.z;
     }
+#pragma unroll
+    for (int c = 0; c < 13; ++c)
+        for (int o = 16; o > 0; o >>= 1) q[c] += __shfl_down_sync(0xffffffffu, q[c], o);
+    if (lane != 0) return;
     double a = q[0] > 0 ? q[0] : 1.0;
     V3 nn = normalized(mk((float) (q[4] / a), (float) (q[5] / a), (float) (q[6] / a)));
     ppos[p] = make_float4((float) (q[1] / a), (float) (q[2] / a), (float) (q[3] / a), 0);
@@ -1673,9 +1749,19 @@ void run_bake(ltr_Scene* S)
     std::vector<float4> ref_nodes;
     std::vector<int> ref_items;
     std::vector<int4> ref_inst(n_inst, make_int4(0, 0, 0, 0));
+    std::vector<float4> fix_box(2 * (size_t) n_inst);   // root boxes for the fixup's instance culling
+    for (int i = 0; i < n_inst; ++i) {
+        fix_box[2 * i] = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.0f);
+        fix_box[2 * i + 1] = make_float4(-3.0e38f, -3.0e38f, -3.0e38f, 0.0f);
+    }
     for (int i = 1; i < n_inst; ++i) {
         const RefTree& rt_i = rtrees[i];
         if (inst_tri_off[i + 1] == inst_tri_off[i]) continue;
+        if (!rt_i.nodes.empty()) {
+            const RefNode& root = rt_i.nodes[0];
+            fix_box[2 * i] = make_float4(root.mn[0], root.mn[1], root.mn[2], 0.0f);
+            fix_box[2 * i + 1] = make_float4(root.mx[0], root.mx[1], root.mx[2], 0.0f);
+        }
         ref_inst[i] = make_int4((int) (ref_nodes.size() / 2), (int) ref_items.size(), inst_tri_off[i],
                                 (int) rt_i.nodes.size());
         for (const RefNode& nd : rt_i.nodes) {
@@ -1809,6 +1895,7 @@ void run_bake(ltr_Scene* S)
     float4* d_ref_nodes = A.upload(ref_nodes);
     int* d_ref_items = A.upload(ref_items);
     int4* d_ref_inst = A.upload(ref_inst);
+    float4* d_fix_box = A.upload(fix_box);
     unsigned char* d_lit = A.upload(lit);
     DLight* d_lights = A.upload(dl);
     float* d_rt = A.upload(rt);
@@ -1975,6 +2062,7 @@ void run_bake(ltr_Scene* S)
         fa.ref_nodes = d_ref_nodes;
         fa.ref_items = d_ref_items;
         fa.ref_inst = d_ref_inst;
+        fa.inst_box = d_fix_box;
         fa.tri_xyz = d_tri_xyz;
         fa.n_inst = n_inst;
         fa.n_probe = n_probe;
@@ -1984,7 +2072,7 @@ void run_bake(ltr_Scene* S)
         fa.spos = d_spos;
         fa.snrm = d_snrm;
         fa.srad = d_srad;
-        k_fixup<<<(n_cov + 127) / 128, 128, 0, st>>>(fa); note_launch();
+        k_fixup<<<(n_cov + kFixupThreads - 1) / kFixupThreads, kFixupThreads, 0, st>>>(fa); note_launch();
         CK(cudaGetLastError());
         checkpoint("sample fixup");
     }
@@ -2299,7 +2387,7 @@ void run_bake(ltr_Scene* S)
             float4* d_pemit = A.alloc<float4>(np);
             float4* d_ptot = A.alloc<float4>(np);
             if (np) {
-                k_patch_inputs<<<(np + 127) / 128, 128, 0, st>>>(np, d_csr_off, d_csr_idx, d_spos, d_snrm, d_srad, d_diff,
+                k_patch_inputs<<<(unsigned) (((size_t) np * 32 + 255) / 256), 256, 0, st>>>(np, d_csr_off, d_csr_idx, d_spos, d_snrm, d_srad, d_diff,
                                                                  d_emis, d_lm, d_ppos, d_pnrm, d_pda, d_pemit); note_launch();
                 CK(cudaGetLastError());
                 RadDevInputs pi{np, d_ppos, d_pnrm, d_pda, d_pemit};
