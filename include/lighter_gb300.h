@@ -26,6 +26,10 @@ extern "C" {
 #define LTRG_F_FP16 1
 #define LTRG_F_BF16 2
 
+/* Scene BVH builders. */
+#define LTRG_BVH_PLOC  0   /* locally-ordered clustering over the Morton order (closer to a SAH tree) */
+#define LTRG_BVH_RADIX 1   /* Karras' radix-tree hierarchy over the Morton order (faster build) */
+
 typedef struct ltrg_Options {
     int device;               /* CUDA device ordinal, default 0 */
     int keep_samples;         /* keep per-sample arrays for ltrdbg_* after the bake, default 0 */
@@ -38,7 +42,9 @@ typedef struct ltrg_Options {
                                    N > 0: group samples into about N patches by (instance, lightmap
                                    tile, dominant normal axis); each texel then receives its patch's
                                    gathered (bounced) light on top of its own direct light */
-    uint32_t reserved[10];
+    uint32_t bvh_builder;     /* LTRG_BVH_*: how the scene BVH is built; results do not depend on it,
+                                 only the trace times do. Default LTRG_BVH_PLOC */
+    uint32_t reserved[9];
 } ltrg_Options;
 
 /* Per-stage device times (CUDA events on the bake stream) and work counters

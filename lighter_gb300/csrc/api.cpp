@@ -316,7 +316,7 @@ LTRAPI void ltrg_GetOptions(ltr_Scene* scene, ltrg_Options* out) { *out = scene-
 LTRAPI LTRBOOL ltrg_SetOptions(ltr_Scene* scene, const ltrg_Options* o)
 {
     if (o->device < 0 || o->radiosity_links < 0 || o->radiosity_links > 1 || o->radiosity_precision < 0 ||
-        o->radiosity_precision > 2 || o->refine_steps < 0 || o->refine_steps > 16)
+        o->radiosity_precision > 2 || o->refine_steps < 0 || o->refine_steps > 16 || o->bvh_builder > 1)
         return 0;
     scene->opt = *o;
     return 1;
@@ -420,7 +420,10 @@ LTRAPI LTRBOOL ltrg_Autotune(ltr_Scene* scene, ltrg_Tuning* out)
             if (!measure(best, d, a)) { ltrg_SetTuning(dev, &start); return 0; }
             nd = std::min(nd, d); na = std::min(na, a);
         }
-        if (!(nd < sd * 0.98)) { best.direct_block = start.direct_block; best.direct_blocks_per_sm = start.direct_blocks_per_sm; }
+        if (!(nd < sd * 0.98)) {
+            best.direct_block = start.direct_block;
+            best.direct_blocks_per_sm = start.direct_blocks_per_sm;
+        }
         if (!(na < sa * 0.98)) { best.ao_block = start.ao_block; best.ao_blocks_per_sm = start.ao_blocks_per_sm; }
     }
     ltrg_SetTuning(dev, &best);

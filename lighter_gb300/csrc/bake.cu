@@ -1927,6 +1927,7 @@ void run_bake(ltr_Scene* S)
     bin.ref_tri = A.upload(ref_tri);
     bin.ref_box = A.upload(ref_box);
     bin.n = (int) ref_tri.size();
+    bin.builder = (int) S->opt.bvh_builder;
     for (int c = 0; c < 3; ++c) { bin.scene_min[c] = bin.n ? rmin[c] : 0; bin.scene_max[c] = bin.n ? rmax[c] : 0; }
     S->stats.reserved[0] = (uint64_t) bin.n;   // leaf references
     bvh_build(bin, bvh, st);

@@ -245,6 +245,131 @@ __global__ void k_pack_records(int nleaf, const float4* __restrict__ tris, float
     d[7] = make_float4(en2.x, en2.y, en2.z, dot(en2, t2));
 }
 
+// ---- locally-ordered clustering (PLOC; Meister and Bittner, "Parallel
+// Locally-Ordered Clustering for Bounding Volume Hierarchy Construction",
+// IEEE TVCG 2018). The leaves in Morton order are the first clusters; every
+// iteration, each cluster finds within kPlocR positions on either side the one
+// whose merged box has the least surface area, mutual nearest pairs merge into
+// a new internal node at the lower position, and the list is compacted,
+// keeping Morton order. Internal nodes are numbered down from n - 2 in merge
+// order (ranks from a scan), so the last merge, the root, is node 0 as in
+// Karras' layout. Ties between equal costs go by a key of the pair alone
+// (distance in the list, then the lower position's parity, then the lower
+// position), so the pairs are totally ordered: the least pair is always mutual
+// (every iteration merges), and a run of equal boxes pairs up (0,1), (2,3), ...
+// and halves each iteration instead of growing a chain.
+
+constexpr int kPlocR = 16;
+constexpr int kPlocB = 256;
+
+__device__ __forceinline__ float merged_area(const float* a, const float* b)
+{
+    float ex = fmaxf(a[3], b[3]) - fminf(a[0], b[0]);
+    float ey = fmaxf(a[4], b[4]) - fminf(a[1], b[1]);
+    float ez = fmaxf(a[5], b[5]) - fminf(a[2], b[2]);
+    return ex * ey + ey * ez + ez * ex;
+}
+
+__global__ void k_leaf_boxes(const float* ref_box, const u32* ids, int n, float* leaf_box, int* cl, float* cbox)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float b[6];
+    leaf_box_of(ref_box + 6 * (size_t) ids[i], b);
+    for (int c = 0; c < 6; ++c) {
+        leaf_box[6 * (size_t) i + c] = b[c];
+        cbox[6 * (size_t) i + c] = b[c];
+    }
+    cl[i] = ~i;
+}
+
+__global__ void __launch_bounds__(kPlocB) k_ploc_nn(int count, const float* __restrict__ cbox, int* __restrict__ nn)
+{
+    __shared__ float sb[(kPlocB + 2 * kPlocR) * 6];
+    const int start = blockIdx.x * kPlocB;
+    for (int k = threadIdx.x; k < (kPlocB + 2 * kPlocR) * 6; k += blockDim.x) {
+        const long g = (long) start * 6 - kPlocR * 6 + k;
+        sb[k] = (g >= 0 && g < (long) count * 6) ? cbox[g] : 0.0f;
+    }
+    __syncthreads();
+    const int i = start + threadIdx.x;
+    if (i >= count) return;
+    const float* me = sb + 6 * (threadIdx.x + kPlocR);
+    float best = FLT_MAX;
+    int bj = -1, bd = 1 << 30, bpar = 2, bmin = 1 << 30;
+    for (int d = -kPlocR; d <= kPlocR; ++d) {
+        const int j = i + d;
+        if (d == 0 || j < 0 || j >= count) continue;
+        const float c = merged_area(me, sb + 6 * (threadIdx.x + kPlocR + d));
+        const int ad = d < 0 ? -d : d, mn = min(i, j), par = mn & 1;
+        if (c < best || (c == best && (ad < bd || (ad == bd && (par < bpar || (par == bpar && mn < bmin)))))) {
+            best = c; bj = j; bd = ad; bpar = par; bmin = mn;
+        }
+    }
+    nn[i] = bj;
+}
+
+// flags[i]: merge (high word: i < nn[i] and mutual), keep (low word: not the
+// upper half of a mutual pair); flags[count] = 0 closes the scan.
+__global__ void k_ploc_flags(int count, const int* __restrict__ nn, unsigned long long* __restrict__ flags)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > count) return;
+    if (i == count) { flags[i] = 0ull; return; }
+    const int j = nn[i];
+    const bool mutual = j >= 0 && nn[j] == i;
+    const unsigned long long merge = (mutual && i < j) ? 1ull : 0ull;
+    const unsigned long long keep = (mutual && i > j) ? 0ull : 1ull;
+    flags[i] = (merge << 32) | keep;
+}
+
+__global__ void k_ploc_merge(int count, int base, const int* __restrict__ nn, const unsigned long long* __restrict__ flags,
+                             const unsigned long long* __restrict__ scan, const int* __restrict__ cl,
+                             const float* __restrict__ cbox, int* __restrict__ ncl, float* __restrict__ ncbox,
+                             int* __restrict__ left, int* __restrict__ right, int* __restrict__ parent_int,
+                             float* __restrict__ int_box)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const unsigned long long f = flags[i];
+    if (!(f & 0xffffffffull)) return;   // merged into its lower partner
+    const int pos = (int) (scan[i] & 0xffffffffull);
+    const float* a = cbox + 6 * (size_t) i;
+    if (f >> 32) {
+        const int j = nn[i];
+        const int id = base - 1 - (int) (scan[i] >> 32);
+        const float* b = cbox + 6 * (size_t) j;
+        const int ca = cl[i], cb = cl[j];
+        left[id] = ca;
+        right[id] = cb;
+        if (ca >= 0) parent_int[ca] = id;
+        if (cb >= 0) parent_int[cb] = id;
+        float u[6];
+        for (int c = 0; c < 3; ++c) {
+            u[c] = fminf(a[c], b[c]);
+            u[3 + c] = fmaxf(a[3 + c], b[3 + c]);
+        }
+        for (int c = 0; c < 6; ++c) {
+            int_box[6 * (size_t) id + c] = u[c];
+            ncbox[6 * (size_t) pos + c] = u[c];
+        }
+        ncl[pos] = id;
+    } else {
+        for (int c = 0; c < 6; ++c) ncbox[6 * (size_t) pos + c] = a[c];
+        ncl[pos] = cl[i];
+    }
+}
+
+// depth (edges from the root) of the deepest internal node
+__global__ void k_max_depth(int n_int, const int* __restrict__ parent_int, int* __restrict__ maxd)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_int) return;
+    int d = 0;
+    for (int p = parent_int[i]; p >= 0 && d < 4096; p = parent_int[p]) ++d;
+    atomicMax(maxd, d);
+}
+
 template <class T>
 T* alloc(size_t count, cudaStream_t st, size_t& bytes)
 {
@@ -292,15 +417,79 @@ void bvh_build(const BvhBuildInput& in, BvhStorage& out, void* stream)
     void* temp = alloc<char>(temp_bytes, st, scratch_bytes);
     BVH_CHECK(cub::DeviceRadixSort::SortPairs(temp, temp_bytes, codes, codes2, ids, ids2, n, 0, 30, st));
 
-    if (n_int > 0) {
+    // The walks keep a stack of kStack entries (the 4-wide walk up to 3 per
+    // 4-wide level): a PLOC tree deeper than kPlocMaxDepth is replaced by the
+    // radix hierarchy, whose depth is bounded by the code and index bits.
+    constexpr int kPlocMaxDepth = 40;
+    bool use_radix = in.builder == 1 || n_int == 0;
+    if (!use_radix) {
+        size_t pb = 0;
+        int* cl = alloc<int>(n, st, pb);
+        int* ncl = alloc<int>(n, st, pb);
+        float* cbox = alloc<float>(6 * (size_t) n, st, pb);
+        float* ncbox = alloc<float>(6 * (size_t) n, st, pb);
+        int* nn = alloc<int>(n, st, pb);
+        unsigned long long* flags = alloc<unsigned long long>(n + 1, st, pb);
+        unsigned long long* scan = alloc<unsigned long long>(n + 1, st, pb);
+        int* maxd = alloc<int>(1, st, pb);
+        unsigned long long h_tot = 0;   // scan total: merges << 32 | kept
+        size_t tb = 0;
+        BVH_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, tb, flags, scan, n + 1, st));
+        void* ptmp = alloc<char>(tb, st, pb);
         BVH_CHECK(cudaMemsetAsync(parent_int, 0xff, sizeof(int) * n_int, st));
-        BVH_CHECK(cudaMemsetAsync(arrivals, 0, sizeof(u32) * n_int, st));
-        k_hierarchy<<<(n_int + B - 1) / B, B, 0, st>>>(codes2, n, left, right, parent_int, parent_leaf); note_launch();
+        k_leaf_boxes<<<(n + B - 1) / B, B, 0, st>>>(in.ref_box, ids2, n, leaf_box, cl, cbox); note_launch();
+        BVH_CHECK(cudaGetLastError());
+        int count = n, base = n_int;
+        std::string fail;
+        for (int it = 0; count > 1; ++it) {
+            if (it >= 4 * n + 64) { fail = "bvh: clustering made no progress"; break; }
+            k_ploc_nn<<<(count + kPlocB - 1) / kPlocB, kPlocB, 0, st>>>(count, cbox, nn); note_launch();
+            k_ploc_flags<<<(count + 1 + B - 1) / B, B, 0, st>>>(count, nn, flags); note_launch();
+            BVH_CHECK(cudaGetLastError());
+            size_t tb2 = tb;
+            BVH_CHECK(cub::DeviceScan::ExclusiveSum(ptmp, tb2, flags, scan, count + 1, st));
+            k_ploc_merge<<<(count + B - 1) / B, B, 0, st>>>(count, base, nn, flags, scan, cl, cbox, ncl, ncbox, left, right,
+                                                            parent_int, int_box); note_launch();
+            BVH_CHECK(cudaGetLastError());
+            BVH_CHECK(cudaMemcpyAsync(&h_tot, scan + count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+            note_d2h(sizeof(unsigned long long));
+            BVH_CHECK(cudaStreamSynchronize(st));
+            const int merged = (int) (h_tot >> 32), kept = (int) (h_tot & 0xffffffffull);
+            if (merged <= 0 || kept != count - merged) { fail = "bvh: clustering step inconsistent"; break; }
+            base -= merged;
+            count = kept;
+            std::swap(cl, ncl);
+            std::swap(cbox, ncbox);
+        }
+        if (fail.empty() && base != 0) fail = "bvh: clustering left " + std::to_string(base) + " nodes unnumbered";
+        int depth = 0;
+        if (fail.empty()) {
+            BVH_CHECK(cudaMemsetAsync(maxd, 0, sizeof(int), st));
+            k_max_depth<<<(n_int + B - 1) / B, B, 0, st>>>(n_int, parent_int, maxd); note_launch();
+            BVH_CHECK(cudaGetLastError());
+            BVH_CHECK(cudaMemcpyAsync(&depth, maxd, sizeof(int), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(int));
+            BVH_CHECK(cudaStreamSynchronize(st));
+        }
+        void* pp[] = {cl, ncl, cbox, ncbox, nn, flags, scan, maxd, ptmp};
+        for (void* p : pp) BVH_CHECK(cudaFreeAsync(p, st));
+        if (!fail.empty()) {
+            void* ptrs[] = {codes, codes2, ids, ids2, left, right, parent_int, parent_leaf, leaf_box, int_box, arrivals, temp};
+            for (void* p : ptrs) cudaFreeAsync(p, st);
+            throw std::runtime_error(fail);
+        }
+        use_radix = depth + 1 > kPlocMaxDepth;   // + 1: the leaves below the deepest internal node
+    }
+    if (use_radix) {
+        if (n_int > 0) {
+            BVH_CHECK(cudaMemsetAsync(parent_int, 0xff, sizeof(int) * n_int, st));
+            BVH_CHECK(cudaMemsetAsync(arrivals, 0, sizeof(u32) * n_int, st));
+            k_hierarchy<<<(n_int + B - 1) / B, B, 0, st>>>(codes2, n, left, right, parent_int, parent_leaf); note_launch();
+            BVH_CHECK(cudaGetLastError());
+        }
+        k_refit<<<(n + B - 1) / B, B, 0, st>>>(in.ref_box, ids2, n, parent_leaf, parent_int, left, right, leaf_box, int_box,
+                                                arrivals); note_launch();
         BVH_CHECK(cudaGetLastError());
     }
-    k_refit<<<(n + B - 1) / B, B, 0, st>>>(in.ref_box, ids2, n, parent_leaf, parent_int, left, right, leaf_box, int_box,
-                                            arrivals); note_launch();
-    BVH_CHECK(cudaGetLastError());
 
     out.nodes = alloc<float4>(4 * (size_t) (n_int > 0 ? n_int : 1), st, out.bytes);
     out.tris = alloc<float4>(3 * (size_t) n, st, out.bytes);
@@ -310,7 +499,7 @@ void bvh_build(const BvhBuildInput& in, BvhStorage& out, void* stream)
     }
     // 4-wide nodes (at most one per binary node)
     out.nodes4 = alloc<float4>(8 * (size_t) (n_int > 0 ? n_int : 1), st, out.bytes);
-    out.root4 = n_int > 0 ? 0 : ~0;   // Karras' root is binary node 0, at depth 0: 4-wide node 0
+    out.root4 = n_int > 0 ? 0 : ~0;   // the root is binary node 0 (both builders), at depth 0: 4-wide node 0
     if (n_int > 0) {
         int* flag = alloc<int>(n_int + 1, st, scratch_bytes);
         int* idx4 = alloc<int>(n_int + 1, st, scratch_bytes);

@@ -447,6 +447,7 @@ struct BvhBuildInput {
     const float* ref_box;   // device: exact box of each reference (min xyz, max xyz)
     int n;                  // number of references (leaves)
     float scene_min[3], scene_max[3];   // bounds of the reference box centres
+    int builder = 0;        // 0: locally-ordered clustering (PLOC), 1: Karras' radix hierarchy
 };
 
 struct BvhStorage {

@@ -10,6 +10,8 @@ LTRG_LINKS_VISIBLE = 1
 LTRG_F_FP32 = 0
 LTRG_F_FP16 = 1
 LTRG_F_BF16 = 2
+LTRG_BVH_PLOC = 0
+LTRG_BVH_RADIX = 1
 
 
 class Options(C.Structure):
@@ -20,7 +22,8 @@ class Options(C.Structure):
         ("radiosity_precision", C.c_int),
         ("refine_steps", C.c_int),
         ("radiosity_patches", u32),
-        ("reserved", u32 * 10),
+        ("bvh_builder", u32),
+        ("reserved", u32 * 9),
     ]
 
 

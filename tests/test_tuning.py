@@ -58,6 +58,26 @@ def test_results_do_not_depend_on_launch_shape(gpu):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("desc", [
+    lambda: scenes.mid(5, lm=128, n_boxes=24, n_spheres=3, bounces=1, ao_rays=8),
+    lambda: scenes.cornell(3, lm=32, bounces=1, ao=True),
+])
+def test_results_do_not_depend_on_bvh_builder(gpu, desc):
+    # PLOC and the radix hierarchy give different trees over the same leaves in the
+    # same order; every query (any hit, closest hit with ties to the lower leaf,
+    # nearest distance) and so every texel and AO hit is the same
+    d = desc()
+    a = bake(gpu, d, gpu_options={"bvh_builder": ext.LTRG_BVH_PLOC, "radiosity_patches": 256, "radiosity_links": 1})
+    b = bake(gpu, d, gpu_options={"bvh_builder": ext.LTRG_BVH_RADIX, "radiosity_patches": 256, "radiosity_links": 1})
+    for x, y in zip(a.lightmaps, b.lightmaps):
+        np.testing.assert_array_equal(x[3], y[3])
+    for x, y in zip(a.debug, b.debug):
+        np.testing.assert_array_equal(x["pos"], y["pos"])
+        if "ao" in x:
+            np.testing.assert_array_equal(x["ao"], y["ao"])
+
+
+@pytest.mark.gpu
 def test_autotune_picks_valid_shapes(gpu):
     lib = gpu
     saved = _get(lib)
