@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <exception>
 #include <unordered_map>
 #include <chrono>
 #include <condition_variable>
@@ -1733,51 +1734,61 @@ void run_bake(ltr_Scene* S)
     std::vector<int> inst_tri_off(n_inst + 1, 0);
     for (int t = 0; t < n_tris; ++t) inst_tri_off[(tri_meta[t] & kInstMask) + 1]++;
     for (int i = 0; i < n_inst; ++i) inst_tri_off[i + 1] += inst_tri_off[i];
-    std::vector<RefTree> rtrees(n_inst);
-    {
-        std::vector<std::thread> pool;
-        std::atomic<int> next(1);
-        int nth = std::max(1, std::min({8, (int) std::thread::hardware_concurrency(), n_inst - 1}));
-        for (int t = 0; t < nth; ++t)
-            pool.emplace_back([&]() {
-                for (int i = next++; i < n_inst; i = next++)
-                    build_ref_tree(tri_xyz.data() + 9 * (size_t) inst_tri_off[i],
-                                   (size_t) (inst_tri_off[i + 1] - inst_tri_off[i]), rtrees[i]);
-            });
-        for (auto& th : pool) th.join();
-    }
+    // The reference-shaped trees serve only the sample fixup: they are built on
+    // a side thread while the upload, the BVH build and the raster run, and
+    // joined before the fixup launch.
     std::vector<float4> ref_nodes;
     std::vector<int> ref_items;
     std::vector<int4> ref_inst(n_inst, make_int4(0, 0, 0, 0));
     std::vector<float4> fix_box(2 * (size_t) n_inst);   // root boxes for the fixup's instance culling
-    for (int i = 0; i < n_inst; ++i) {
-        fix_box[2 * i] = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.0f);
-        fix_box[2 * i + 1] = make_float4(-3.0e38f, -3.0e38f, -3.0e38f, 0.0f);
-    }
-    for (int i = 1; i < n_inst; ++i) {
-        const RefTree& rt_i = rtrees[i];
-        if (inst_tri_off[i + 1] == inst_tri_off[i]) continue;
-        if (!rt_i.nodes.empty()) {
-            const RefNode& root = rt_i.nodes[0];
-            fix_box[2 * i] = make_float4(root.mn[0], root.mn[1], root.mn[2], 0.0f);
-            fix_box[2 * i + 1] = make_float4(root.mx[0], root.mx[1], root.mx[2], 0.0f);
+    std::exception_ptr reftree_error;
+    std::thread reftree_thread([&]() {
+        try {
+            std::vector<RefTree> rtrees(n_inst);
+            {
+                std::vector<std::thread> pool;
+                std::atomic<int> next(1);
+                int nth = std::max(1, std::min({8, (int) std::thread::hardware_concurrency(), n_inst - 1}));
+                for (int t = 0; t < nth; ++t)
+                    pool.emplace_back([&]() {
+                        for (int i = next++; i < n_inst; i = next++)
+                            build_ref_tree(tri_xyz.data() + 9 * (size_t) inst_tri_off[i],
+                                           (size_t) (inst_tri_off[i + 1] - inst_tri_off[i]), rtrees[i]);
+                    });
+                for (auto& th : pool) th.join();
+            }
+            for (int i = 0; i < n_inst; ++i) {
+                fix_box[2 * i] = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.0f);
+                fix_box[2 * i + 1] = make_float4(-3.0e38f, -3.0e38f, -3.0e38f, 0.0f);
+            }
+            for (int i = 1; i < n_inst; ++i) {
+                const RefTree& rt_i = rtrees[i];
+                if (inst_tri_off[i + 1] == inst_tri_off[i]) continue;
+                if (!rt_i.nodes.empty()) {
+                    const RefNode& root = rt_i.nodes[0];
+                    fix_box[2 * i] = make_float4(root.mn[0], root.mn[1], root.mn[2], 0.0f);
+                    fix_box[2 * i + 1] = make_float4(root.mx[0], root.mx[1], root.mx[2], 0.0f);
+                }
+                ref_inst[i] = make_int4((int) (ref_nodes.size() / 2), (int) ref_items.size(), inst_tri_off[i],
+                                        (int) rt_i.nodes.size());
+                for (const RefNode& nd : rt_i.nodes) {
+                    float chf, idof;
+                    memcpy(&chf, &nd.ch, 4);
+                    memcpy(&idof, &nd.ido, 4);
+                    ref_nodes.push_back(make_float4(nd.mn[0], nd.mn[1], nd.mn[2], nd.mx[0]));
+                    ref_nodes.push_back(make_float4(nd.mx[1], nd.mx[2], chf, idof));
+                }
+                ref_items.insert(ref_items.end(), rt_i.items.begin(), rt_i.items.end());
+            }
+        } catch (...) {
+            reftree_error = std::current_exception();
         }
-        ref_inst[i] = make_int4((int) (ref_nodes.size() / 2), (int) ref_items.size(), inst_tri_off[i],
-                                (int) rt_i.nodes.size());
-        for (const RefNode& nd : rt_i.nodes) {
-            float chf, idof;
-            memcpy(&chf, &nd.ch, 4);
-            memcpy(&idof, &nd.ido, 4);
-            ref_nodes.push_back(make_float4(nd.mn[0], nd.mn[1], nd.mn[2], nd.mx[0]));
-            ref_nodes.push_back(make_float4(nd.mx[1], nd.mx[2], chf, idof));
-        }
-        ref_items.insert(ref_items.end(), rt_i.items.begin(), rt_i.items.end());
-    }
+    });
+    struct JoinReftree {   // joined on every way out (the thread reads this frame's vectors)
+        std::thread& th;
+        ~JoinReftree() { if (th.joinable()) th.join(); }
+    } join_reftree{reftree_thread};
 
-    // Light culling against instance boxes (ltr_Light::QueryMeshInsts,
-    // lighter.cpp:80-98, 1079-1093): point/spot lights reach instances whose
-    // box meets [pos - range, pos + range]; directional lights reach every
-    // instance with a box; the probe container (instance 0) is always lit.
     const int n_lights = (int) S->lights.size();
     std::vector<unsigned char> lit((size_t) n_lights * n_inst, 0);
     std::vector<DLight> dl(n_lights);
@@ -1892,10 +1903,6 @@ void run_bake(ltr_Scene* S)
     float* d_tri_xyz = A.upload(tri_xyz);
     u32* d_tri_meta = A.upload(tri_meta);
     u32* d_tri_local = A.upload(tri_local);
-    float4* d_ref_nodes = A.upload(ref_nodes);
-    int* d_ref_items = A.upload(ref_items);
-    int4* d_ref_inst = A.upload(ref_inst);
-    float4* d_fix_box = A.upload(fix_box);
     unsigned char* d_lit = A.upload(lit);
     DLight* d_lights = A.upload(dl);
     float* d_rt = A.upload(rt);
@@ -2056,6 +2063,13 @@ void run_bake(ltr_Scene* S)
         CK(cudaGetLastError());
         checkpoint("compaction");
     }
+    reftree_thread.join();
+    TRACE("reference trees joined");
+    if (reftree_error) std::rethrow_exception(reftree_error);
+    float4* d_ref_nodes = A.upload(ref_nodes);
+    int* d_ref_items = A.upload(ref_items);
+    int4* d_ref_inst = A.upload(ref_inst);
+    float4* d_fix_box = A.upload(fix_box);
     if (n_cov) {
         FixupArgs fa;
         fa.bvh = bv;

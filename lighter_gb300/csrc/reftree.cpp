@@ -15,6 +15,7 @@ inline V3 centre(const Box& b) { return (b.mn + b.mx) * 0.5f; }
 struct Builder {
     const Box* boxes;
     RefTree* t;
+    std::vector<float> key;   // per item: centre along the current split axis
 
     void emit(int32_t node, const int32_t* ids, size_t n)
     {
@@ -52,10 +53,11 @@ struct Builder {
                     else self.push_back(ids[i]);
                 }
                 if (!self.empty()) emit(node, self.data(), self.size());
-                const Box* bx = boxes;
-                std::sort(split.begin(), split.end(), [bx, axis](int32_t a, int32_t b) {
-                    return dot(axis, centre(bx[a])) < dot(axis, centre(bx[b]));
-                });
+                // the keys are the values the comparison dot(axis, centre(a)) < dot(axis,
+                // centre(b)) would compute, so std::sort sees the same comparisons
+                for (int32_t id : split) key[id] = dot(axis, centre(boxes[id]));
+                const float* kv = key.data();
+                std::sort(split.begin(), split.end(), [kv](int32_t a, int32_t b) { return kv[a] < kv[b]; });
                 size_t mid = split.size() / 2;
                 t->nodes.push_back(RefNode());
                 make((int32_t) t->nodes.size() - 1, split.data(), mid, depth + 1);
@@ -91,7 +93,7 @@ void build_ref_tree(const float* xyz, size_t n, RefTree& out)
         const Box& bb = boxes[i];
         if (bb.mn.x <= bb.mx.x && bb.mn.y <= bb.mx.y && bb.mn.z <= bb.mx.z) ids.push_back((int32_t) i);
     }
-    Builder bld{boxes.data(), &out};
+    Builder bld{boxes.data(), &out, std::vector<float>(n)};
     bld.make(0, ids.data(), ids.size(), 0);
 }
 
