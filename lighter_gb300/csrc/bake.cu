@@ -1372,6 +1372,12 @@ void build_refs_host(const std::vector<float>& xyz, std::vector<u32>& ref_tri, s
 // stream waits on the launch's completion event. The per-sample rand() draws
 // of AO take turns in scene order, so a batch gives every scene the random
 // offsets it would get from bakes run one after another in that order.
+// A scene of a batch whose trace phase has at least this many work items
+// (pairs or rays) launches that phase alone on its own stream instead of
+// waiting for the others: such a launch fills the GPU by itself, and the
+// scenes' other stages overlap.
+constexpr unsigned long long kBatchSoloItems = 1ull << 22;
+
 struct BatchCtx {
     BatchCtx(int n_, int device_)
         : n(n_), device(device_), rand_done(n_, 0), member(n_, 0), started(n_, 0), cv_turn(n_), cv_start(n_)
@@ -2141,10 +2147,11 @@ void run_bake(ltr_Scene* S)
         u32* d_next = A.zeros<u32>(1);
         int dev_sms = 0;
         CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, S->opt.device));
-        if (batch) {   // one trace launch for the whole batch
+        if (batch && items < kBatchSoloItems) {   // one trace launch for the whole batch
             DirectJob job{da, d_items, d_dscan + items};
             CK(cudaStreamWaitEvent(st, batch->join(0, bidx, st, &job, nullptr, 0), 0));
         } else {
+            if (batch) batch->skip(0, bidx);   // enough pairs to fill the GPU alone
             const ltrg_Tuning tu = get_tuning(S->opt.device);
             unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * tu.direct_blocks_per_sm,
                                                                     (items + tu.direct_block - 1) / tu.direct_block);
@@ -2462,10 +2469,11 @@ void run_bake(ltr_Scene* S)
             int dev_sms = 0;
             CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, S->opt.device));
             const unsigned long long n_items = ao_items(n_samples, aa.ns);
-            if (batch) {   // one trace launch for the whole batch
+            if (batch && n_items < kBatchSoloItems) {   // one trace launch for the whole batch
                 AoJob job{aa, d_hits};
                 CK(cudaStreamWaitEvent(st, batch->join(1, bidx, st, nullptr, &job, n_items), 0));
             } else {
+                if (batch) batch->skip(1, bidx);   // enough rays to fill the GPU alone
                 const ltrg_Tuning tu = get_tuning(S->opt.device);
                 unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * tu.ao_blocks_per_sm,
                                                                         (n_items + tu.ao_block - 1) / tu.ao_block);

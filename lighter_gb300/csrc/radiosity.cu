@@ -59,44 +59,21 @@ __device__ __forceinline__ float pair_pretest(V3 AP, V3 AN, V3 BP, V3 BN)
 // FP16 range. A factor grows as 1 / (pi |d|^2) for close elements, past FP16's
 // largest value (65504) for elements a few millimetres apart, so an FP16 F is
 // stored per row scaled by a power of two: row i holds f * 2^-e_i with e_i in
-// [0, 14] chosen from the row's largest factor (k_ff_rowmax, k_row_scale) so
-// that it stays below 2^15, and values past 65504 (rows that would need
-// e_i > 14) saturate. With e_i <= 14 the smallest linked factor, SMALL_FLOAT,
-// stays above FP16's smallest subnormal (0.001 * 2^-14 > 2^-24), so a factor
-// is zero in FP16 exactly where it is zero in FP32. The bounce multiplies each
-// row's sum by 2^e_i, which is exact: rounding happens only where F is stored.
+// [0, 14] chosen from the row's largest factor so that it stays below 2^15,
+// and values past 65504 (rows that would need e_i > 14) saturate. With
+// e_i <= 14 the smallest linked factor, SMALL_FLOAT, stays above FP16's
+// smallest subnormal (0.001 * 2^-14 > 2^-24), so a factor is zero in FP16
+// exactly where it is zero in FP32. The bounce multiplies each row's sum by
+// 2^e_i, which is exact: rounding happens only where F is stored.
+// Rows that need a scale are rare (close pairs), so k_ff_pretest stores FP16
+// unscaled (saturating) and records the largest factor only of rows that hold
+// one above 2^15 (k_row_scale then gives every other row e_i = 0);
+// k_ff_rescale rewrites just the rows with e_i > 0, before the visibility pass.
 constexpr int kF16MaxExp = 14;
 constexpr float kF16Max = 65504.0f;
+constexpr float kF16Big = 32768.0f;
 
-// rowmax[i] = float bits of max_j f_ij (f >= 0, so unsigned order is float order)
-__global__ void k_ff_rowmax(u32 n, const float4* __restrict__ pos, const float4* __restrict__ nrm,
-                            unsigned* __restrict__ rowmax)
-{
-    __shared__ float tile[32][33];
-    const u32 bi = blockIdx.y, bj = blockIdx.x;
-    if (bj < bi) return;
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    for (int k = 0; k < 4; ++k) {
-        int r = ty + 8 * k;
-        u32 i = bi * 32 + r, j = bj * 32 + tx;
-        float f = 0.0f;
-        if (i < j && j < n) f = pair_pretest(ld3(pos[i]), ld3(nrm[i]), ld3(pos[j]), ld3(nrm[j]));
-        tile[r][tx] = f;
-        float m = f;
-        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
-        if (tx == 0 && m > 0.0f && i < n) atomicMax(&rowmax[i], __float_as_uint(m));
-    }
-    __syncthreads();
-    for (int k = 0; k < 4; ++k) {   // column maxima: row j of the mirrored entries
-        int c = ty + 8 * k;
-        u32 j = bj * 32 + c;
-        float m = tile[tx][c];
-        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
-        if (tx == 0 && m > 0.0f && j < n) atomicMax(&rowmax[j], __float_as_uint(m));
-    }
-}
-
-// up[i] = 2^e_i, e_i = clamp(k - 15, 0, 14) where rowmax < 2^k
+// up[i] = 2^e_i, e_i = clamp(k - 15, 0, 14) where rowmax < 2^k (0 for rows without a big factor)
 __global__ void k_row_scale(u32 n, const unsigned* __restrict__ rowmax, float* __restrict__ up)
 {
     u32 i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -110,16 +87,24 @@ __global__ void k_row_scale(u32 n, const unsigned* __restrict__ rowmax, float* _
 template <class T> __device__ __forceinline__ T store_f(float f, const float* up, u32 row)
 {
     if constexpr (std::is_same<T, __half>::value) {
-        if (up) f = fminf(f / up[row], kF16Max);   // division by a power of two: exact
+        if (up) f = f / up[row];   // division by a power of two: exact
+        f = fminf(f, kF16Max);
     }
     return to_store<T>(f);
+}
+
+// rowmax[i] = float bits of the largest factor of row i when it exceeds 2^15
+// (f >= 0, so unsigned order is float order)
+__device__ __forceinline__ void note_big(unsigned* rowmax, u32 row, float f)
+{
+    if (rowmax && f > kF16Big) atomicMax(&rowmax[row], __float_as_uint(f));
 }
 
 // counts[0]: pairs that passed (appended; entries past `cap` are dropped and
 // the host runs the pass again with room for all of them)
 template <class T>
 __global__ void k_ff_pretest(u32 n, size_t ld, const float4* __restrict__ pos, const float4* __restrict__ nrm,
-                             const float* __restrict__ up, T* __restrict__ F, PairRef* __restrict__ cand,
+                             unsigned* __restrict__ rowmax, T* __restrict__ F, PairRef* __restrict__ cand,
                              unsigned long long cap, unsigned long long* counts)
 {
     __shared__ float tile[32][33];
@@ -149,13 +134,43 @@ __global__ void k_ff_pretest(u32 n, size_t ld, const float4* __restrict__ pos, c
         int r = ty + 8 * k;
         if (bi == bj) {
             u32 i = bi * 32 + r, j = bj * 32 + tx;
-            if (i < n && j < ld) F[(size_t) i * ld + j] = store_f<T>(tile[r][tx] + tile[tx][r], up, i);
+            if (i < n && j < ld) {
+                const float f = tile[r][tx] + tile[tx][r];
+                note_big(rowmax, i, f);
+                F[(size_t) i * ld + j] = store_f<T>(f, nullptr, i);
+            }
         } else {
             u32 i = bi * 32 + r, j = bj * 32 + tx;
-            if (i < n && j < ld) F[(size_t) i * ld + j] = store_f<T>(tile[r][tx], up, i);
+            if (i < n && j < ld) {
+                note_big(rowmax, i, tile[r][tx]);
+                F[(size_t) i * ld + j] = store_f<T>(tile[r][tx], nullptr, i);
+            }
             u32 i2 = bj * 32 + r, j2 = bi * 32 + tx;
-            if (i2 < n && j2 < ld) F[(size_t) i2 * ld + j2] = store_f<T>(tile[tx][r], up, i2);
+            if (i2 < n && j2 < ld) {
+                note_big(rowmax, i2, tile[tx][r]);
+                F[(size_t) i2 * ld + j2] = store_f<T>(tile[tx][r], nullptr, i2);
+            }
         }
+    }
+}
+
+// Rows with a scale (e_i > 0) written again, one warp per row: the factors of
+// k_ff_pretest (lower index first) divided by 2^e_i. Runs before the visibility
+// pass, which then zeroes the rejected pairs in the rescaled rows as well.
+__global__ void k_ff_rescale(u32 n, size_t ld, const float4* __restrict__ pos, const float4* __restrict__ nrm,
+                             const float* __restrict__ up, __half* __restrict__ F)
+{
+    const u32 i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= n || up[i] == 1.0f) return;
+    const V3 ap = ld3(pos[i]), an = ld3(nrm[i]);
+    for (u32 j = lane; j < n; j += 32) {
+        float f = 0.0f;
+        if (j != i) {
+            const V3 bp = ld3(pos[j]), bn = ld3(nrm[j]);
+            f = i < j ? pair_pretest(ap, an, bp, bn) : pair_pretest(bp, bn, ap, an);
+        }
+        F[(size_t) i * ld + j] = store_f<__half>(f, up, i);
     }
 }
 
@@ -345,7 +360,7 @@ __global__ void k_rad_update(u32 n, const float4* __restrict__ Y, float4* __rest
 // the stream once after the first pass, to size the pair list).
 template <class T>
 RadFormFactors build_ff(u32 n, size_t ld, const float4* pos, const float4* nrm, const BvhView& bvh, ErrFlag err,
-                        int links, T* F, const float* up, cudaStream_t st)
+                        int links, T* F, unsigned* rowmax, float* up, cudaStream_t st)
 {
     RadFormFactors out;
     if (n == 0) return out;
@@ -365,7 +380,8 @@ RadFormFactors build_ff(u32 n, size_t ld, const float4* pos, const float4* nrm, 
     for (int attempt = 0; attempt < 2; ++attempt) {
         RCK(cudaMallocAsync(&cand, std::max<unsigned long long>(cap, 1) * sizeof(PairRef), st));
         RCK(cudaMemsetAsync(counts, 0, 3 * sizeof(unsigned long long), st));
-        k_ff_pretest<T><<<dim3(nb, nb), dim3(32, 8), 0, st>>>(n, ld, pos, nrm, up, F, cand, cap, counts); note_launch();
+        if (rowmax) RCK(cudaMemsetAsync(rowmax, 0, n * sizeof(unsigned), st));
+        k_ff_pretest<T><<<dim3(nb, nb), dim3(32, 8), 0, st>>>(n, ld, pos, nrm, rowmax, F, cand, cap, counts); note_launch();
         RCK(cudaGetLastError());
         RCK(cudaMemcpyAsync(&n_cand, counts, sizeof(n_cand), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(n_cand));
         RCK(cudaStreamSynchronize(st));
@@ -375,6 +391,13 @@ RadFormFactors build_ff(u32 n, size_t ld, const float4* pos, const float4* nrm, 
         cap = n_cand;
     }
     if (n_cand > cap) throw std::runtime_error("radiosity: pair list overflow");
+    if constexpr (std::is_same<T, __half>::value) {
+        if (rowmax && up) {
+            k_row_scale<<<(n + 255) / 256, 256, 0, st>>>(n, rowmax, up); note_launch();
+            k_ff_rescale<<<(unsigned) (((size_t) n * 32 + 255) / 256), 256, 0, st>>>(n, ld, pos, nrm, up, F); note_launch();
+            RCK(cudaGetLastError());
+        }
+    }
     if (n_cand) {
         int dev = 0, sms = 0;
         RCK(cudaGetDevice(&dev));
@@ -433,15 +456,10 @@ RadResult solve_t(const RadDevInputs& in, const RadSettings& rs, const BvhView& 
         ~FreeScale() { for (void** q : p) if (*q) cudaFreeAsync(*q, st); }
     } guard_scale{st, {(void**) &up, (void**) &rowmax}};
     if (std::is_same<T, __half>::value) {
-        const u32 nb = (n + 31) / 32;
         RCK(cudaMallocAsync(&up, n * sizeof(float), st));
         RCK(cudaMallocAsync(&rowmax, n * sizeof(unsigned), st));
-        RCK(cudaMemsetAsync(rowmax, 0, n * sizeof(unsigned), st));
-        k_ff_rowmax<<<dim3(nb, nb), dim3(32, 8), 0, st>>>(n, in.pos, in.nrm, rowmax); note_launch();
-        k_row_scale<<<(n + 255) / 256, 256, 0, st>>>(n, rowmax, up); note_launch();
-        RCK(cudaGetLastError());
     }
-    RadFormFactors ff = build_ff<T>(n, ld, in.pos, in.nrm, bvh, err, rs.links, F, up, st);
+    RadFormFactors ff = build_ff<T>(n, ld, in.pos, in.nrm, bvh, err, rs.links, F, rowmax, up, st);
     RCK(cudaEventRecord(e1, st));
     if (rs.f_host) {
         const size_t nn = (size_t) n * n;
@@ -494,7 +512,7 @@ RadResult radiosity_solve_dev(const RadDevInputs& in, const RadSettings& rs, con
 RadFormFactors radiosity_form_factors_f32(uint32_t n, const float4* pos, const float4* nrm, const BvhView& bvh,
                                           ErrFlag err, int links, float* F, cudaStream_t st)
 {
-    return build_ff<float>(n, n, pos, nrm, bvh, err, links, F, nullptr, st);
+    return build_ff<float>(n, n, pos, nrm, bvh, err, links, F, nullptr, nullptr, st);
 }
 
 RadResult radiosity_solve(const RadInputs& in, const RadSettings& rs, const BvhView& bvh, ErrFlag err, cudaStream_t st,
