@@ -214,10 +214,14 @@ typedef struct ltrg_Tuning {
     u32 direct_blocks_per_sm; /* persistent blocks per SM, default 8 */
     u32 ao_block;             /* threads per block of the AO-ray kernel, default 128 */
     u32 ao_blocks_per_sm;     /* default 16 */
-    u32 reserved[8];
+    u32 direct_order;         /* order in which the warps take the shadow-trace pairs of a light:
+                                 0 = sample order, 1 = by lightmap texel (Morton order per instance),
+                                 2 = by position (3D Morton order in the scene bounds); default 2 */
+    u32 ao_order;             /* the same for the AO rays; default 1 */
+    u32 reserved[6];
 } ltrg_Tuning;
 LTRAPI LTRBOOL ltrg_GetTuning(int device, ltrg_Tuning* out);
-/* Values outside 32..512 threads (multiples of 32) or 1..64 blocks per SM are rejected. */
+/* Values outside 32..512 threads (multiples of 32), 1..64 blocks per SM or orders above 2 are rejected. */
 LTRAPI LTRBOOL ltrg_SetTuning(int device, const ltrg_Tuning* t);
 /* Autotuner: bakes `scene` (not running; its device) repeatedly, coordinate
  * descent over the candidate shapes of each kernel, each timed by that

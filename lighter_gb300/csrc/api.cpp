@@ -60,6 +60,8 @@ ltrg_Tuning default_tuning()
     t.direct_blocks_per_sm = 8;
     t.ao_block = 128;
     t.ao_blocks_per_sm = 16;
+    t.direct_order = 2;
+    t.ao_order = 1;
     return t;
 }
 
@@ -67,7 +69,8 @@ bool tuning_valid(const ltrg_Tuning& t)
 {
     auto block_ok = [](u32 b) { return b >= 32 && b <= 512 && b % 32 == 0; };
     auto bps_ok = [](u32 k) { return k >= 1 && k <= 64; };
-    return block_ok(t.direct_block) && block_ok(t.ao_block) && bps_ok(t.direct_blocks_per_sm) && bps_ok(t.ao_blocks_per_sm);
+    return block_ok(t.direct_block) && block_ok(t.ao_block) && bps_ok(t.direct_blocks_per_sm) && bps_ok(t.ao_blocks_per_sm) &&
+           t.direct_order <= 2 && t.ao_order <= 2;
 }
 }  // namespace
 
@@ -388,8 +391,10 @@ LTRAPI LTRBOOL ltrg_Autotune(ltr_Scene* scene, ltrg_Tuning* out)
     const Param params[] = {
         {&ltrg_Tuning::direct_blocks_per_sm, true, {2, 4, 8, 16, 32}},
         {&ltrg_Tuning::direct_block, true, {64, 128, 256}},
+        {&ltrg_Tuning::direct_order, true, {0, 1, 2}},
         {&ltrg_Tuning::ao_blocks_per_sm, false, {4, 8, 16, 32}},
         {&ltrg_Tuning::ao_block, false, {64, 128, 256}},
+        {&ltrg_Tuning::ao_order, false, {0, 1, 2}},
     };
     for (const Param& p : params) {
         for (u32 v : p.cand) {
@@ -423,8 +428,13 @@ LTRAPI LTRBOOL ltrg_Autotune(ltr_Scene* scene, ltrg_Tuning* out)
         if (!(nd < sd * 0.98)) {
             best.direct_block = start.direct_block;
             best.direct_blocks_per_sm = start.direct_blocks_per_sm;
+            best.direct_order = start.direct_order;
         }
-        if (!(na < sa * 0.98)) { best.ao_block = start.ao_block; best.ao_blocks_per_sm = start.ao_blocks_per_sm; }
+        if (!(na < sa * 0.98)) {
+            best.ao_block = start.ao_block;
+            best.ao_blocks_per_sm = start.ao_blocks_per_sm;
+            best.ao_order = start.ao_order;
+        }
     }
     ltrg_SetTuning(dev, &best);
     if (out) *out = best;

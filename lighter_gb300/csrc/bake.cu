@@ -415,6 +415,7 @@ struct DirectArgs {
     float4* ndir;               // [light][sample] normal-map contribution, w = 1 when recorded (may be null)
     Counters* counters;
     float* vis;                 // [light][sample] shadow factor, -1 when not traced (debug record, may be null)
+    const u32* order;           // samples in trace order (see k_order_keys)
 };
 
 // Unshadowed terms of one (light, sample) pair of
@@ -463,13 +464,16 @@ __device__ __forceinline__ bool light_terms(const DirectArgs& a, const DLight& L
 
 // Pass 1 over every (light, sample) pair: zero the outputs and flag the
 // pairs that need a shadow trace (lit instance, positive unshadowed term).
+// flags[v] is indexed in trace order, v = light * n_samples + rank, the pair
+// being w = light * n_samples + order[rank].
 __global__ void k_direct_setup(DirectArgs a, u32* __restrict__ flags)
 {
     unsigned long long total = (unsigned long long) a.n_lights * a.n_samples;
-    for (unsigned long long w = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; w < total;
-         w += (unsigned long long) gridDim.x * blockDim.x) {
-        int l = (int) (w / a.n_samples);
-        u32 s = (u32) (w % a.n_samples);
+    for (unsigned long long v = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; v < total;
+         v += (unsigned long long) gridDim.x * blockDim.x) {
+        int l = (int) (v / a.n_samples);
+        u32 s = a.order ? a.order[v % a.n_samples] : (u32) (v % a.n_samples);
+        const unsigned long long w = (unsigned long long) l * a.n_samples + s;
         const DLight L = a.lights[l];
         u32 inst = a.sinst[s];
         bool go = false;
@@ -480,16 +484,63 @@ __global__ void k_direct_setup(DirectArgs a, u32* __restrict__ flags)
         a.kval[w] = 0.0f;
         if (a.ndir) a.ndir[w] = make_float4(0, 0, 0, 0);
         if (a.vis) a.vis[w] = -1.0f;
-        flags[w] = go ? 1u : 0u;
+        flags[v] = go ? 1u : 0u;
     }
 }
 
-__global__ void k_direct_compact(unsigned long long total, const u32* __restrict__ flags, const u32* __restrict__ scan,
-                                 u32* __restrict__ items)
+// The traced pairs w in trace order.
+__global__ void k_direct_compact(unsigned long long total, u32 n_samples, const u32* __restrict__ order,
+                                 const u32* __restrict__ flags, const u32* __restrict__ scan, u32* __restrict__ items)
 {
-    for (unsigned long long w = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; w < total;
-         w += (unsigned long long) gridDim.x * blockDim.x)
-        if (flags[w]) items[scan[w]] = (u32) w;
+    for (unsigned long long v = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; v < total;
+         v += (unsigned long long) gridDim.x * blockDim.x)
+        if (flags[v]) items[scan[v]] = order ? (u32) ((v / n_samples) * n_samples + order[v % n_samples]) : (u32) v;
+}
+
+// Trace orders of the samples (tuning direct_order / ao_order): the warps of
+// the trace kernels take their pairs and rays in this order, so 32
+// consecutive entries should lie close together. 1: by instance, then by the
+// Morton (Z-order) code of the texel in its lightmap (a compact block of
+// texels instead of a row segment); 2: by the 3D Morton code of the sample
+// position in the scene bounds (close in the world, across charts and
+// instances). 0 keeps the sample order. Outputs stay indexed by sample.
+__device__ __forceinline__ u32 spread16(u32 v)
+{
+    v &= 0xffffu;
+    v = (v | (v << 8)) & 0x00ff00ffu;
+    v = (v | (v << 4)) & 0x0f0f0f0fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+}
+
+__device__ __forceinline__ u32 spread10(u32 v)
+{
+    v &= 0x3ffu;
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+__global__ void k_order_keys(int mode, u32 n, const u32* __restrict__ sinst, const u32* __restrict__ sloc,
+                             const u32* __restrict__ inst_w, const float4* __restrict__ spos, float3 mn, float3 inv_ext,
+                             unsigned long long* __restrict__ keys, u32* __restrict__ vals)
+{
+    for (u32 s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        if (mode == 1) {
+            const u32 inst = sinst[s], w = max(inst_w[inst], 1u), loc = sloc[s];
+            const u32 x = loc % w, y = loc / w;
+            keys[s] = ((unsigned long long) inst << 32) | (spread16(x) | (spread16(y) << 1));
+        } else {
+            const float4 p = spos[s];
+            auto q = [](float v) { return (u32) fminf(fmaxf(v * 1024.0f, 0.0f), 1023.0f); };
+            const u32 x = q((p.x - mn.x) * inv_ext.x), y = q((p.y - mn.y) * inv_ext.y), z = q((p.z - mn.z) * inv_ext.z);
+            keys[s] = (spread10(x) << 2) | (spread10(y) << 1) | spread10(z);
+        }
+        vals[s] = s;
+    }
 }
 
 // Pass 2: persistent warps over the compacted pairs: a warp takes the next 32
@@ -750,6 +801,7 @@ struct AoArgs {
     int ns;
     float aoc[3];
     Counters* counters;
+    const u32* order;   // samples in trace order (see k_order_keys)
 };
 
 // Job_AORender_Inner (lighter.cpp:799-841), pass 1: every (sample, ray) is an
@@ -781,12 +833,14 @@ __host__ __device__ __forceinline__ unsigned long long ao_items(u32 n_samples, i
     return ((unsigned long long) (n_samples + 31) / 32) * 32ull * (unsigned long long) ns;
 }
 
-__device__ __forceinline__ bool ao_item(unsigned long long g, u32 n_samples, int ns, unsigned long long& i)
+__device__ __forceinline__ bool ao_item(unsigned long long g, u32 n_samples, int ns, const u32* order,
+                                        unsigned long long& i)
 {
     const unsigned long long per_tile = 32ull * (unsigned long long) ns;
     const unsigned long long tile = g / per_tile, w = g % per_tile;
-    const unsigned long long s = tile * 32 + w % 32;
-    if (s >= n_samples) return false;
+    const unsigned long long rank = tile * 32 + w % 32;
+    if (rank >= n_samples) return false;
+    const unsigned long long s = order ? order[rank] : rank;
     i = s * (unsigned long long) ns + w / 32;
     return true;
 }
@@ -803,7 +857,7 @@ __global__ void k_ao_rays(AoArgs a, float* __restrict__ hits, unsigned long long
         for (unsigned k = 0; k < kAoChunk; ++k) {
             const unsigned long long g = base + 32ull * k + lane;
             unsigned long long i;
-            if (g < n_items && ao_item(g, a.n_samples, a.ns, i)) {
+            if (g < n_items && ao_item(g, a.n_samples, a.ns, a.order, i)) {
                 ao_ray(a, hits, i);
                 ++c_rays;
             }
@@ -926,7 +980,7 @@ __global__ void k_ao_rays_batch(const AoJob* __restrict__ jobs, int n, const uns
                 job0 = off[k];
             }
             unsigned long long i;
-            if (ao_item(g - job0, a.n_samples, a.ns, i)) {
+            if (ao_item(g - job0, a.n_samples, a.ns, a.order, i)) {
                 ao_ray(a, hits, i);
                 ++c_rays;
             }
@@ -1735,6 +1789,19 @@ void run_bake(ltr_Scene* S)
     }
     const int n_tris = (int) tri_meta.size();
     S->stats.triangles = (uint64_t) n_tris;
+    float gmin[3] = {0, 0, 0}, gmax[3] = {0, 0, 0};   // bounds of all occluder geometry
+    {
+        bool any = false;
+        for (int i = 0; i < n_inst; ++i) {
+            const float* b = &inst_box[6 * i];
+            if (!(b[0] <= b[3] && b[1] <= b[4] && b[2] <= b[5])) continue;
+            for (int c = 0; c < 3; ++c) {
+                gmin[c] = any ? fminf(gmin[c], b[c]) : b[c];
+                gmax[c] = any ? fmaxf(gmax[c], b[3 + c]) : b[3 + c];
+            }
+            any = true;
+        }
+    }
 
     // reference-shaped per-instance trees for the sample-offset pass
     std::vector<int> inst_tri_off(n_inst + 1, 0);
@@ -2069,6 +2136,40 @@ void run_bake(ltr_Scene* S)
         CK(cudaGetLastError());
         checkpoint("compaction");
     }
+    // trace orders of the two trace stages (null: sample order)
+    const u32* d_order_dir = nullptr;
+    const u32* d_order_ao = nullptr;
+    {
+        const ltrg_Tuning tu = get_tuning(S->opt.device);
+        u32* made[3] = {nullptr, nullptr, nullptr};
+        auto order_for = [&](u32 mode) -> const u32* {
+            if (mode == 0 || mode > 2 || !n_samples) return nullptr;
+            if (made[mode]) return made[mode];
+            u32* d_ord = A.alloc<u32>(n_samples);
+            unsigned long long* d_okeys = A.alloc<unsigned long long>(n_samples);
+            unsigned long long* d_okeys2 = A.alloc<unsigned long long>(n_samples);
+            u32* d_ovals = A.alloc<u32>(n_samples);
+            float3 mn = make_float3(gmin[0], gmin[1], gmin[2]);
+            float3 ie = make_float3(gmax[0] > gmin[0] ? 1.0f / (gmax[0] - gmin[0]) : 0.0f,
+                                    gmax[1] > gmin[1] ? 1.0f / (gmax[1] - gmin[1]) : 0.0f,
+                                    gmax[2] > gmin[2] ? 1.0f / (gmax[2] - gmin[2]) : 0.0f);
+            k_order_keys<<<blocks_for(n_samples), kThreads, 0, st>>>((int) mode, n_samples, d_sinst, d_sloc, d_inst_w, d_spos,
+                                                                    mn, ie, d_okeys, d_ovals);
+            note_launch();
+            CK(cudaGetLastError());
+            int end_bit = 32;
+            if (mode == 1)
+                while (end_bit < 64 && ((unsigned long long) n_inst >> (end_bit - 32)) != 0) ++end_bit;
+            size_t tb = 0;
+            CK(cub::DeviceRadixSort::SortPairs(nullptr, tb, d_okeys, d_okeys2, d_ovals, d_ord, (int) n_samples, 0, end_bit, st));
+            void* tmp = A.alloc<char>(tb);
+            CK(cub::DeviceRadixSort::SortPairs(tmp, tb, d_okeys, d_okeys2, d_ovals, d_ord, (int) n_samples, 0, end_bit, st));
+            made[mode] = d_ord;
+            return d_ord;
+        };
+        d_order_dir = order_for(tu.direct_order);
+        d_order_ao = order_for(tu.ao_order);
+    }
     reftree_thread.join();
     TRACE("reference trees joined");
     if (reftree_error) std::rethrow_exception(reftree_error);
@@ -2128,6 +2229,7 @@ void run_bake(ltr_Scene* S)
         da.ndir = d_ndir;
         da.counters = d_cnt;
         da.vis = d_vis;
+        da.order = d_order_dir;
         unsigned long long items = (unsigned long long) n_lights * n_samples;
         if (items >= 0xffffffffull) throw std::runtime_error("too many (light, sample) pairs for one bake");
         u32* d_dflags = A.alloc<u32>(items + 1);
@@ -2140,7 +2242,8 @@ void run_bake(ltr_Scene* S)
         void* tmp = A.alloc<char>(tb);
         CK(cub::DeviceScan::ExclusiveSum(tmp, tb, d_dflags, d_dscan, (int64_t) (items + 1), st));
         u32* d_items = A.alloc<u32>(items);
-        k_direct_compact<<<blocks_for(items), kThreads, 0, st>>>(items, d_dflags, d_dscan, d_items); note_launch();
+        k_direct_compact<<<blocks_for(items), kThreads, 0, st>>>(items, n_samples, d_order_dir, d_dflags, d_dscan, d_items);
+        note_launch();
         CK(cudaGetLastError());
         // persistent grid of a few blocks per SM; the number of traced pairs
         // stays on the device (scan total), so the host does not wait here
@@ -2459,6 +2562,7 @@ void run_bake(ltr_Scene* S)
         aa.mult = cfg.ao_multiplier;
         aa.effect = cfg.ao_effect;
         aa.ns = cfg.ao_num_samples;
+        aa.order = d_order_ao;
         for (int c = 0; c < 3; ++c) aa.aoc[c] = cfg.ao_color_rgb[c];
         aa.counters = d_cnt;
         if (aa.ns > 0) {

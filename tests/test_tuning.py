@@ -28,6 +28,8 @@ def test_tuning_defaults_and_validation(gpu):
         assert lib.ltrg_SetTuning(0, C.byref(bad)) == 0
         bad.direct_block, bad.ao_blocks_per_sm = 64, 0
         assert lib.ltrg_SetTuning(0, C.byref(bad)) == 0
+        bad.ao_blocks_per_sm, bad.ao_order = 8, 3   # no such order
+        assert lib.ltrg_SetTuning(0, C.byref(bad)) == 0
         assert lib.ltrg_SetTuning(-1, C.byref(t)) == 0
         ok = ext.Tuning()
         C.memmove(C.byref(ok), C.byref(t), C.sizeof(t))
@@ -75,6 +77,29 @@ def test_results_do_not_depend_on_bvh_builder(gpu, desc):
         np.testing.assert_array_equal(x["pos"], y["pos"])
         if "ao" in x:
             np.testing.assert_array_equal(x["ao"], y["ao"])
+
+
+@pytest.mark.gpu
+def test_trace_orders_change_no_result(gpu):
+    # direct_order / ao_order only change which warp traces which pair or ray
+    lib = gpu
+    saved = _get(lib)
+    d = scenes.mid(5, lm=128, n_boxes=24, n_spheres=3, bounces=0, ao_rays=8)
+    try:
+        res = {}
+        for order in (0, 1, 2):
+            t = _get(lib)
+            t.direct_order = t.ao_order = order
+            assert lib.ltrg_SetTuning(0, C.byref(t))
+            res[order] = bake(lib, d)
+        for order in (1, 2):
+            for x, y in zip(res[0].lightmaps, res[order].lightmaps):
+                np.testing.assert_array_equal(x[3], y[3])
+            for x, y in zip(res[0].debug, res[order].debug):
+                np.testing.assert_array_equal(x["vis"], y["vis"])
+                np.testing.assert_array_equal(x["ao"], y["ao"])
+    finally:
+        lib.ltrg_SetTuning(0, C.byref(saved))
 
 
 @pytest.mark.gpu
