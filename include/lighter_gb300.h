@@ -218,10 +218,13 @@ typedef struct ltrg_Tuning {
                                  0 = sample order, 1 = by lightmap texel (Morton order per instance),
                                  2 = by position (3D Morton order in the scene bounds); default 2 */
     u32 ao_order;             /* the same for the AO rays; default 1 */
-    u32 reserved[6];
+    u32 direct_regs;          /* 0 = the shadow-trace kernel's registers as compiled, 1 = capped at 64
+                                 (more warps per SM, some spills); default 0 */
+    u32 reserved[5];
 } ltrg_Tuning;
 LTRAPI LTRBOOL ltrg_GetTuning(int device, ltrg_Tuning* out);
-/* Values outside 32..512 threads (multiples of 32), 1..64 blocks per SM or orders above 2 are rejected. */
+/* Values outside 32..512 threads (multiples of 32), 1..64 blocks per SM, orders above 2 or
+ * direct_regs above 1 are rejected. */
 LTRAPI LTRBOOL ltrg_SetTuning(int device, const ltrg_Tuning* t);
 /* Autotuner: bakes `scene` (not running; its device) repeatedly, coordinate
  * descent over the candidate shapes of each kernel, each timed by that

@@ -70,7 +70,7 @@ bool tuning_valid(const ltrg_Tuning& t)
     auto block_ok = [](u32 b) { return b >= 32 && b <= 512 && b % 32 == 0; };
     auto bps_ok = [](u32 k) { return k >= 1 && k <= 64; };
     return block_ok(t.direct_block) && block_ok(t.ao_block) && bps_ok(t.direct_blocks_per_sm) && bps_ok(t.ao_blocks_per_sm) &&
-           t.direct_order <= 2 && t.ao_order <= 2;
+           t.direct_order <= 2 && t.ao_order <= 2 && t.direct_regs <= 1;
 }
 }  // namespace
 
@@ -392,6 +392,7 @@ LTRAPI LTRBOOL ltrg_Autotune(ltr_Scene* scene, ltrg_Tuning* out)
         {&ltrg_Tuning::direct_blocks_per_sm, true, {2, 4, 8, 16, 32}},
         {&ltrg_Tuning::direct_block, true, {64, 128, 256}},
         {&ltrg_Tuning::direct_order, true, {0, 1, 2}},
+        {&ltrg_Tuning::direct_regs, true, {0, 1}},
         {&ltrg_Tuning::ao_blocks_per_sm, false, {4, 8, 16, 32}},
         {&ltrg_Tuning::ao_block, false, {64, 128, 256}},
         {&ltrg_Tuning::ao_order, false, {0, 1, 2}},
@@ -429,6 +430,7 @@ LTRAPI LTRBOOL ltrg_Autotune(ltr_Scene* scene, ltrg_Tuning* out)
             best.direct_block = start.direct_block;
             best.direct_blocks_per_sm = start.direct_blocks_per_sm;
             best.direct_order = start.direct_order;
+            best.direct_regs = start.direct_regs;
         }
         if (!(na < sa * 0.98)) {
             best.ao_block = start.ao_block;

@@ -574,7 +574,11 @@ __device__ __forceinline__ void direct_pair(const DirectArgs& a, u32 w, u32& nq,
     if (a.ndir && a.sinst[s] != 0 && fac > 0) a.ndir[w] = st4(t.dir * fac, 1.0f);
 }
 
-__global__ void k_direct_trace(DirectArgs a, const u32* __restrict__ items, const u32* __restrict__ n_items_dev,
+// kMinBlocks 2 caps the registers at 64 (two blocks of 512 threads per SM):
+// more warps in flight for the latency-bound walks, at the price of a few
+// spills; which is faster depends on the scene (tuning direct_regs).
+template <int kMinBlocks>
+__global__ void __launch_bounds__(512, kMinBlocks) k_direct_trace(DirectArgs a, const u32* __restrict__ items, const u32* __restrict__ n_items_dev,
                                u32* __restrict__ next)
 {
     unsigned long long c_traced = 0, c_nq = 0, c_nv = 0, c_nt = 0;
@@ -2258,7 +2262,11 @@ void run_bake(ltr_Scene* S)
             const ltrg_Tuning tu = get_tuning(S->opt.device);
             unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * tu.direct_blocks_per_sm,
                                                                     (items + tu.direct_block - 1) / tu.direct_block);
-            k_direct_trace<<<grid, tu.direct_block, 0, st>>>(da, d_items, d_dscan + items, d_next); note_launch();
+            if (tu.direct_regs == 1)
+                k_direct_trace<2><<<grid, tu.direct_block, 0, st>>>(da, d_items, d_dscan + items, d_next);
+            else
+                k_direct_trace<1><<<grid, tu.direct_block, 0, st>>>(da, d_items, d_dscan + items, d_next);
+            note_launch();
             CK(cudaGetLastError());
         }
     } else if (batch) {

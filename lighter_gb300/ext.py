@@ -51,7 +51,7 @@ EXT_API = {
 
 class Tuning(C.Structure):
     _fields_ = [("direct_block", u32), ("direct_blocks_per_sm", u32), ("ao_block", u32), ("ao_blocks_per_sm", u32),
-                ("direct_order", u32), ("ao_order", u32), ("reserved", u32 * 6)]
+                ("direct_order", u32), ("ao_order", u32), ("direct_regs", u32), ("reserved", u32 * 5)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
