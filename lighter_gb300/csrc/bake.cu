@@ -56,6 +56,55 @@ void ck(cudaError_t e, const char* what, int line)
 constexpr int kThreads = 256;
 constexpr u32 kNoLoc = 0xffffffffu;
 
+// f(begin, end) over [0, n) in contiguous chunks on up to 16 host threads
+// (one thread below 2 * grain items).
+template <class F>
+void parallel_for(size_t n, size_t grain, F&& f)
+{
+    size_t nt = std::min<size_t>({(size_t) 16, (size_t) std::max(1u, std::thread::hardware_concurrency()),
+                                  (n + grain - 1) / std::max<size_t>(grain, 1)});
+    if (nt <= 1) {
+        if (n) f((size_t) 0, n);
+        return;
+    }
+    const size_t chunk = (n + nt - 1) / nt;
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < nt; ++t) {
+        const size_t b = t * chunk, e = std::min(n, b + chunk);
+        if (b < e) th.emplace_back([&f, b, e]() { f(b, e); });
+    }
+    for (auto& x : th) x.join();
+}
+
+// f(i) for i in [0, n) on up to 16 host threads taking items one at a time;
+// the first exception is rethrown after all threads end.
+template <class F>
+void parallel_items(int n, F&& f)
+{
+    int nt = std::min({16, (int) std::max(1u, std::thread::hardware_concurrency()), n});
+    if (nt <= 1) {
+        for (int i = 0; i < n; ++i) f(i);
+        return;
+    }
+    std::atomic<int> next(0);
+    std::exception_ptr err;
+    std::mutex mu;
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+        th.emplace_back([&]() {
+            for (int i = next++; i < n; i = next++) {
+                try {
+                    f(i);
+                } catch (...) {
+                    std::lock_guard<std::mutex> lk(mu);
+                    if (!err) err = std::current_exception();
+                }
+            }
+        });
+    for (auto& x : th) x.join();
+    if (err) std::rethrow_exception(err);
+}
+
 inline unsigned blocks_for(size_t n, int threads = kThreads, size_t cap = 152 * 64)
 {
     size_t b = (n + threads - 1) / threads;
@@ -1704,7 +1753,7 @@ void keep_pool_memory(int device)
     if (done[device]) return;
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
-        uint64_t keep = 8ull << 30;
+        uint64_t keep = 32ull << 30;
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
     done[device] = 1;
@@ -1751,20 +1800,24 @@ void run_bake(ltr_Scene* S)
     };
     S->stage = "transforming spatial data";
     const int n_inst = (int) S->insts.size();
-    for (int i = 1; i < n_inst; ++i) prexform(S, S->insts[i]);
+    // instances in parallel: the reference too calls size_fn from its pool threads
+    parallel_items(n_inst - 1, [&](int k) { prexform(S, S->insts[k + 1]); });
     check_abort(S);
 
     // ---- host: triangle soup of shadow parts (Job_ColInfo) + instance boxes
     TRACE("prexform done");
     S->stage = "generating data structures";
-    std::vector<float> tri_xyz;
-    std::vector<u32> tri_meta, tri_local;
+    // per instance in parallel, then concatenated in instance order
+    struct InstSoup {
+        std::vector<float> xyz;
+        float smin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, smax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    };
+    std::vector<InstSoup> soup(n_inst);
     std::vector<float> inst_box(6 * n_inst);
-    float smin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, smax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-    for (int i = 0; i < n_inst; ++i) {
+    parallel_items(n_inst, [&](int i) {
         HostInst* mi = S->insts[i];
+        InstSoup& o = soup[i];
         V3 bmn = splat(FLT_MAX), bmx = splat(-FLT_MAX);
-        u32 local = 0;
         if (!mi->container) {
             ltr_Mesh* me = mi->mesh;
             for (const HostPart& p : me->parts) {
@@ -1776,23 +1829,47 @@ void run_bake(ltr_Scene* S)
                     if (near_zero(cross(P2 - P1, P3 - P1))) continue;   // Triangle::CheckIsUseful
                     const V3 ps[3] = {P1, P2, P3};
                     for (const V3& q : ps) {
-                        tri_xyz.push_back(q.x); tri_xyz.push_back(q.y); tri_xyz.push_back(q.z);
+                        o.xyz.push_back(q.x); o.xyz.push_back(q.y); o.xyz.push_back(q.z);
                         bmn = vmin(bmn, q); bmx = vmax(bmx, q);
                     }
                     float cx = (P1.x + P2.x + P3.x) * (1.0f / 3.0f), cy = (P1.y + P2.y + P3.y) * (1.0f / 3.0f),
                           cz = (P1.z + P2.z + P3.z) * (1.0f / 3.0f);
-                    smin[0] = fminf(smin[0], cx); smin[1] = fminf(smin[1], cy); smin[2] = fminf(smin[2], cz);
-                    smax[0] = fmaxf(smax[0], cx); smax[1] = fmaxf(smax[1], cy); smax[2] = fmaxf(smax[2], cz);
-                    tri_meta.push_back((u32) i | (mi->shadow ? kOccluderBit : 0u));
-                    tri_local.push_back(local++);
+                    o.smin[0] = fminf(o.smin[0], cx); o.smin[1] = fminf(o.smin[1], cy); o.smin[2] = fminf(o.smin[2], cz);
+                    o.smax[0] = fmaxf(o.smax[0], cx); o.smax[1] = fmaxf(o.smax[1], cy); o.smax[2] = fmaxf(o.smax[2], cz);
                 }
             }
         }
         inst_box[6 * i + 0] = bmn.x; inst_box[6 * i + 1] = bmn.y; inst_box[6 * i + 2] = bmn.z;
         inst_box[6 * i + 3] = bmx.x; inst_box[6 * i + 4] = bmx.y; inst_box[6 * i + 5] = bmx.z;
+    });
+    std::vector<float> tri_xyz;
+    std::vector<u32> tri_meta, tri_local;
+    float smin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, smax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    {
+        size_t total = 0;
+        for (const InstSoup& o : soup) total += o.xyz.size() / 9;
+        tri_xyz.reserve(9 * total);
+        tri_meta.reserve(total);
+        tri_local.reserve(total);
+        for (int i = 0; i < n_inst; ++i) {
+            const InstSoup& o = soup[i];
+            const u32 nt_i = (u32) (o.xyz.size() / 9);
+            tri_xyz.insert(tri_xyz.end(), o.xyz.begin(), o.xyz.end());
+            const u32 meta = (u32) i | (S->insts[i]->shadow ? kOccluderBit : 0u);
+            for (u32 t = 0; t < nt_i; ++t) {
+                tri_meta.push_back(meta);
+                tri_local.push_back(t);
+            }
+            for (int c = 0; c < 3; ++c) {
+                smin[c] = fminf(smin[c], o.smin[c]);
+                smax[c] = fmaxf(smax[c], o.smax[c]);
+            }
+        }
+        soup.clear();
     }
     const int n_tris = (int) tri_meta.size();
     S->stats.triangles = (uint64_t) n_tris;
+    TRACE("triangle soup done");
     float gmin[3] = {0, 0, 0}, gmax[3] = {0, 0, 0};   // bounds of all occluder geometry
     {
         bool any = false;
@@ -1902,11 +1979,15 @@ void run_bake(ltr_Scene* S)
 
     // Raster records and per-pass bounding boxes (RasterizeInstance /
     // RasterizeTriangle2D_x2_ex set-up, lighter.cpp:32-66, lighter_math.cpp:251-267).
-    std::vector<float> rt;
-    std::vector<u32> rinst;
+    TRACE("light culling done");
+    // Raster records (kRT floats per triangle, in instance / part / triangle
+    // order) and their bounding boxes, filled in parallel over the triangles.
     std::vector<unsigned long long> tex_off(n_inst + 1, 0);
     std::vector<u32> inst_w(n_inst, 0), inst_h(n_inst, 0);
     unsigned long long ntex = 0;
+    struct Seg { int inst; u32 part; size_t first; };   // a part's triangles start at record `first`
+    std::vector<Seg> segs;
+    size_t n_rec = 0;
     for (int i = 0; i < n_inst; ++i) {
         HostInst* mi = S->insts[i];
         tex_off[i] = ntex;
@@ -1914,27 +1995,40 @@ void run_bake(ltr_Scene* S)
         inst_w[i] = mi->w;
         inst_h[i] = mi->h;
         ntex += (unsigned long long) mi->w * mi->h;
-        ltr_Mesh* me = mi->mesh;
-        for (u32 part = 0; part < me->parts.size(); ++part) {
-            const HostPart& p = me->parts[part];
-            const u32* ib = &me->idx[p.ioff];
-            for (u32 t = 0; t + 2 < p.icount; t += 3) {
-                u32 i1 = p.voff + ib[t], i2 = p.voff + ib[t + 1], i3 = p.voff + ib[t + 2];
-                float lmarea = tri_area2(mi->ltex[i1], mi->ltex[i2], mi->ltex[i3]);
-                float coarea = tri_area3(mi->vpos[i1], mi->vpos[i2], mi->vpos[i3]);
-                float sa = lmarea > 0 ? coarea / lmarea : 0;
-                const u32 ids[3] = {i1, i2, i3};
-                for (u32 v : ids) { rt.push_back(mi->ltex[v].x); rt.push_back(mi->ltex[v].y); }
-                for (u32 v : ids) { rt.push_back(mi->vpos[v].x); rt.push_back(mi->vpos[v].y); rt.push_back(mi->vpos[v].z); }
-                for (u32 v : ids) { rt.push_back(mi->vnrm[v].x); rt.push_back(mi->vnrm[v].y); rt.push_back(mi->vnrm[v].z); }
-                for (u32 v : ids) { rt.push_back(mi->vtex[v].x); rt.push_back(mi->vtex[v].y); }
-                rt.push_back((float) part);
-                rt.push_back(sa);
-                rinst.push_back((u32) i);
-            }
+        for (u32 part = 0; part < mi->mesh->parts.size(); ++part) {
+            segs.push_back(Seg{i, part, n_rec});
+            n_rec += mi->mesh->parts[part].icount / 3;
         }
     }
+    std::vector<float> rt(n_rec * kRT);
+    std::vector<u32> rinst(n_rec);
+    parallel_for(n_rec, 4096, [&](size_t k0, size_t k1) {
+        size_t si = std::upper_bound(segs.begin(), segs.end(), k0, [](size_t k, const Seg& g) { return k < g.first; }) -
+                    segs.begin() - 1;
+        for (size_t k = k0; k < k1; ++k) {
+            while (si + 1 < segs.size() && segs[si + 1].first <= k) ++si;
+            const Seg& g = segs[si];
+            HostInst* mi = S->insts[g.inst];
+            const HostPart& p = mi->mesh->parts[g.part];
+            const u32* ib = &mi->mesh->idx[p.ioff];
+            const u32 t = (u32) (k - g.first) * 3;
+            u32 i1 = p.voff + ib[t], i2 = p.voff + ib[t + 1], i3 = p.voff + ib[t + 2];
+            float lmarea = tri_area2(mi->ltex[i1], mi->ltex[i2], mi->ltex[i3]);
+            float coarea = tri_area3(mi->vpos[i1], mi->vpos[i2], mi->vpos[i3]);
+            float sa = lmarea > 0 ? coarea / lmarea : 0;
+            const u32 ids[3] = {i1, i2, i3};
+            float* o = &rt[k * kRT];
+            for (u32 v : ids) { *o++ = mi->ltex[v].x; *o++ = mi->ltex[v].y; }
+            for (u32 v : ids) { *o++ = mi->vpos[v].x; *o++ = mi->vpos[v].y; *o++ = mi->vpos[v].z; }
+            for (u32 v : ids) { *o++ = mi->vnrm[v].x; *o++ = mi->vnrm[v].y; *o++ = mi->vnrm[v].z; }
+            for (u32 v : ids) { *o++ = mi->vtex[v].x; *o++ = mi->vtex[v].y; }
+            *o++ = (float) g.part;
+            *o++ = sa;
+            rinst[k] = (u32) g.inst;
+        }
+    });
     tex_off[n_inst] = ntex;
+    TRACE("raster records done");
     const int n_rt = (int) rinst.size();
     if (n_rt >= (1 << 30) - 1) throw std::runtime_error("too many triangles for the raster keys");
     S->stats.texels = ntex;
@@ -1944,31 +2038,32 @@ void run_bake(ltr_Scene* S)
     for (int pass = 0; pass < 2; ++pass) {
         bbox[pass].resize(n_rt);
         woff[pass].resize(n_rt + 1);
-        unsigned long long acc = 0;
-        for (int k = 0; k < n_rt; ++k) {
-            const float* r = &rt[(size_t) k * kRT];
-            u32 inst = rinst[k];
-            int w = (int) inst_w[inst], h = (int) inst_h[inst];
-            float mg = margins[pass];
-            int maxX = (int) (fmax_(r[0], fmax_(r[2], r[4])) + mg);
-            int minX = (int) (fmin_(r[0], fmin_(r[2], r[4])) - mg);
-            int maxY = (int) (fmax_(r[1], fmax_(r[3], r[5])) + mg);
-            int minY = (int) (fmin_(r[1], fmin_(r[3], r[5])) - mg);
-            bool empty = maxX < 0 || minX >= w || maxY < 0 || minY >= h;
-            if (minX < 0) minX = 0;
-            if (maxX >= w) maxX = w - 1;
-            if (minY < 0) minY = 0;
-            if (maxY >= h) maxY = h - 1;
-            V2 p1 = mk2(r[0], r[1]), p2 = mk2(r[2], r[3]), p3 = mk2(r[4], r[5]);
-            if (cross2(p2 - p1, p3 - p1) == 0) empty = true;
-            if (maxX < minX || maxY < minY) empty = true;
-            woff[pass][k] = acc;
-            if (empty) {
-                bbox[pass][k] = make_int4(0, 0, 1, 0);
-            } else {
-                bbox[pass][k] = make_int4(minX, minY, maxX - minX + 1, maxY - minY + 1);
-                acc += (unsigned long long) (maxX - minX + 1) * (unsigned long long) (maxY - minY + 1);
+        const float mg = margins[pass];
+        parallel_for((size_t) n_rt, 4096, [&](size_t k0, size_t k1) {
+            for (size_t k = k0; k < k1; ++k) {
+                const float* r = &rt[k * kRT];
+                u32 inst = rinst[k];
+                int w = (int) inst_w[inst], h = (int) inst_h[inst];
+                int maxX = (int) (fmax_(r[0], fmax_(r[2], r[4])) + mg);
+                int minX = (int) (fmin_(r[0], fmin_(r[2], r[4])) - mg);
+                int maxY = (int) (fmax_(r[1], fmax_(r[3], r[5])) + mg);
+                int minY = (int) (fmin_(r[1], fmin_(r[3], r[5])) - mg);
+                bool empty = maxX < 0 || minX >= w || maxY < 0 || minY >= h;
+                if (minX < 0) minX = 0;
+                if (maxX >= w) maxX = w - 1;
+                if (minY < 0) minY = 0;
+                if (maxY >= h) maxY = h - 1;
+                V2 p1 = mk2(r[0], r[1]), p2 = mk2(r[2], r[3]), p3 = mk2(r[4], r[5]);
+                if (cross2(p2 - p1, p3 - p1) == 0) empty = true;
+                if (maxX < minX || maxY < minY) empty = true;
+                bbox[pass][k] = empty ? make_int4(0, 0, 1, 0) : make_int4(minX, minY, maxX - minX + 1, maxY - minY + 1);
             }
+        });
+        unsigned long long acc = 0;   // work offsets (texels covered by each box), in order
+        for (int k = 0; k < n_rt; ++k) {
+            woff[pass][k] = acc;
+            const int4 b = bbox[pass][k];
+            if (b.w > 0) acc += (unsigned long long) b.z * (unsigned long long) b.w;
         }
         woff[pass][n_rt] = acc;
     }
@@ -2768,6 +2863,7 @@ void run_bake(ltr_Scene* S)
         }
     }
 
+    TRACE("outputs assembled");
     S->stats.ms_upload = StageClock::ms(e_up0, e_up1);
     S->stats.ms_bvh = StageClock::ms(e_up1, e_bvh);
     S->stats.ms_samples = StageClock::ms(e_bvh, e_samples);
