@@ -41,6 +41,12 @@ ltr_Scene::~ltr_Scene()
     clear_outputs();
     if (pinned) cudaFreeHost(pinned);
     if (ao_pinned) cudaFreeHost(ao_pinned);
+    // the bake's buffers stay cached in the device's memory pool for the next
+    // bake; a destroyed scene gives back what the pool holds beyond 8 GiB
+    // (an error of these calls is cleared: it must not surface in the caller's next CUDA call)
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, opt.device) != cudaSuccess || cudaMemPoolTrimTo(pool, 8ull << 30) != cudaSuccess)
+        (void) cudaGetLastError();
     for (HostInst* mi : insts) delete mi;
     for (ltr_Mesh* m : meshes) delete m;
 }

@@ -1751,9 +1751,17 @@ void keep_pool_memory(int device)
     std::lock_guard<std::mutex> lk(mu);
     if ((int) done.size() <= device) done.resize(device + 1, 0);
     if (done[device]) return;
+    // The pool keeps up to half the device's memory across synchronisations,
+    // so a scene baked again reuses its buffers instead of mapping them anew.
     cudaMemPool_t pool;
+    size_t free_b = 0, total_b = 0;
     if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
-        uint64_t keep = 32ull << 30;
+        uint64_t keep = 8ull << 30;
+        int prev = -1;
+        if (cudaGetDevice(&prev) == cudaSuccess && cudaSetDevice(device) == cudaSuccess) {
+            if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) keep = std::max<uint64_t>(keep, total_b / 2);
+            cudaSetDevice(prev);
+        }
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
     done[device] = 1;
