@@ -593,10 +593,10 @@ __global__ void k_order_keys(int mode, u32 n, const u32* __restrict__ sinst, con
 }
 
 // Pass 2: persistent warps over the compacted pairs: a warp takes the next 32
-// pairs (one light, 32 neighbouring samples), so its lanes walk the BVH along
-// nearby paths. Coherence pays for the lanes that wait on the warp's longest
-// sphere trace (on the mid scene: 26.9 ms instead of 42.5 ms with per-thread
-// fetching).
+// pairs (one light, 32 samples neighbouring in the trace order), so its lanes
+// walk the BVH along nearby paths. Coherence pays for the lanes that wait on
+// the warp's longest sphere trace: per-thread fetching, and lanes refilled
+// from larger per-warp chunks, both measured slower on the mid scene.
 // One traced (light, sample) pair w = light * n_samples + sample.
 __device__ __forceinline__ void direct_pair(const DirectArgs& a, u32 w, u32& nq, u32& nv, u32& nt)
 {
