@@ -283,10 +283,16 @@ __global__ void k_leaf_boxes(const float* ref_box, const u32* ids, int n, float*
     cl[i] = ~i;
 }
 
-__global__ void __launch_bounds__(kPlocB) k_ploc_nn(int count, const float* __restrict__ cbox, int* __restrict__ nn)
+// The cluster count and the next node number live on the device (state[0],
+// state[1]): the host launches every iteration's kernels for the count it last
+// read (an upper bound), and threads past the current count do nothing.
+__global__ void __launch_bounds__(kPlocB) k_ploc_nn(const int* __restrict__ state, const float* __restrict__ cbox,
+                                                    int* __restrict__ nn)
 {
     __shared__ float sb[(kPlocB + 2 * kPlocR) * 6];
+    const int count = state[0];
     const int start = blockIdx.x * kPlocB;
+    if (start >= count) return;
     for (int k = threadIdx.x; k < (kPlocB + 2 * kPlocR) * 6; k += blockDim.x) {
         const long g = (long) start * 6 - kPlocR * 6 + k;
         sb[k] = (g >= 0 && g < (long) count * 6) ? cbox[g] : 0.0f;
@@ -310,12 +316,17 @@ __global__ void __launch_bounds__(kPlocB) k_ploc_nn(int count, const float* __re
 }
 
 // flags[i]: merge (high word: i < nn[i] and mutual), keep (low word: not the
-// upper half of a mutual pair); flags[count] = 0 closes the scan.
-__global__ void k_ploc_flags(int count, const int* __restrict__ nn, unsigned long long* __restrict__ flags)
+// upper half of a mutual pair); zero from the current count up to the bound
+// `ub` the scan runs over. A single cluster keeps itself (an iteration after
+// the root is done changes nothing).
+__global__ void k_ploc_flags(const int* __restrict__ state, int ub, const int* __restrict__ nn,
+                             unsigned long long* __restrict__ flags)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i > count) return;
-    if (i == count) { flags[i] = 0ull; return; }
+    if (i > ub) return;
+    const int count = state[0];
+    if (i >= count) { flags[i] = 0ull; return; }
+    if (count == 1) { flags[i] = 1ull; return; }
     const int j = nn[i];
     const bool mutual = j >= 0 && nn[j] == i;
     const unsigned long long merge = (mutual && i < j) ? 1ull : 0ull;
@@ -323,13 +334,14 @@ __global__ void k_ploc_flags(int count, const int* __restrict__ nn, unsigned lon
     flags[i] = (merge << 32) | keep;
 }
 
-__global__ void k_ploc_merge(int count, int base, const int* __restrict__ nn, const unsigned long long* __restrict__ flags,
+__global__ void k_ploc_merge(const int* __restrict__ state, const int* __restrict__ nn, const unsigned long long* __restrict__ flags,
                              const unsigned long long* __restrict__ scan, const int* __restrict__ cl,
                              const float* __restrict__ cbox, int* __restrict__ ncl, float* __restrict__ ncbox,
                              int* __restrict__ left, int* __restrict__ right, int* __restrict__ parent_int,
                              float* __restrict__ int_box)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int count = state[0], base = state[1];
     if (i >= count) return;
     const unsigned long long f = flags[i];
     if (!(f & 0xffffffffull)) return;   // merged into its lower partner
@@ -358,6 +370,14 @@ __global__ void k_ploc_merge(int count, int base, const int* __restrict__ nn, co
         for (int c = 0; c < 6; ++c) ncbox[6 * (size_t) pos + c] = a[c];
         ncl[pos] = cl[i];
     }
+}
+
+// state = (kept, base - merged) from the scan total at scan[ub]
+__global__ void k_ploc_state(int* __restrict__ state, const unsigned long long* __restrict__ scan, int ub)
+{
+    const unsigned long long tot = scan[ub];
+    state[1] -= (int) (tot >> 32);
+    state[0] = (int) (tot & 0xffffffffull);
 }
 
 // depth (edges from the root) of the deepest internal node
@@ -439,27 +459,39 @@ void bvh_build(const BvhBuildInput& in, BvhStorage& out, void* stream)
         BVH_CHECK(cudaMemsetAsync(parent_int, 0xff, sizeof(int) * n_int, st));
         k_leaf_boxes<<<(n + B - 1) / B, B, 0, st>>>(in.ref_box, ids2, n, leaf_box, cl, cbox); note_launch();
         BVH_CHECK(cudaGetLastError());
-        int count = n, base = n_int;
+        int* state = alloc<int>(2, st, pb);   // device: cluster count, next node number
+        {
+            const int init[2] = {n, n_int};
+            BVH_CHECK(cudaMemcpyAsync(state, init, sizeof(init), cudaMemcpyHostToDevice, st));
+        }
+        int count = n, base = n_int;   // as last read back; count bounds the launches
         std::string fail;
-        for (int it = 0; count > 1; ++it) {
+        constexpr int kItersPerRead = 8;
+        for (int it = 0; count > 1;) {
             if (it >= 4 * n + 64) { fail = "bvh: clustering made no progress"; break; }
-            k_ploc_nn<<<(count + kPlocB - 1) / kPlocB, kPlocB, 0, st>>>(count, cbox, nn); note_launch();
-            k_ploc_flags<<<(count + 1 + B - 1) / B, B, 0, st>>>(count, nn, flags); note_launch();
-            BVH_CHECK(cudaGetLastError());
-            size_t tb2 = tb;
-            BVH_CHECK(cub::DeviceScan::ExclusiveSum(ptmp, tb2, flags, scan, count + 1, st));
-            k_ploc_merge<<<(count + B - 1) / B, B, 0, st>>>(count, base, nn, flags, scan, cl, cbox, ncl, ncbox, left, right,
-                                                            parent_int, int_box); note_launch();
-            BVH_CHECK(cudaGetLastError());
-            BVH_CHECK(cudaMemcpyAsync(&h_tot, scan + count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-            note_d2h(sizeof(unsigned long long));
+            const int ub = count;
+            for (int k = 0; k < kItersPerRead; ++k, ++it) {
+                k_ploc_nn<<<(ub + kPlocB - 1) / kPlocB, kPlocB, 0, st>>>(state, cbox, nn); note_launch();
+                k_ploc_flags<<<(ub + 1 + B - 1) / B, B, 0, st>>>(state, ub, nn, flags); note_launch();
+                BVH_CHECK(cudaGetLastError());
+                size_t tb2 = tb;
+                BVH_CHECK(cub::DeviceScan::ExclusiveSum(ptmp, tb2, flags, scan, ub + 1, st));
+                k_ploc_merge<<<(ub + B - 1) / B, B, 0, st>>>(state, nn, flags, scan, cl, cbox, ncl, ncbox, left, right,
+                                                             parent_int, int_box); note_launch();
+                k_ploc_state<<<1, 1, 0, st>>>(state, scan, ub); note_launch();
+                BVH_CHECK(cudaGetLastError());
+                std::swap(cl, ncl);
+                std::swap(cbox, ncbox);
+            }
+            int hs[2] = {0, 0};
+            BVH_CHECK(cudaMemcpyAsync(hs, state, sizeof(hs), cudaMemcpyDeviceToHost, st));
+            note_d2h(sizeof(hs));
             BVH_CHECK(cudaStreamSynchronize(st));
-            const int merged = (int) (h_tot >> 32), kept = (int) (h_tot & 0xffffffffull);
-            if (merged <= 0 || kept != count - merged) { fail = "bvh: clustering step inconsistent"; break; }
-            base -= merged;
-            count = kept;
-            std::swap(cl, ncl);
-            std::swap(cbox, ncbox);
+            // every merge takes one cluster and one node number, so the next
+            // number is count - 1; with more than one cluster every iteration merges
+            if (hs[0] < 1 || hs[0] >= count || hs[1] != hs[0] - 1) { fail = "bvh: clustering step inconsistent"; break; }
+            count = hs[0];
+            base = hs[1];
         }
         if (fail.empty() && base != 0) fail = "bvh: clustering left " + std::to_string(base) + " nodes unnumbered";
         int depth = 0;
@@ -470,7 +502,7 @@ void bvh_build(const BvhBuildInput& in, BvhStorage& out, void* stream)
             BVH_CHECK(cudaMemcpyAsync(&depth, maxd, sizeof(int), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(int));
             BVH_CHECK(cudaStreamSynchronize(st));
         }
-        void* pp[] = {cl, ncl, cbox, ncbox, nn, flags, scan, maxd, ptmp};
+        void* pp[] = {cl, ncl, cbox, ncbox, nn, flags, scan, maxd, ptmp, state};
         for (void* p : pp) BVH_CHECK(cudaFreeAsync(p, st));
         if (!fail.empty()) {
             void* ptrs[] = {codes, codes2, ids, ids2, left, right, parent_int, parent_leaf, leaf_box, int_box, arrivals, temp};
