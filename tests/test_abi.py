@@ -190,3 +190,26 @@ def test_bake_without_gpu_fails_loudly(gpu):
         pytest.skip("a CUDA device is present")
     with pytest.raises(RuntimeError, match="no CUDA device"):
         bake(gpu, scenes.basic())
+
+
+def test_extension_struct_layouts_match_ctypes():
+    # every field of the extension structs in include/lighter_gb300.h sits where
+    # the ctypes mirror in lighter_gb300/ext.py puts it
+    structs = {"ltrg_Options": ext.Options, "ltrg_Stats": ext.Stats, "ltrg_Tuning": ext.Tuning,
+               "ltrg_GatherStats": ext.GatherStats}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "lighter_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'  printf("{cname}.{f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["  return 0;", "}"]
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = os.path.join(d, "probe.cpp"), os.path.join(d, "probe")
+        open(src, "w").write("\n".join(lines) + "\n")
+        subprocess.run(["g++", "-I", os.path.join(ROOT, "include"), src, "-o", exe], check=True, capture_output=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
+    lay = dict(ln.rsplit(" ", 1) for ln in out.strip().splitlines())
+    for cname, py in structs.items():
+        assert int(lay[cname]) == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert int(lay[f"{cname}.{f}"]) == getattr(py, f).offset, f"{cname}.{f}"
