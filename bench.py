@@ -447,11 +447,15 @@ def run_headline(args, local, single):
             lib.ltr_DestroyScene(h)
     t = statistics.median(times)
     rays = sum(x["shadow_evals"] + x["ao_rays"] + x["rad_vis_rays"] for x in st)
-    spb = statistics.median(x["ms_rad_bounce"] / 2 / 1000.0 for x in st)
+    in_batch = statistics.median(x["ms_rad_bounce"] / 2 / 1000.0 for x in st)
+    solo = (single.get("bake_radiosity_precisions") or {}).get("fp16_refine1", {}).get("s_per_bounce")
     return {
         "workload": HEADLINE_WORKLOAD.format(n=n), "wall_s": t, "rays": rays, "rays_per_s": rays / t,
-        "s_per_bounce": spb,
-        "s_per_bounce_note": "per-scene CUDA-event time of the bounces while the batch's scenes share the GPU",
+        "s_per_bounce": solo,
+        "s_per_bounce_note": "FP16 F with one refinement bounce, one scene baked alone (the same settings as the batch)",
+        "s_per_bounce_in_batch": in_batch,
+        "s_per_bounce_in_batch_note": "per-scene CUDA-event time of the bounces while the batch's other scenes' "
+                                      "trace kernels hold the GPU (waiting included)",
         "plain_fp32_single_scene": {"rays_per_s_e2e": single["e2e"]["value"], "rays_per_s_device": single["value"],
                                     "s_per_bounce": single["s_per_bounce"]},
         "rays_per_s_vs_plain_e2e": rays / t / single["e2e"]["value"],
