@@ -222,6 +222,9 @@ def run_ours(args, world, rank, local, dist):
     return rays, dev_ms, wall, stats, clocks, stats[-1]["bytes_h2d"], stats[-1]["bytes_d2h"], launches, tuning
 
 
+# algorithmic bytes per lightmap texel of the finalize stage: scatter 13, three dilations x 26, two blur passes x 24
+TEXEL_STAGE_BYTES = 13 + 3 * 26 + 2 * 24
+
 # bake radiosity precisions: (name, LTRG_F_*, refine_steps)
 RAD_MODES = (("fp32", 0, 0), ("fp16", 1, 0), ("fp16_refine1", 1, 1), ("bf16", 2, 0), ("bf16_refine1", 2, 1))
 
@@ -555,6 +558,16 @@ def main():
         "clocks": clocks,
         "s_per_bounce": s0["ms_rad_bounce"] / bounces / 1000.0,
         "texels_per_s": s0["samples"] / (s0["ms_device"] / 1000.0),
+        # the texel stage (scatter, three dilations, two blur passes) over every lightmap texel:
+        # scatter 13 B (colour + mask written), a dilation 26 B (colour + mask read and written),
+        # a blur pass 24 B (colour read and written) per texel
+        "texel_roofline": {
+            "bound": "hbm", "kernels": "k_scatter, 3 x k_dilate, 2 x k_conv_t (finalize stage)",
+            "bytes_per_texel": TEXEL_STAGE_BYTES, "texels": s0["texels"],
+            "achieved": s0["texels"] * TEXEL_STAGE_BYTES / (s0["ms_finalize"] / 1000.0) / 1e9 if s0["ms_finalize"] > 0 else 0.0,
+            "peak": peak, "unit": "GB/s", "peak_source": peak_kind,
+            "frac": (s0["texels"] * TEXEL_STAGE_BYTES / (s0["ms_finalize"] / 1000.0) / 1e9 / peak) if s0["ms_finalize"] > 0 else 0.0,
+        },
         "rays_per_step": {"shadow": s0["shadow_evals"], "ao": s0["ao_rays"], "radiosity_visibility": s0["rad_vis_rays"]},
         "distance_queries_per_s": s0["distance_queries"] / (s0["ms_device"] / 1000.0),
         "stages_ms": {k: round(s0[k], 3) for k in ("ms_upload", "ms_bvh", "ms_samples", "ms_direct", "ms_rad_links",
