@@ -6,7 +6,9 @@ boxes and 50 320-triangle icospheres (about 21k triangles), 8 point + 2 spot
 lights, AO 32 rays of 2 m. large: 1024 x 512 terrain quads (1.05M triangles)
 in 16 tiles plus 2000 80-triangle rocks (about 1.2M), 16 lightmaps of 2048^2, 1
 directional + 32 point lights, AO 64 rays. batch: 256 scenes with 200..20k
-triangles, lightmap sides in [64, 512], 1-8 point lights, AO 16 rays.
+triangles, lightmap sides in [64, 512], 1-8 point lights, AO 16 rays. The multi-RHS
+room (C5): 32,768 patches of a furnished room (about 67k triangles), 64 emitter
+subsets as 192 RGB right-hand sides.
 Seeds give the same scene every time.
 """
 import numpy as np
@@ -73,3 +75,21 @@ def test_generators_are_deterministic():
             np.testing.assert_array_equal(pa.positions, pb.positions)
             np.testing.assert_array_equal(pa.indices, pb.indices)
     assert [L.position for L in a.lights] == [L.position for L in b.lights]
+
+
+def test_multi_rhs_room():
+    # the C5 patch set: a furnished room of about 60k triangles, 32,768 patches, 64 emitter
+    # subsets as RGB right-hand sides (R = 192); unit normals, positive areas, albedo U(0.3, 0.8)
+    from lighter_gb300 import patches
+    sc = patches.room(seed=1, n_patches=32768, n_configs=64)
+    n = len(sc["pos"])
+    assert n == 32768 and sc["emission"].shape == (n, 192)
+    assert 50_000 <= len(sc["tri"]) <= 80_000
+    np.testing.assert_allclose(np.linalg.norm(sc["nrm"], axis=1), 1.0, rtol=1e-5)
+    assert (sc["area"] > 0).all()
+    assert sc["albedo"].min() >= 0.3 and sc["albedo"].max() <= 0.8
+    lit = (sc["emission"] > 0).any(axis=0)
+    assert lit.all()                                  # every configuration lights something
+    b = patches.room(seed=1, n_patches=32768, n_configs=64)
+    np.testing.assert_array_equal(sc["pos"], b["pos"])
+    np.testing.assert_array_equal(sc["emission"], b["emission"])
