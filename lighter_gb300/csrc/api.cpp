@@ -37,7 +37,7 @@ void ltr_Scene::clear_outputs()
 
 ltr_Scene::~ltr_Scene()
 {
-    if (worker.joinable()) worker.join();
+    join_worker();
     clear_outputs();
     if (pinned) cudaFreeHost(pinned);
     if (ao_pinned) cudaFreeHost(ao_pinned);
@@ -151,7 +151,7 @@ static void start_bake(ltr_Scene* scene);
 
 LTRAPI void ltr_Start(ltr_Scene* scene)
 {
-    if (scene->worker.joinable()) scene->worker.join();
+    scene->join_worker();
     scene->batch.reset();
     scene->batch_index = -1;
     start_bake(scene);
@@ -168,7 +168,7 @@ LTRAPI LTRBOOL ltrg_StartBatch(ltr_Scene** scenes, u32 count)
             if (scenes[j] == scenes[k]) return 0;
     }
     for (u32 k = 0; k < count; ++k)
-        if (scenes[k]->worker.joinable()) scenes[k]->worker.join();
+        scenes[k]->join_worker();
     std::shared_ptr<BatchCtx> ctx = make_batch((int) count, scenes[0]->opt.device);
     for (u32 k = 0; k < count; ++k) {
         scenes[k]->batch = ctx;
@@ -218,7 +218,7 @@ LTRAPI LTRBOOL ltr_GetStatus(ltr_Scene* scene, ltr_WorkStatus* wsout)
     const char* st = scene->stage.load();
     wsout->completion = scene->completion.load();
     wsout->stage = st ? st : "finished";
-    if (!running && scene->worker.joinable()) scene->worker.join();
+    if (!running) scene->join_worker(false);   // a concurrent poller may be joining it already
     return running ? 1 : 0;
 }
 
@@ -451,7 +451,7 @@ LTRAPI LTRBOOL ltrg_Autotune(ltr_Scene* scene, ltrg_Tuning* out)
 
 LTRAPI LTRBOOL ltrg_Wait(ltr_Scene* scene)
 {
-    if (scene->worker.joinable()) scene->worker.join();
+    scene->join_worker();
     return scene->error.empty() && scene->stage.load() == nullptr ? 1 : 0;
 }
 

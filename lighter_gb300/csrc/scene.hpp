@@ -7,6 +7,7 @@
 #include <atomic>
 #include <memory>
 #include <string>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -98,12 +99,22 @@ struct ltr_Scene {
     std::atomic<bool> abort_flag{false};
     std::atomic<bool> running{false};
     std::thread worker;
+    std::mutex join_mu;                     // serialises joins of `worker` (pollers may run on several threads)
     std::shared_ptr<lg::BatchCtx> batch;   // set for the bake started by ltrg_StartBatch
     int batch_index = -1;
 
     ltr_Scene();
     ~ltr_Scene();
     void clear_outputs();
+    // Joins the bake thread if there is one to join. `wait` false: returns at
+    // once when another thread is joining it.
+    void join_worker(bool wait = true)
+    {
+        std::unique_lock<std::mutex> lk(join_mu, std::defer_lock);
+        if (wait) lk.lock();
+        else if (!lk.try_lock()) return;
+        if (worker.joinable()) worker.join();
+    }
 };
 
 namespace lg {

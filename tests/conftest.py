@@ -7,7 +7,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REF_SRC = "/root/reference"
+# sources of the reference project (read only; absent where the GPU tests run)
+REF_SRC = os.environ.get("LIGHTER_REF_SRC", "/root/reference")
 
 
 def pytest_configure(config):
