@@ -26,6 +26,27 @@ extern "C" {
 #define LTRG_F_FP16 1
 #define LTRG_F_BF16 2
 
+/* How the direct lights' shadows are evaluated (ltrg_Options.shadow_mode). */
+#define LTRG_SHADOW_SPHERE  0   /* the reference's sphere-traced soft-shadow factor per (sample, light)
+                                   (CalcInvShadowFactor, lighter.cpp:190-207); light_radius is its
+                                   penumbra factor and shadow_sample_count is not read */
+#define LTRG_SHADOW_SAMPLED 1   /* shadow_sample_count visibility rays per (sample, light); the shadow
+                                   factor is the fraction of them that reach the light. Directional
+                                   lights: the ray directions of the reference's disabled sampled
+                                   block (lighter.cpp:566-584), i.e. the spiral drawn by ltr_LightAdd
+                                   (lighter.cpp:1295-1312), traced from the sample position over
+                                   `range`, with N.L averaged over the directions. Point and spot
+                                   lights (no reference code): the rays end on a disk of radius
+                                   light_radius around the light, facing the sample, at golden-angle
+                                   spiral points rho = radius * sqrt((s + 0.5) / n), phi = (s +
+                                   randoff) * 137.508 deg, randoff being the light's rand() draw */
+
+/* Segment/triangle test of every ray query (ltrg_Options.intersect_mode). */
+#define LTRG_ISECT_REFERENCE  0  /* IntersectLineSegmentTriangle (lighter_math.cpp:315-354) */
+#define LTRG_ISECT_WATERTIGHT 1  /* watertight test (shear to the ray's dominant axis, edge functions
+                                    with a double-precision retry on exact zeros): no ray passes
+                                    between two triangles that share an edge */
+
 /* Scene BVH builders. */
 #define LTRG_BVH_PLOC  0   /* locally-ordered clustering over the Morton order (closer to a SAH tree) */
 #define LTRG_BVH_RADIX 1   /* Karras' radix-tree hierarchy over the Morton order (faster build) */
@@ -44,7 +65,9 @@ typedef struct ltrg_Options {
                                    gathered (bounced) light on top of its own direct light */
     uint32_t bvh_builder;     /* LTRG_BVH_*: how the scene BVH is built; results do not depend on it,
                                  only the trace times do. Default LTRG_BVH_PLOC */
-    uint32_t reserved[9];
+    uint32_t shadow_mode;     /* LTRG_SHADOW_*, default LTRG_SHADOW_SPHERE */
+    uint32_t intersect_mode;  /* LTRG_ISECT_*, default LTRG_ISECT_REFERENCE */
+    uint32_t reserved[7];
 } ltrg_Options;
 
 /* Per-stage device times (CUDA events on the bake stream) and work counters
@@ -63,7 +86,8 @@ typedef struct ltrg_Stats {
     uint64_t texels;          /* lightmap texels rasterised */
     uint64_t samples;         /* covered texels + probe samples */
     uint64_t triangles;       /* shadow-casting triangles in the BVH */
-    uint64_t shadow_evals;    /* (sample, light) shadow evaluations traced */
+    uint64_t shadow_evals;    /* shadow evaluations traced: one per (sample, light) pair, or one per
+                                 (sample, light, shadow sample) ray with LTRG_SHADOW_SAMPLED */
     uint64_t distance_queries;/* sphere-trace steps (nearest-triangle queries) */
     uint64_t ao_rays;         /* AO segment queries */
     uint64_t rad_pairs;       /* radiosity pairs i<j examined */
@@ -75,6 +99,10 @@ typedef struct ltrg_Stats {
     uint64_t bytes_h2d;       /* host->device bytes copied for the bake */
     uint64_t bytes_d2h;       /* device->host bytes copied for the bake */
     double ms_device;         /* device time from the first kernel to the last (CUDA events) */
+    double ms_direct_trace;   /* the shadow-trace kernel alone (CUDA events around its launch; 0 when
+                                 the scene's pairs were traced in a batch launch) */
+    double ms_ao_trace;       /* the AO-ray kernel alone (0 when traced in a batch launch) */
+    uint64_t shadow_pairs;    /* (sample, light) pairs traced */
     uint64_t reserved[1];
 } ltrg_Stats;
 
@@ -111,9 +139,12 @@ LTRAPI LTRBOOL ltrg_TableSampleFn(ltr_Config* config, ltr_SampleRequest* req);
  * Limits: width*height <= LTRG_NOALLOC_MAX_TEXELS (1024 x 1024) and
  * ceil(blur_size) <= 16. The scratch is one static device array of
  * LTRG_NOALLOC_SCRATCH_BYTES held by every GPU that loads the library until
- * exit; the first call on a device looks up its address (make that call
- * before any stream capture). Calls share the scratch: calls that overlap on
- * the GPU race and must be serialised by the caller.
+ * exit. A call on a stream that is not being captured looks up the array's
+ * device address for the current device and CUDA context; a call under stream
+ * capture reuses the address remembered for that device and context, so make
+ * the first call in each context (per device, and again after a
+ * cudaDeviceReset) before any stream capture. Calls share the scratch: calls
+ * that overlap on the GPU race and must be serialised by the caller.
  * Returns LTRG_NOALLOC_OK or a negative LTRG_NOALLOC_E* code. */
 #define LTRG_NOALLOC_MAX_TEXELS (1u << 20)
 #define LTRG_NOALLOC_SCRATCH_BYTES (2u * LTRG_NOALLOC_MAX_TEXELS + 12u * LTRG_NOALLOC_MAX_TEXELS)
@@ -184,6 +215,14 @@ LTRAPI u32 ltrg_GatherSize(ltrg_Gather* g);
 /* Copies G (n x n FP32, row-major) to host memory. */
 LTRAPI LTRBOOL ltrg_GatherGetG(ltrg_Gather* g, float* out);
 LTRAPI const char* ltrg_GatherLastError(ltrg_Gather* g);
+/* Test hook for the bounded waits of the tensor-core gather: in the next FP16
+ * or BF16 solve of `g`, the kernel's copy producer issues no copies and every
+ * mbarrier wait gives up after about wait_us microseconds (instead of about
+ * 2 s). The waits expire, the kernel records the expiry in its error word,
+ * waits for its own products, frees its tensor memory and returns; that solve
+ * fails with the error word in ltrg_GatherLastError, and later solves run
+ * normally. No GPU fault or hang is involved. wait_us in 1..2000000. */
+LTRAPI LTRBOOL ltrdbg_GatherStallNextSolve(ltrg_Gather* g, u32 wait_us);
 /* B after `bounces` sweeps for R right-hand sides; host buffers:
  *   albedo_rgb n x 3, emission n x R, out n x R (row-major).
  * precision LTRG_F_*, refine LTRG_REFINE_*; for FP16/BF16 R <= 256.
@@ -219,12 +258,27 @@ typedef struct ltrg_Tuning {
                                  2 = by position (3D Morton order in the scene bounds); default 2 */
     u32 ao_order;             /* the same for the AO rays; default 1 */
     u32 direct_regs;          /* 0 = the shadow-trace kernel's registers as compiled, 1 = capped at 64
-                                 (more warps per SM, some spills); default 0 */
-    u32 reserved[5];
+                                 (more warps per SM, some spills), for sphere-traced shadows;
+                                 default 0 */
+    u32 direct_stack;         /* traversal-stack entries per thread kept in shared memory by the
+                                 shadow-trace kernel's per-lane walks (0, 4, 8 or 16; deeper entries
+                                 stay in local memory); default 0 */
+    u32 ao_stack;             /* the same for the AO-ray kernel; default 0 */
+    u32 ao_chunk;             /* AO wavefront: rays per lane per work fetch of a warp (1..8; a warp
+                                 takes 32 x ao_chunk rays); default 1 */
+    u32 direct_packet;        /* 1: the shadow traces of a warp's 32 pairs share each BVH walk (one
+                                 walk for the union of the lanes' query spheres or shadow rays, every
+                                 lane keeping its own radius or segment and result); 0: one walk per
+                                 lane. Same results either way; default 1 */
+    u32 sampled_regs;         /* direct_regs for sampled shadows (LTRG_SHADOW_SAMPLED); default 1 */
+    u32 ao_packet;            /* 1: the 32 AO rays a warp traces at a step share one BVH walk (each
+                                 lane keeping its own segment and closest hit); default 0 */
+    u32 reserved[3];
 } ltrg_Tuning;
 LTRAPI LTRBOOL ltrg_GetTuning(int device, ltrg_Tuning* out);
-/* Values outside 32..512 threads (multiples of 32), 1..64 blocks per SM, orders above 2 or
- * direct_regs above 1 are rejected. */
+/* Values outside 32..512 threads (multiples of 32), 1..64 blocks per SM, orders above 2,
+ * direct_regs, sampled_regs, direct_packet or ao_packet above 1, stacks other than 0, 4, 8 and 16
+ * or ao_chunk outside 1..8 are rejected. */
 LTRAPI LTRBOOL ltrg_SetTuning(int device, const ltrg_Tuning* t);
 /* Autotuner: bakes `scene` (not running; its device) repeatedly, coordinate
  * descent over the candidate shapes of each kernel, each timed by that
@@ -257,6 +311,14 @@ LTRAPI LTRBOOL ltrdbg_GetRayData(ltr_Scene* scene, u32 inst, float* vis, float* 
  * and not kept. */
 LTRAPI LTRBOOL ltrdbg_GetRadiosity(ltr_Scene* scene, u32* n, float* pos4, float* nrm4, float* diff_area4, float* emit4,
                                    float* total4, float* F);
+/* Closest hits of n_segs segments (6 floats each: start, end) against a
+ * triangle soup (n_tris x 9 floats, every triangle an occluder), through the
+ * bake's BVH, traversal and segment test of `intersect_mode` (LTRG_ISECT_*):
+ * out_r[i] = smallest hit fraction in [0, 1] along segment i, or 2 for none.
+ * The segments are traced as given (not shortened). Returns 0 on an error
+ * (message on stderr). */
+LTRAPI LTRBOOL ltrdbg_TraceSegments(const float* tri_xyz, u32 n_tris, const float* seg6, u32 n_segs,
+                                    int intersect_mode, float* out_r, int device);
 /* n values of (float) rand() / RAND_MAX exactly as n rand() calls would give
  * them, leaving the C library's generator where those calls would (the AO
  * stage's bulk draw, exposed for testing). */

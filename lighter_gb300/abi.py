@@ -192,7 +192,14 @@ LTRDBG_API = {
 # Bound where the library has them (the GPU library and the oracle port; not the reference build).
 LTRDBG_OPTIONAL = {
     "ltrdbg_GetRayData": (C.c_int, [C.c_void_p, u32, C.c_void_p, C.c_void_p]),
+    # the oracle port's switch for the modes beyond the reference (shadow_mode,
+    # intersect_mode, radiosity_patches, radiosity_links)
+    "orc_SetOptions": (None, [C.c_void_p, C.POINTER(u32), u32]),
+    "ltrdbg_GetRadiosity": (C.c_int, [C.c_void_p, C.POINTER(u32)] + [C.c_void_p] * 6),
 }
+
+# ltrg_Options fields the oracle port also understands, in orc_SetOptions order.
+ORACLE_OPTIONS = ("shadow_mode", "intersect_mode", "radiosity_patches", "radiosity_links")
 
 
 def bind(lib, table):

@@ -17,7 +17,8 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "liblighter_gb300.so")
 
-SOURCES = ["api.cpp", "bake.cu", "bvh.cu", "radiosity.cu", "reftree.cpp", "noalloc.cu", "gather.cu", "rng.cpp"]
+SOURCES = ["api.cpp", "bake.cu", "bvh.cu", "radiosity.cu", "reftree.cpp", "noalloc.cu", "gather.cu", "rng.cpp",
+           "trace.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false (device) and -ffp-contract=off (host; aarch64 g++ contracts by
 # default) keep a*b+c as two roundings, like the reference's CPU build,

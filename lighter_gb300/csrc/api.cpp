@@ -41,6 +41,7 @@ ltr_Scene::~ltr_Scene()
     clear_outputs();
     if (pinned) cudaFreeHost(pinned);
     if (ao_pinned) cudaFreeHost(ao_pinned);
+    if (abort_alloc) cudaFreeHost(abort_alloc);
     // the bake's buffers stay cached in the device's memory pool for the next
     // bake; a destroyed scene gives back what the pool holds beyond 8 GiB
     // (an error of these calls is cleared: it must not surface in the caller's next CUDA call)
@@ -68,6 +69,9 @@ ltrg_Tuning default_tuning()
     t.ao_blocks_per_sm = 16;
     t.direct_order = 2;
     t.ao_order = 1;
+    t.ao_chunk = 1;
+    t.direct_packet = 1;
+    t.sampled_regs = 1;
     return t;
 }
 
@@ -75,8 +79,11 @@ bool tuning_valid(const ltrg_Tuning& t)
 {
     auto block_ok = [](u32 b) { return b >= 32 && b <= 512 && b % 32 == 0; };
     auto bps_ok = [](u32 k) { return k >= 1 && k <= 64; };
+    auto stack_ok = [](u32 k) { return k == 0 || k == 4 || k == 8 || k == 16; };
     return block_ok(t.direct_block) && block_ok(t.ao_block) && bps_ok(t.direct_blocks_per_sm) && bps_ok(t.ao_blocks_per_sm) &&
-           t.direct_order <= 2 && t.ao_order <= 2 && t.direct_regs <= 1;
+           t.direct_order <= 2 && t.ao_order <= 2 && t.direct_regs <= 1 && stack_ok(t.direct_stack) &&
+           stack_ok(t.ao_stack) && t.ao_chunk >= 1 && t.ao_chunk <= 8 && t.direct_packet <= 1 &&
+           t.sampled_regs <= 1 && t.ao_packet <= 1;
 }
 }  // namespace
 
@@ -93,6 +100,45 @@ static u32 next_pow2(u32 x)
     x |= x >> 1; x |= x >> 2; x |= x >> 4; x |= x >> 8; x |= x >> 16;
     return x + 1;
 }
+
+namespace lg {
+// Golden-angle spiral around `dir` (Vec3::CreateSpiralDirVector,
+// lighter_int.hpp:457-471), in float with the C library's functions.
+static V3 spiral_dir_host(V3 dir, float randoff, int i, int count)
+{
+    float q = (i + 0.5f) / count;
+    float cos_side = std::sqrt(q);
+    float sin_side = std::sin(std::acos(cos_side));
+    float angle = (i + randoff) * (137.508f / 180.0f * (float) M_PI);
+    float cos_around = std::cos(angle);
+    float sin_around = std::sin(angle);
+    V3 diffvec = mk(dir.y, -dir.z, dir.x);
+    V3 up = normalized(cross(dir, diffvec));
+    V3 rt = cross(dir, up);
+    return cos_around * sin_side * rt + sin_around * sin_side * up + cos_side * dir;
+}
+
+std::vector<V3> light_shadow_samples(const HostLight& L)
+{
+    std::vector<V3> out((size_t) L.nsamples);
+    for (int s = 0; s < L.nsamples; ++s) {
+        if (L.type == LTR_LT_DIRECT) {
+            // lighter.cpp:1303-1305: the spiral around -direction pulled towards
+            // +direction by tan((light_radius - 0.5) * pi * 0.999)
+            V3 nd = -L.dir;
+            V3 adj = spiral_dir_host(nd, L.randoff, s, L.nsamples);
+            adj = normalized(adj + nd * std::tan((L.radius - 0.5f) * (float) M_PI * 0.999f));
+            out[s] = adj;
+        } else {
+            // disk point s of the golden-angle spiral of radius light_radius
+            float rho = L.radius * std::sqrt((s + 0.5f) / L.nsamples);
+            float phi = (s + L.randoff) * (137.508f / 180.0f * (float) M_PI);
+            out[s] = mk(rho * std::cos(phi), rho * std::sin(phi), 0.0f);
+        }
+    }
+    return out;
+}
+}  // namespace lg
 
 extern "C" {
 
@@ -207,7 +253,11 @@ static void start_bake(ltr_Scene* scene)
 
 // The reference leaves this empty (lighter.cpp:1154-1157); here the bake
 // stops at the next stage boundary and reports stage "aborted".
-LTRAPI void ltr_Abort(ltr_Scene* scene) { scene->abort_flag = true; }
+LTRAPI void ltr_Abort(ltr_Scene* scene)
+{
+    scene->abort_flag = true;
+    if (u32* w = scene->abort_word.load()) *(volatile u32*) w = 1u;
+}
 
 // Returns 1 while the bake runs (lighter.cpp:1159-1164). A finished bake
 // reports "finished"; a failed or aborted one returns 0 with a stage text
@@ -293,7 +343,7 @@ LTRAPI void ltr_LightAdd(ltr_Scene* scene, ltr_LightInfo* li)
     L.out = li->spot_angle_out;
     L.in = li->spot_angle_in;
     L.curve = li->spot_curve;
-    (void) rand();
+    L.randoff = (float) rand() / (float) RAND_MAX;   // randf(), lighter_int.hpp:271
     scene->lights.push_back(L);
 }
 
@@ -325,7 +375,8 @@ LTRAPI void ltrg_GetOptions(ltr_Scene* scene, ltrg_Options* out) { *out = scene-
 LTRAPI LTRBOOL ltrg_SetOptions(ltr_Scene* scene, const ltrg_Options* o)
 {
     if (o->device < 0 || o->radiosity_links < 0 || o->radiosity_links > 1 || o->radiosity_precision < 0 ||
-        o->radiosity_precision > 2 || o->refine_steps < 0 || o->refine_steps > 16 || o->bvh_builder > 1)
+        o->radiosity_precision > 2 || o->refine_steps < 0 || o->refine_steps > 16 || o->bvh_builder > 1 ||
+        o->shadow_mode > 1 || o->intersect_mode > 1)
         return 0;
     scene->opt = *o;
     return 1;
@@ -399,9 +450,15 @@ LTRAPI LTRBOOL ltrg_Autotune(ltr_Scene* scene, ltrg_Tuning* out)
         {&ltrg_Tuning::direct_block, true, {64, 128, 256}},
         {&ltrg_Tuning::direct_order, true, {0, 1, 2}},
         {&ltrg_Tuning::direct_regs, true, {0, 1}},
+        {&ltrg_Tuning::direct_stack, true, {0, 4, 8, 16}},
+        {&ltrg_Tuning::direct_packet, true, {0, 1}},
+        {&ltrg_Tuning::sampled_regs, true, {0, 1}},
         {&ltrg_Tuning::ao_blocks_per_sm, false, {4, 8, 16, 32}},
         {&ltrg_Tuning::ao_block, false, {64, 128, 256}},
         {&ltrg_Tuning::ao_order, false, {0, 1, 2}},
+        {&ltrg_Tuning::ao_stack, false, {0, 4, 8, 16}},
+        {&ltrg_Tuning::ao_chunk, false, {1, 2, 4, 8}},
+        {&ltrg_Tuning::ao_packet, false, {0, 1}},
     };
     for (const Param& p : params) {
         for (u32 v : p.cand) {
@@ -437,11 +494,17 @@ LTRAPI LTRBOOL ltrg_Autotune(ltr_Scene* scene, ltrg_Tuning* out)
             best.direct_blocks_per_sm = start.direct_blocks_per_sm;
             best.direct_order = start.direct_order;
             best.direct_regs = start.direct_regs;
+            best.direct_stack = start.direct_stack;
+            best.direct_packet = start.direct_packet;
+            best.sampled_regs = start.sampled_regs;
         }
         if (!(na < sa * 0.98)) {
             best.ao_block = start.ao_block;
             best.ao_blocks_per_sm = start.ao_blocks_per_sm;
             best.ao_order = start.ao_order;
+            best.ao_stack = start.ao_stack;
+            best.ao_chunk = start.ao_chunk;
+            best.ao_packet = start.ao_packet;
         }
     }
     ltrg_SetTuning(dev, &best);

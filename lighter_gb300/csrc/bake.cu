@@ -118,6 +118,7 @@ struct DLight {
     int type;
     float pos[3], dir[3], color[3];
     float range, power, radius, out_rad, diff, curve;
+    int ns, soff;   // LTRG_SHADOW_SAMPLED: shadow samples of the light at lsmp[soff .. soff + ns)
 };
 
 // Raster record of one triangle (RasterizeInstance, lighter.cpp:32-66):
@@ -126,7 +127,7 @@ struct DLight {
 constexpr int kRT = 32;
 
 struct Counters {
-    unsigned long long shadow_evals, distance_queries, ao_rays, rad_pairs, rad_vis_rays, node_visits, tri_tests, pad;
+    unsigned long long shadow_evals, distance_queries, ao_rays, rad_pairs, rad_vis_rays, node_visits, tri_tests, shadow_pairs;
 };
 
 // Warp total of a per-thread count, added once per warp; every lane of the
@@ -419,8 +420,9 @@ __global__ void __launch_bounds__(kFixupThreads) k_fixup(FixupArgs a)
 // ----------------------------------------------------------------------------- direct light
 
 // Sphere-traced soft-shadow factor (ltr_Scene::CalcInvShadowFactor, lighter.cpp:190-207).
+template <class Stack>
 __device__ __forceinline__ float inv_shadow(const BvhView& bvh, V3 from, V3 to, float k, ErrFlag err, u32& nq, u32& nv,
-                                            u32& nt)
+                                            u32& nt, Stack& st)
 {
     V3 rd = normalized(to - from);
     float maxt = len(to - from);
@@ -435,10 +437,10 @@ __device__ __forceinline__ float inv_shadow(const BvhView& bvh, V3 from, V3 to, 
     for (float t = 0.001f; t < maxt;) {
         V3 p = from + rd * t;
         float r0 = fminf(kMaxPenumbraSize, reach * 1.0001f + 1e-5f);
-        float h = bvh_distance(bvh, p, r0, err, &nv, &nt);
+        float h = bvh_distance_s(bvh, p, r0, err, st, &nv, &nt);
         ++nq;
         if (!(h < r0) && r0 < kMaxPenumbraSize) {
-            h = bvh_distance(bvh, p, kMaxPenumbraSize, err, &nv, &nt);
+            h = bvh_distance_s(bvh, p, kMaxPenumbraSize, err, st, &nv, &nt);
             ++nq;
         }
         if (h < 0.001f) return 0.0f;
@@ -446,6 +448,50 @@ __device__ __forceinline__ float inv_shadow(const BvhView& bvh, V3 from, V3 to, 
         float step = fmin_(h, kMaxPenumbraStep);
         reach = h + step;
         t += step;
+    }
+    return res;
+}
+
+// inv_shadow for the 32 lanes of a warp at once (every lane calls it; `has`
+// marks the lanes with a pair): each step runs one warp_distance for all lanes
+// still marching, so the lanes walk the BVH together instead of 32 divergent
+// walks. Every lane makes the same queries (points and radii) as inv_shadow
+// and gets the same distances, so the factor is inv_shadow's bit for bit.
+__device__ __forceinline__ float inv_shadow_warp(const BvhView& bvh, bool has, V3 from, V3 to, float k, ErrFlag err,
+                                                 u32& nq, u32& nv, u32& nt)
+{
+    V3 rd = mk(0, 0, 0);
+    float maxt = 0.0f;
+    if (has) {
+        rd = normalized(to - from);
+        maxt = len(to - from);
+    }
+    float res = 1.0f;
+    float reach = kMaxPenumbraSize;
+    float t = 0.001f;
+    bool active = has && t < maxt;
+    while (__any_sync(0xffffffffu, active)) {
+        const V3 p = from + rd * t;
+        const float r0 = fminf(kMaxPenumbraSize, reach * 1.0001f + 1e-5f);
+        float h = warp_distance(bvh, p, r0, active, err, nv, nt);
+        if (active) ++nq;
+        const bool again = active && !(h < r0) && r0 < kMaxPenumbraSize;
+        if (__any_sync(0xffffffffu, again)) {
+            const float h2 = warp_distance(bvh, p, kMaxPenumbraSize, again, err, nv, nt);
+            if (again) { h = h2; ++nq; }
+        }
+        if (active) {
+            if (h < 0.001f) {
+                res = 0.0f;
+                active = false;
+            } else {
+                res = fmin_(res, h / fmin_(t * k, kMaxPenumbraSize));
+                const float step = fmin_(h, kMaxPenumbraStep);
+                reach = h + step;
+                t += step;
+                active = t < maxt;
+            }
+        }
     }
     return res;
 }
@@ -465,6 +511,9 @@ struct DirectArgs {
     Counters* counters;
     float* vis;                 // [light][sample] shadow factor, -1 when not traced (debug record, may be null)
     const u32* order;           // samples in trace order (see k_order_keys)
+    int shadow_mode;            // LTRG_SHADOW_*
+    const float4* lsmp;         // LTRG_SHADOW_SAMPLED: per-light ray directions (directional) or disk offsets
+    const volatile u32* abort_word;   // mapped host word set by ltr_Abort (may be null)
 };
 
 // Unshadowed terms of one (light, sample) pair of
@@ -501,14 +550,99 @@ __device__ __forceinline__ bool light_terms(const DirectArgs& a, const DLight& L
     }
     if (L.type == 3) {
         o.f_dist = 1.0f;
-        o.f_ndotl = fmax_(0.0f, dot(Ldir, SN));
         o.dir = Ldir;
+        if (a.shadow_mode == 1) {
+            // sampled block of Job_LMRender_Direct_Inner (lighter.cpp:566-584): N.L
+            // averaged over the light's ray directions, rays from the sample itself
+            float f = 0.0f;
+            for (int k = 0; k < L.ns; ++k) f += fmax_(0.0f, dot(ld3(a.lsmp[L.soff + k]), SN));
+            o.f_ndotl = f / L.ns;
+            o.from = SP;
+            o.to = SP;
+            return o.f_ndotl > 0.0f;
+        }
+        o.f_ndotl = fmax_(0.0f, dot(Ldir, SN));
         o.to = SP + Ldir * L.range;
         // the reference traces even when N.L = 0; its term is then 0 * vis = 0,
         // so the trace is skipped without changing the result
         return o.f_ndotl > 0.0f;
     }
     return false;
+}
+
+// ltr_Scene::VisibilityTest (lighter.cpp:112-147): an occluder on the segment
+// A -> B shortened by SMALL_FLOAT at both ends.
+template <class Stack>
+__device__ __forceinline__ bool occluded(const BvhView& bvh, V3 A, V3 B, ErrFlag err, Stack& st)
+{
+    V3 dn = normalized(B - A);
+    return bvh_any_hit_s<false>(bvh, A + dn * kSmall, B - dn * kSmall, err, st);
+}
+
+// LTRG_SHADOW_SAMPLED: the fraction of the light's ns shadow rays that reach
+// it. Directional lights: rays from the sample along each stored direction
+// over `range` (lighter.cpp:566-584). Point and spot lights: rays from the
+// offset sample position to the stored disk points, placed on the disk of
+// radius light_radius around the light that faces the sample (basis built
+// from the sample-to-light direction as in CreateSpiralDirVector,
+// lighter_int.hpp:465-467).
+template <class Stack>
+__device__ __forceinline__ float sampled_vis(const DirectArgs& a, const DLight& L, const LightTerms& t, Stack& st)
+{
+    float f = 0.0f;
+    if (L.type == 3) {
+        for (int k = 0; k < L.ns; ++k) {
+            V3 adj = ld3(a.lsmp[L.soff + k]);
+            if (occluded(a.bvh, t.from, t.from + adj * L.range, a.err, st)) f += 1.0f;
+        }
+    } else {
+        V3 dir = t.dir;
+        V3 diffvec = mk(dir.y, -dir.z, dir.x);
+        V3 up = normalized(cross(dir, diffvec));
+        V3 rt = cross(dir, up);
+        V3 Lpos = mk(L.pos[0], L.pos[1], L.pos[2]);
+        for (int k = 0; k < L.ns; ++k) {
+            float4 d = a.lsmp[L.soff + k];
+            V3 T = Lpos + rt * d.x + up * d.y;
+            if (occluded(a.bvh, t.from, T, a.err, st)) f += 1.0f;
+        }
+    }
+    f /= L.ns;
+    return 1.0f - f;
+}
+
+// sampled_vis for the 32 lanes of a warp at once (every lane calls it; `has`
+// marks the lanes with a pair): shadow sample k of every lane's light is
+// traced by one warp_any_hit for all lanes, so neighbouring samples' rays to
+// the same light point share their walk. Same rays, same hit counts, same
+// factor as sampled_vis.
+__device__ __forceinline__ float sampled_vis_warp(const DirectArgs& a, bool has, const DLight& L, const LightTerms& t)
+{
+    const int ns = has ? L.ns : 0;
+    int n_max = ns;
+    for (int o = 16; o > 0; o >>= 1) n_max = max(n_max, __shfl_xor_sync(0xffffffffu, n_max, o));
+    V3 rt = mk(0, 0, 0), up = mk(0, 0, 0);
+    const V3 Lpos = mk(L.pos[0], L.pos[1], L.pos[2]);
+    if (has && L.type != 3) {
+        V3 dir = t.dir;
+        V3 diffvec = mk(dir.y, -dir.z, dir.x);
+        up = normalized(cross(dir, diffvec));
+        rt = cross(dir, up);
+    }
+    float f = 0.0f;
+    for (int k = 0; k < n_max; ++k) {
+        const bool go = k < ns;
+        V3 A = t.from, B = t.from;
+        if (go) {
+            const float4 q = a.lsmp[L.soff + k];
+            B = L.type == 3 ? t.from + ld3(q) * L.range : Lpos + rt * q.x + up * q.y;
+        }
+        const V3 dn = normalized(B - A);
+        if (warp_any_hit(a.bvh, A + dn * kSmall, B - dn * kSmall, go, a.err)) f += 1.0f;
+    }
+    if (!has) return 1.0f;
+    f /= L.ns;
+    return 1.0f - f;
 }
 
 // Pass 1 over every (light, sample) pair: zero the outputs and flag the
@@ -598,14 +732,43 @@ __global__ void k_order_keys(int mode, u32 n, const u32* __restrict__ sinst, con
 // the warp's longest sphere trace: per-thread fetching, and lanes refilled
 // from larger per-warp chunks, both measured slower on the mid scene.
 // One traced (light, sample) pair w = light * n_samples + sample.
-__device__ __forceinline__ void direct_pair(const DirectArgs& a, u32 w, u32& nq, u32& nv, u32& nt)
+__device__ __forceinline__ void direct_pair_finish(const DirectArgs& a, u32 w, const DLight& L, const LightTerms& t,
+                                                   float vis);
+
+template <class Stack>
+__device__ __forceinline__ void direct_pair(const DirectArgs& a, u32 w, u32& nq, u32& nv, u32& nt, Stack& st)
 {
     int l = (int) (w / a.n_samples);
     u32 s = w % a.n_samples;
     const DLight L = a.lights[l];
     LightTerms t;
     light_terms(a, L, s, t);
-    float vis = inv_shadow(a.bvh, t.from, t.to, L.radius, a.err, nq, nv, nt);
+    float vis = a.shadow_mode == 1 ? sampled_vis(a, L, t, st) : inv_shadow(a.bvh, t.from, t.to, L.radius, a.err, nq, nv, nt, st);
+    direct_pair_finish(a, w, L, t, vis);
+}
+
+// The traced pairs of a warp (lanes with has = false take part without a
+// pair), traced together: inv_shadow_warp for sphere-traced shadows,
+// sampled_vis_warp for sampled ones.
+__device__ __forceinline__ void direct_pair_warp(const DirectArgs& a, bool has, u32 w, u32& nq, u32& nv, u32& nt)
+{
+    DLight L = {};
+    LightTerms t;
+    t.from = t.to = t.dir = mk(0, 0, 0);
+    if (has) {
+        L = a.lights[w / a.n_samples];
+        light_terms(a, L, w % a.n_samples, t);
+    }
+    const float vis = a.shadow_mode == 1 ? sampled_vis_warp(a, has, L, t)
+                                         : inv_shadow_warp(a.bvh, has, t.from, t.to, L.radius, a.err, nq, nv, nt);
+    if (has) direct_pair_finish(a, w, L, t, vis);
+}
+
+// Outputs of one traced pair from its shadow factor.
+__device__ __forceinline__ void direct_pair_finish(const DirectArgs& a, u32 w, const DLight& L, const LightTerms& t,
+                                                   float vis)
+{
+    const u32 s = w % a.n_samples;
     if (a.vis) a.vis[w] = vis;
     V3 Lcol = mk(L.color[0], L.color[1], L.color[2]);
     float kv, fac;
@@ -626,29 +789,52 @@ __device__ __forceinline__ void direct_pair(const DirectArgs& a, u32 w, u32& nq,
 // kMinBlocks 2 caps the registers at 64 (two blocks of 512 threads per SM):
 // more warps in flight for the latency-bound walks, at the price of a few
 // spills; which is faster depends on the scene (tuning direct_regs).
-template <int kMinBlocks>
+// kStackK: traversal-stack entries kept in shared memory by the per-lane walks
+// (TStack; tuning direct_stack). kPacket: the shadow traces of a warp's 32
+// pairs run together (inv_shadow_warp, sampled_vis_warp; tuning direct_packet).
+template <int kMinBlocks, int kStackK, bool kPacket>
 __global__ void __launch_bounds__(512, kMinBlocks) k_direct_trace(DirectArgs a, const u32* __restrict__ items, const u32* __restrict__ n_items_dev,
                                u32* __restrict__ next)
 {
-    unsigned long long c_traced = 0, c_nq = 0, c_nv = 0, c_nt = 0;
+    extern __shared__ __align__(16) unsigned char smem[];
+    TStack<kStackK> st = make_stack<kStackK>(smem);
+    unsigned long long c_traced = 0, c_nq = 0, c_nv = 0, c_nt = 0, c_pairs = 0;
     const u32 n_items = *n_items_dev;
     const int lane = threadIdx.x & 31;
     for (;;) {
         u32 base = 0;
-        if (lane == 0) base = atomicAdd(next, 32u);
+        if (lane == 0) {
+            base = atomicAdd(next, 32u);
+            if (a.abort_word && *a.abort_word) base = n_items;   // ltr_Abort: take no more work
+        }
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n_items) break;
         const u32 i = base + lane;
-        if (i < n_items) {
+        if (kPacket) {
+            const bool has = i < n_items;
             u32 nq = 0, nv = 0, nt = 0;
-            direct_pair(a, items[i], nq, nv, nt);
-            c_traced += 1;
+            const u32 w = has ? items[i] : 0u;
+            direct_pair_warp(a, has, w, nq, nv, nt);
+            if (has) {
+                c_traced += a.shadow_mode == 1 ? (unsigned) a.lights[w / a.n_samples].ns : 1u;
+                c_pairs += 1;
+                c_nq += nq;
+                c_nv += nv;
+                c_nt += nt;
+            }
+        } else if (i < n_items) {
+            u32 nq = 0, nv = 0, nt = 0;
+            const u32 w = items[i];
+            direct_pair(a, w, nq, nv, nt, st);
+            c_traced += a.shadow_mode == 1 ? (unsigned) a.lights[w / a.n_samples].ns : 1u;
+            c_pairs += 1;
             c_nq += nq;
             c_nv += nv;
             c_nt += nt;
         }
     }
     if (a.counters) {
+        warp_add(&a.counters->shadow_pairs, c_pairs);
         warp_add(&a.counters->shadow_evals, c_traced);
         warp_add(&a.counters->distance_queries, c_nq);
         warp_add(&a.counters->node_visits, c_nv);
@@ -855,15 +1041,21 @@ struct AoArgs {
     float aoc[3];
     Counters* counters;
     const u32* order;   // samples in trace order (see k_order_keys)
+    const volatile u32* abort_word;   // mapped host word set by ltr_Abort (may be null)
 };
 
 // Job_AORender_Inner (lighter.cpp:799-841), pass 1: every (sample, ray) is an
-// independent closest-hit query; persistent warps take 32 x kAoChunk rays at a
-// time (see ao_item for their order) and store the hit fractions.
-constexpr unsigned kAoChunk = 4;
+// independent closest-hit query; persistent warps take 32 x ao_chunk rays at a
+// time (see ao_item for their order) and store the hit fractions. One ray per
+// lane per fetch measured fastest (mid scene: 9.2 ms against 16.0 ms with four):
+// a lane that ends its ray early waits for the warp's longest ray only once
+// instead of running ahead into its next ray on a diverged path. The batch
+// kernel takes kAoChunk rays per lane as well.
+constexpr unsigned kAoChunk = 1;
 
 // Ray r of sample s (i = s * ns + r): closest-hit fraction along the AO segment.
-__device__ __forceinline__ void ao_ray(const AoArgs& a, float* __restrict__ hits, unsigned long long i)
+template <class Stack>
+__device__ __forceinline__ void ao_ray(const AoArgs& a, float* __restrict__ hits, unsigned long long i, Stack& st)
 {
     u32 s = (u32) (i / a.ns);
     int r = (int) (i % a.ns);
@@ -872,7 +1064,7 @@ __device__ __forceinline__ void ao_ray(const AoArgs& a, float* __restrict__ hits
     V3 rd = spiral_dir(SN, a.randoff[s], r, a.ns) * a.dist;
     V3 B = ro + rd;
     V3 dn = normalized(B - ro);
-    hits[i] = bvh_closest(a.bvh, ro + dn * kSmall, B - dn * kSmall, a.err, nullptr);
+    hits[i] = bvh_closest_s(a.bvh, ro + dn * kSmall, B - dn * kSmall, a.err, nullptr, st);
 }
 
 // AO work items in sample-tile order: tiles of 32 consecutive samples, and in a
@@ -898,25 +1090,130 @@ __device__ __forceinline__ bool ao_item(unsigned long long g, u32 n_samples, int
     return true;
 }
 
-__global__ void k_ao_rays(AoArgs a, float* __restrict__ hits, unsigned long long n_items, unsigned long long* next)
+// AO ray of item g for every lane of a warp at once (warp_closest); lanes
+// whose item is past the end or past the samples take part without a ray.
+__device__ __forceinline__ bool ao_ray_warp(const AoArgs& a, float* __restrict__ hits, unsigned long long g,
+                                            unsigned long long n_items)
 {
+    unsigned long long i = 0;
+    const bool has = g < n_items && ao_item(g, a.n_samples, a.ns, a.order, i);
+    V3 A = mk(0, 0, 0), B = mk(0, 0, 0);
+    if (has) {
+        const u32 s = (u32) (i / a.ns);
+        const int r = (int) (i % a.ns);
+        const V3 SP = ld3(a.spos[s]), SN = ld3(a.snrm[s]);
+        const V3 ro = SP + SN * (kSmall * 2);
+        const V3 rd = spiral_dir(SN, a.randoff[s], r, a.ns) * a.dist;
+        const V3 E = ro + rd;
+        const V3 dn = normalized(E - ro);
+        A = ro + dn * kSmall;
+        B = E - dn * kSmall;
+    }
+    const float h = warp_closest(a.bvh, A, B, has, a.err);
+    if (has) hits[i] = h;
+    return has;
+}
+
+// kStackK: traversal-stack entries kept in shared memory (TStack; tuning
+// ao_stack); `chunk`: rays per lane per work fetch (tuning ao_chunk);
+// kPacket: the warp's 32 rays of a step share one walk (ao_ray_warp; tuning
+// ao_packet).
+template <int kStackK, bool kPacket = false>
+__global__ void k_ao_rays(AoArgs a, float* __restrict__ hits, unsigned long long n_items, unsigned long long* next,
+                          unsigned chunk)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    TStack<kStackK> st = make_stack<kStackK>(smem);
     const int lane = threadIdx.x & 31;
     unsigned long long c_rays = 0;
-    for (;;) {
+    for (u32 fetch = 0;; ++fetch) {
         unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(next, 32ull * kAoChunk);
+        if (lane == 0) {
+            base = atomicAdd(next, 32ull * chunk);
+            // ltr_Abort: take no more work (polled every 16th fetch: an AO fetch is short)
+            if (a.abort_word && (fetch & 15u) == 0 && *a.abort_word) base = n_items;
+        }
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n_items) break;
-        for (unsigned k = 0; k < kAoChunk; ++k) {
+        for (unsigned k = 0; k < chunk; ++k) {
             const unsigned long long g = base + 32ull * k + lane;
+            if (kPacket) {
+                if (ao_ray_warp(a, hits, g, n_items)) ++c_rays;
+                continue;
+            }
             unsigned long long i;
             if (g < n_items && ao_item(g, a.n_samples, a.ns, a.order, i)) {
-                ao_ray(a, hits, i);
+                ao_ray(a, hits, i, st);
                 ++c_rays;
             }
         }
     }
     if (a.counters) warp_add(&a.counters->ao_rays, c_rays);
+}
+
+// Launch of the two trace kernels with the tuning's register budget, stack
+// split, walk sharing and wavefront size. Dynamic shared memory: the short
+// stacks, K entries of 8 bytes per thread.
+template <int kMinBlocks, int K, bool kPacket = false>
+void launch_direct_k(unsigned grid, unsigned block, cudaStream_t st, const DirectArgs& da, const u32* items,
+                     const u32* n_items, u32* next)
+{
+    const size_t smem = (size_t) K * block * 8;
+    if (smem > 48 * 1024)
+        CK(cudaFuncSetAttribute(k_direct_trace<kMinBlocks, K, kPacket>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int) smem));
+    k_direct_trace<kMinBlocks, K, kPacket><<<grid, block, smem, st>>>(da, items, n_items, next);
+}
+
+template <int kMinBlocks>
+void launch_direct_r(unsigned stack, bool packet, unsigned grid, unsigned block, cudaStream_t st, const DirectArgs& da,
+                     const u32* items, const u32* n_items, u32* next)
+{
+    if (packet) {   // the warp's walks share one stack in registers; the shared-memory split does not apply
+        launch_direct_k<kMinBlocks, 0, true>(grid, block, st, da, items, n_items, next);
+        return;
+    }
+    switch (stack) {
+    case 4: launch_direct_k<kMinBlocks, 4>(grid, block, st, da, items, n_items, next); break;
+    case 8: launch_direct_k<kMinBlocks, 8>(grid, block, st, da, items, n_items, next); break;
+    case 16: launch_direct_k<kMinBlocks, 16>(grid, block, st, da, items, n_items, next); break;
+    default: launch_direct_k<kMinBlocks, 0>(grid, block, st, da, items, n_items, next); break;
+    }
+}
+
+void launch_direct_trace(const ltrg_Tuning& tu, unsigned grid, cudaStream_t st, const DirectArgs& da, const u32* items,
+                         const u32* n_items, u32* next)
+{
+    const bool packet = tu.direct_packet != 0;
+    const u32 regs = da.shadow_mode == LTRG_SHADOW_SAMPLED ? tu.sampled_regs : tu.direct_regs;
+    if (regs == 1) launch_direct_r<2>(tu.direct_stack, packet, grid, tu.direct_block, st, da, items, n_items, next);
+    else launch_direct_r<1>(tu.direct_stack, packet, grid, tu.direct_block, st, da, items, n_items, next);
+}
+
+template <int K, bool kPacket = false>
+void launch_ao_k(unsigned grid, unsigned block, cudaStream_t st, const AoArgs& aa, float* hits,
+                 unsigned long long n_items, unsigned long long* next, unsigned chunk)
+{
+    const size_t smem = (size_t) K * block * 8;
+    if (smem > 48 * 1024)
+        CK(cudaFuncSetAttribute(k_ao_rays<K, kPacket>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+    k_ao_rays<K, kPacket><<<grid, block, smem, st>>>(aa, hits, n_items, next, chunk);
+}
+
+void launch_ao_rays(const ltrg_Tuning& tu, unsigned grid, cudaStream_t st, const AoArgs& aa, float* hits,
+                    unsigned long long n_items, unsigned long long* next)
+{
+    const unsigned chunk = tu.ao_chunk ? tu.ao_chunk : kAoChunk;
+    if (tu.ao_packet) {   // one shared walk per step: the shared-memory stack split does not apply
+        launch_ao_k<0, true>(grid, tu.ao_block, st, aa, hits, n_items, next, chunk);
+        return;
+    }
+    switch (tu.ao_stack) {
+    case 4: launch_ao_k<4>(grid, tu.ao_block, st, aa, hits, n_items, next, chunk); break;
+    case 8: launch_ao_k<8>(grid, tu.ao_block, st, aa, hits, n_items, next, chunk); break;
+    case 16: launch_ao_k<16>(grid, tu.ao_block, st, aa, hits, n_items, next, chunk); break;
+    default: launch_ao_k<0>(grid, tu.ao_block, st, aa, hits, n_items, next, chunk); break;
+    }
 }
 
 // ----------------------------------------------------------------------------- batches of scenes
@@ -959,22 +1256,23 @@ __global__ void k_direct_batch_offsets(const DirectJob* __restrict__ jobs, int n
 }
 
 __device__ __forceinline__ void flush_direct(Counters* c, unsigned long long& tr, unsigned long long& nq,
-                                             unsigned long long& nv, unsigned long long& nt)
+                                             unsigned long long& nv, unsigned long long& nt, unsigned long long& np)
 {
     if (c && tr) {
+        atomicAdd(&c->shadow_pairs, np);
         atomicAdd(&c->shadow_evals, tr);
         atomicAdd(&c->distance_queries, nq);
         atomicAdd(&c->node_visits, nv);
         atomicAdd(&c->tri_tests, nt);
     }
-    tr = nq = nv = nt = 0;
+    tr = nq = nv = nt = np = 0;
 }
 
 __global__ void k_direct_trace_batch(const DirectJob* __restrict__ jobs, int n, const unsigned long long* __restrict__ off,
                                      unsigned long long* __restrict__ next)
 {
     const unsigned long long total = off[n];
-    unsigned long long c_traced = 0, c_nq = 0, c_nv = 0, c_nt = 0;
+    unsigned long long c_traced = 0, c_nq = 0, c_nv = 0, c_nt = 0, c_pairs = 0;
     int cur = -1;
     DirectArgs a;
     const u32* items = nullptr;
@@ -989,20 +1287,23 @@ __global__ void k_direct_trace_batch(const DirectJob* __restrict__ jobs, int n, 
         if (g >= total) continue;
         const int k = find_job(off, n, g);
         if (k != cur) {
-            if (cur >= 0) flush_direct(a.counters, c_traced, c_nq, c_nv, c_nt);
+            if (cur >= 0) flush_direct(a.counters, c_traced, c_nq, c_nv, c_nt, c_pairs);
             cur = k;
             a = jobs[k].args;
             items = jobs[k].items;
             base = off[k];
         }
         u32 nq = 0, nv = 0, nt = 0;
-        direct_pair(a, items[g - base], nq, nv, nt);
-        c_traced += 1;
+        const u32 w = items[g - base];
+        TStack<0> st;
+        direct_pair(a, w, nq, nv, nt, st);
+        c_traced += a.shadow_mode == 1 ? (unsigned) a.lights[w / a.n_samples].ns : 1u;
+        c_pairs += 1;
         c_nq += nq;
         c_nv += nv;
         c_nt += nt;
     }
-    if (cur >= 0) flush_direct(a.counters, c_traced, c_nq, c_nv, c_nt);
+    if (cur >= 0) flush_direct(a.counters, c_traced, c_nq, c_nv, c_nt, c_pairs);
 }
 
 __global__ void k_ao_rays_batch(const AoJob* __restrict__ jobs, int n, const unsigned long long* __restrict__ off,
@@ -1034,7 +1335,8 @@ __global__ void k_ao_rays_batch(const AoJob* __restrict__ jobs, int n, const uns
             }
             unsigned long long i;
             if (ao_item(g - job0, a.n_samples, a.ns, a.order, i)) {
-                ao_ray(a, hits, i);
+                TStack<0> st;
+                ao_ray(a, hits, i, st);
                 ++c_rays;
             }
         }
@@ -1787,6 +2089,14 @@ void run_bake(ltr_Scene* S)
     if (S->opt.device >= ndev) throw std::runtime_error("ltrg_Options.device out of range");
     CK(cudaSetDevice(S->opt.device));
     keep_pool_memory(S->opt.device);
+    // the abort word (see ltr_Scene::abort_word): 0, published, then the flag read again
+    if (!S->abort_alloc) CK(cudaHostAlloc(&S->abort_alloc, 64, cudaHostAllocMapped | cudaHostAllocPortable));
+    u32* abort_host = (u32*) S->abort_alloc;
+    *(volatile u32*) abort_host = 0u;
+    S->abort_word.store(abort_host);
+    if (S->abort_flag.load()) *(volatile u32*) abort_host = 1u;
+    u32* d_abort = nullptr;
+    CK(cudaHostGetDevicePointer((void**) &d_abort, abort_host, 0));
     if (batch) {
         batch->acquire_start(bidx);
         batch_leave_end.slot = true;
@@ -1802,9 +2112,15 @@ void run_bake(ltr_Scene* S)
     const bool trace_on = getenv("LTRG_TRACE") != nullptr;
     const auto t_start = std::chrono::steady_clock::now();
     auto TRACE = [&](const char* what) {
-        if (trace_on)
-            fprintf(stderr, "[ltrg] %9.3f ms  %s\n",
-                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count(), what);
+        if (!trace_on) return;
+        const auto now = std::chrono::steady_clock::now();
+        if (batch)   // scene index and time since the batch started, for merging the scenes' lines
+            fprintf(stderr, "[ltrg s%d] %9.3f ms (batch %9.3f ms)  %s\n", bidx,
+                    std::chrono::duration<double, std::milli>(now - t_start).count(),
+                    std::chrono::duration<double, std::milli>(now - batch->t0).count(), what);
+        else
+            fprintf(stderr, "[ltrg] %9.3f ms  %s\n", std::chrono::duration<double, std::milli>(now - t_start).count(),
+                    what);
     };
     S->stage = "transforming spatial data";
     const int n_inst = (int) S->insts.size();
@@ -1954,9 +2270,14 @@ void run_bake(ltr_Scene* S)
     const int n_lights = (int) S->lights.size();
     std::vector<unsigned char> lit((size_t) n_lights * n_inst, 0);
     std::vector<DLight> dl(n_lights);
+    std::vector<float4> lsmp;   // shadow samples of every light (LTRG_SHADOW_SAMPLED)
     for (int l = 0; l < n_lights; ++l) {
         const HostLight& L = S->lights[l];
         DLight& d = dl[l];
+        d.ns = L.nsamples;
+        d.soff = (int) lsmp.size();
+        if (S->opt.shadow_mode == LTRG_SHADOW_SAMPLED)
+            for (const V3& v : light_shadow_samples(L)) lsmp.push_back(make_float4(v.x, v.y, v.z, 0.0f));
         d.type = (int) L.type;
         d.pos[0] = L.pos.x; d.pos[1] = L.pos.y; d.pos[2] = L.pos.z;
         d.dir[0] = L.dir.x; d.dir[1] = L.dir.y; d.dir[2] = L.dir.z;
@@ -2120,6 +2441,7 @@ void run_bake(ltr_Scene* S)
     bvh_build(bin, bvh, st);
     struct BvhGuard { BvhStorage* b; cudaStream_t s; ~BvhGuard() { bvh_free(*b, s); } } bvh_guard{&bvh, st};
     BvhView bv = bvh.view();
+    bv.watertight = S->opt.intersect_mode == LTRG_ISECT_WATERTIGHT ? 1 : 0;
     cudaEvent_t e_bvh = clock.mark();
     // LTRG_VALIDATE=1: re-check the BVH topology after every stage
     const bool validate = getenv("LTRG_VALIDATE") && getenv("LTRG_VALIDATE")[0] == '1';
@@ -2307,6 +2629,7 @@ void run_bake(ltr_Scene* S)
     }
     TRACE("fixup issued");
     cudaEvent_t e_samples = clock.mark();
+    cudaEvent_t e_dtr0 = nullptr, e_dtr1 = nullptr, e_aotr0 = nullptr, e_aotr1 = nullptr;   // the trace kernels alone
     check_abort(S);
 
     // ---- direct light (Int_LMRender per light)
@@ -2337,6 +2660,9 @@ void run_bake(ltr_Scene* S)
         da.counters = d_cnt;
         da.vis = d_vis;
         da.order = d_order_dir;
+        da.shadow_mode = (int) S->opt.shadow_mode;
+        da.lsmp = lsmp.empty() ? nullptr : A.upload(lsmp);
+        da.abort_word = d_abort;
         unsigned long long items = (unsigned long long) n_lights * n_samples;
         if (items >= 0xffffffffull) throw std::runtime_error("too many (light, sample) pairs for one bake");
         u32* d_dflags = A.alloc<u32>(items + 1);
@@ -2365,12 +2691,11 @@ void run_bake(ltr_Scene* S)
             const ltrg_Tuning tu = get_tuning(S->opt.device);
             unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * tu.direct_blocks_per_sm,
                                                                     (items + tu.direct_block - 1) / tu.direct_block);
-            if (tu.direct_regs == 1)
-                k_direct_trace<2><<<grid, tu.direct_block, 0, st>>>(da, d_items, d_dscan + items, d_next);
-            else
-                k_direct_trace<1><<<grid, tu.direct_block, 0, st>>>(da, d_items, d_dscan + items, d_next);
+            e_dtr0 = clock.mark();
+            launch_direct_trace(tu, grid, st, da, d_items, d_dscan + items, d_next);
             note_launch();
             CK(cudaGetLastError());
+            e_dtr1 = clock.mark();
         }
     } else if (batch) {
         batch->skip(0, bidx);
@@ -2674,6 +2999,7 @@ void run_bake(ltr_Scene* S)
         aa.effect = cfg.ao_effect;
         aa.ns = cfg.ao_num_samples;
         aa.order = d_order_ao;
+        aa.abort_word = d_abort;
         for (int c = 0; c < 3; ++c) aa.aoc[c] = cfg.ao_color_rgb[c];
         aa.counters = d_cnt;
         if (aa.ns > 0) {
@@ -2692,8 +3018,10 @@ void run_bake(ltr_Scene* S)
                 const ltrg_Tuning tu = get_tuning(S->opt.device);
                 unsigned grid = (unsigned) std::min<unsigned long long>((unsigned long long) dev_sms * tu.ao_blocks_per_sm,
                                                                         (n_items + tu.ao_block - 1) / tu.ao_block);
-                k_ao_rays<<<grid, tu.ao_block, 0, st>>>(aa, d_hits, n_items, d_next); note_launch();
+                e_aotr0 = clock.mark();
+                launch_ao_rays(tu, grid, st, aa, d_hits, n_items, d_next); note_launch();
                 CK(cudaGetLastError());
+                e_aotr1 = clock.mark();
             }
             k_ao<<<blocks_for(n_samples), kThreads, 0, st>>>(aa, d_hits); note_launch();
             CK(cudaGetLastError());
@@ -2823,6 +3151,9 @@ void run_bake(ltr_Scene* S)
     cudaEvent_t e_down = clock.mark();
     CK(cudaStreamSynchronize(st));
     TRACE("readback done");
+    // the host queues the whole bake and waits here; an ltr_Abort during that
+    // wait stopped the trace kernels early, so their outputs are incomplete
+    check_abort(S);
     static const char* kStageName[4] = {"sample fixup", "direct light", "radiosity", "ambient occlusion"};
     for (int k = 0; k < 4; ++k) {
         if (!err_words[k]) continue;
@@ -2877,6 +3208,9 @@ void run_bake(ltr_Scene* S)
     S->stats.ms_samples = StageClock::ms(e_bvh, e_samples);
     S->stats.ms_direct = StageClock::ms(e_samples, e_direct);
     S->stats.ms_ao = StageClock::ms(e_ao0, e_ao1);
+    S->stats.ms_direct_trace = e_dtr0 ? StageClock::ms(e_dtr0, e_dtr1) : 0.0;
+    S->stats.ms_ao_trace = e_aotr0 ? StageClock::ms(e_aotr0, e_aotr1) : 0.0;
+    S->stats.shadow_pairs = cnt.shadow_pairs;
     S->stats.ms_finalize = StageClock::ms(e_ao1, e_fin);
     S->stats.ms_download = StageClock::ms(e_fin, e_down);
     S->stats.shadow_evals = cnt.shadow_evals;

@@ -38,6 +38,7 @@ struct BvhView {
     int root;        // >= 0 internal node, < 0 leaf (single triangle)
     const float4* nodes4;   // 4-wide nodes (see below)
     int root4;              // >= 0 4-wide node, < 0 leaf
+    int watertight;         // segment queries use seg_tri_wt instead of the reference's test
 };
 
 // 4-wide nodes, used by the any-hit walk: the binary nodes at even depth with
@@ -64,6 +65,62 @@ struct ErrFlag { u32* word; };
 __device__ __forceinline__ void raise_err(ErrFlag e, u32 bit)
 {
     if (e.word) atomicOr(e.word, bit);
+}
+
+// Traversal stack of one thread: entries (node, entry key) with the first K
+// in shared memory -- this thread's column of a K x blockDim array, so the 32
+// lanes of a warp hit 32 different banks -- and deeper entries in local
+// memory. K = 0 keeps the whole stack in local memory. The walks push only
+// when both children qualify, so most walks stay within a few entries; which
+// K is fastest is a per-device tuning choice (ltrg_Tuning.direct_stack /
+// ao_stack). A push past kStack entries records error bit 0 and drops the entry.
+template <int K>
+struct TStack {
+    int* sn;
+    float* sk;
+    int stride;
+    int sp = 0;
+    int ln[kStack - K];
+    float lk[kStack - K];
+    __device__ __forceinline__ TStack(int* s_n, float* s_k, int st) : sn(s_n), sk(s_k), stride(st) {}
+    __device__ __forceinline__ void push(int n, float k, ErrFlag err)
+    {
+        if (sp < K) { sn[sp * stride] = n; sk[sp * stride] = k; }
+        else if (sp < kStack) { ln[sp - K] = n; lk[sp - K] = k; }
+        else { raise_err(err, 1u); return; }
+        ++sp;
+    }
+    __device__ __forceinline__ void pop(int& n, float& k)
+    {
+        --sp;
+        if (sp < K) { n = sn[sp * stride]; k = sk[sp * stride]; }
+        else { n = ln[sp - K]; k = lk[sp - K]; }
+    }
+};
+
+template <>
+struct TStack<0> {
+    int sp = 0;
+    int ln[kStack];
+    float lk[kStack];
+    __device__ __forceinline__ TStack() {}
+    __device__ __forceinline__ TStack(int*, float*, int) {}
+    __device__ __forceinline__ void push(int n, float k, ErrFlag err)
+    {
+        if (sp < kStack) { ln[sp] = n; lk[sp] = k; ++sp; }
+        else raise_err(err, 1u);
+    }
+    __device__ __forceinline__ void pop(int& n, float& k) { --sp; n = ln[sp]; k = lk[sp]; }
+};
+
+// This thread's short stack over the block's dynamic shared memory (K x
+// blockDim node ids, then K x blockDim keys: K x blockDim x 8 bytes).
+template <int K>
+__device__ __forceinline__ TStack<K> make_stack(unsigned char* smem)
+{
+    int* sn = reinterpret_cast<int*>(smem) + threadIdx.x;
+    float* sk = reinterpret_cast<float*>(smem + (size_t) K * blockDim.x * sizeof(int)) + threadIdx.x;
+    return TStack<K>(sn, sk, (int) blockDim.x);
 }
 
 __device__ __forceinline__ void load_tri(const BvhView& b, int t, V3& P1, V3& P2, V3& P3, u32& meta, u32& local)
@@ -171,18 +228,16 @@ struct Near4 {
 // not in small ones (the 67k-triangle room of the gather: 64 -> 76 ms); the
 // short AO rays and the sphere-trace queries are faster on the binary nodes,
 // whose two-box tests prune more tightly.
-template <class Leaf>
-__device__ __forceinline__ void walk_segment4(const BvhView& b, V3 o, V3 e, ErrFlag err, Leaf&& leaf)
+template <class Stack, class Leaf>
+__device__ __forceinline__ void walk_segment4(const BvhView& b, V3 o, V3 e, ErrFlag err, Stack& st, Leaf&& leaf)
 {
+    st.sp = 0;
     if (b.n_tris <= 0) return;
     V3 d = e - o;
     V3 inv = inv_dir(d);
     V3 oinv = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
     float tlimit = 1.0f;
     if (b.root4 < 0) { leaf(~b.root4, tlimit); return; }
-    int stack[kStack];
-    float stack_t[kStack];
-    int sp = 0;
     int cur = b.root4;
     for (;;) {
         const Node4 nd = load_node4(b, cur);
@@ -204,40 +259,32 @@ __device__ __forceinline__ void walk_segment4(const BvhView& b, V3 o, V3 e, ErrF
         // visit the nearest internal child now, the others later (farthest pushed first);
         // the leaf tests may have shrunk the limit
         near.sort();
-        auto push = [&](float t, int c) {
-            if (t <= tlimit) {
-                if (sp < kStack) { stack[sp] = c; stack_t[sp] = t; ++sp; }
-                else raise_err(err, 1u);
-            }
-        };
-        push(near.k3, near.c3);
-        push(near.k2, near.c2);
-        push(near.k1, near.c1);
+        if (near.k3 <= tlimit) st.push(near.c3, near.k3, err);
+        if (near.k2 <= tlimit) st.push(near.c2, near.k2, err);
+        if (near.k1 <= tlimit) st.push(near.c1, near.k1, err);
         if (near.k0 <= tlimit) { cur = near.c0; continue; }
         // pop, dropping subtrees whose entry lies beyond the (shrunken) limit
         for (;;) {
-            if (sp == 0) return;
-            --sp;
-            if (stack_t[sp] <= tlimit) break;
+            if (st.sp == 0) return;
+            float k;
+            st.pop(cur, k);
+            if (k <= tlimit) break;
         }
-        cur = stack[sp];
     }
 }
 
 // Generic segment walk: visits leaves whose boxes the segment [o, e] enters
 // before `tlimit` (updated by the leaf functor), nearer child first.
 // Leaf functor: bool f(int tri, float& tlimit) -> false stops the walk.
-template <class Leaf>
-__device__ __forceinline__ void walk_segment(const BvhView& b, V3 o, V3 e, ErrFlag err, Leaf&& leaf)
+template <class Stack, class Leaf>
+__device__ __forceinline__ void walk_segment(const BvhView& b, V3 o, V3 e, ErrFlag err, Stack& st, Leaf&& leaf)
 {
     if (b.n_tris <= 0) return;
     V3 d = e - o;
     V3 inv = inv_dir(d);
     V3 oinv = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
     float tlimit = 1.0f;
-    int stack[kStack];
-    float stack_t[kStack];
-    int sp = 0;
+    st.sp = 0;
     int cur = b.root;
     for (;;) {
         if (cur >= 0) {
@@ -247,8 +294,7 @@ __device__ __forceinline__ void walk_segment(const BvhView& b, V3 o, V3 e, ErrFl
             bool hr = slab(nb.rmin, nb.rmax, oinv, inv, tlimit, tr);
             if (hl && hr) {
                 bool lfirst = tl <= tr;
-                if (sp < kStack) { stack[sp] = lfirst ? nb.r : nb.l; stack_t[sp] = lfirst ? tr : tl; ++sp; }
-                else raise_err(err, 1u);
+                st.push(lfirst ? nb.r : nb.l, lfirst ? tr : tl, err);
                 cur = lfirst ? nb.l : nb.r;
                 continue;
             }
@@ -259,11 +305,11 @@ __device__ __forceinline__ void walk_segment(const BvhView& b, V3 o, V3 e, ErrFl
         }
         // pop, dropping subtrees whose entry lies beyond the (shrunken) limit
         for (;;) {
-            if (sp == 0) return;
-            --sp;
-            if (stack_t[sp] <= tlimit) break;
+            if (st.sp == 0) return;
+            float k;
+            st.pop(cur, k);
+            if (k <= tlimit) break;
         }
-        cur = stack[sp];
     }
 }
 
@@ -318,33 +364,54 @@ __device__ __forceinline__ float point_tri_dist_rec(const BvhView& b, int t, V3 
     return pd;
 }
 
+// Segment test of leaf t: the reference's (from the leaf's record) or the
+// watertight one (from the leaf's vertices), per the view's mode.
+__device__ __forceinline__ float seg_leaf(const BvhView& b, V3 o, V3 e, int t, u32& meta)
+{
+    if (b.watertight) {
+        const float4 a = __ldg(&b.tris[3 * (size_t) t]), c = __ldg(&b.tris[3 * (size_t) t + 1]),
+                     d = __ldg(&b.tris[3 * (size_t) t + 2]);
+        meta = __float_as_uint(a.w);
+        return seg_tri_wt(o, e, mk(a.x, a.y, a.z), mk(c.x, c.y, c.z), mk(d.x, d.y, d.z));
+    }
+    return seg_tri_rec(o, e, b.srec + 4 * (size_t) t, meta);
+}
+
 // Any occluder triangle hit with r < 1 on [o, e] (TriTree::IntersectRay,
 // lighter_math.cpp:804-832, over every shadowing instance).
-template <bool kWide = false>
-__device__ __forceinline__ bool bvh_any_hit(const BvhView& b, V3 o, V3 e, ErrFlag err)
+template <bool kWide, class Stack>
+__device__ __forceinline__ bool bvh_any_hit_s(const BvhView& b, V3 o, V3 e, ErrFlag err, Stack& st)
 {
     bool hit = false;
     auto leaf = [&](int t, float&) {
         u32 meta;
-        float r = seg_tri_rec(o, e, b.srec + 4 * (size_t) t, meta);
+        float r = seg_leaf(b, o, e, t, meta);
         if (!(meta & kOccluderBit)) return true;
         if (r < 1.0f) { hit = true; return false; }
         return true;
     };
-    if (kWide) walk_segment4(b, o, e, err, leaf);
-    else walk_segment(b, o, e, err, leaf);
+    if (kWide) walk_segment4(b, o, e, err, st, leaf);
+    else walk_segment(b, o, e, err, st, leaf);
     return hit;
+}
+
+template <bool kWide = false>
+__device__ __forceinline__ bool bvh_any_hit(const BvhView& b, V3 o, V3 e, ErrFlag err)
+{
+    TStack<0> st;
+    return bvh_any_hit_s<kWide>(b, o, e, err, st);
 }
 
 // Smallest hit fraction over occluders (TriTree::IntersectRayDist,
 // lighter_math.cpp:835-871); *tri_out = leaf-order index of the hit triangle.
-__device__ __forceinline__ float bvh_closest(const BvhView& b, V3 o, V3 e, ErrFlag err, int* tri_out)
+template <class Stack>
+__device__ __forceinline__ float bvh_closest_s(const BvhView& b, V3 o, V3 e, ErrFlag err, int* tri_out, Stack& st)
 {
     float best = kNoHit;
     int bt = -1;
-    walk_segment(b, o, e, err, [&](int t, float& tlimit) {
+    walk_segment(b, o, e, err, st, [&](int t, float& tlimit) {
         u32 meta;
-        float r = seg_tri_rec(o, e, b.srec + 4 * (size_t) t, meta);
+        float r = seg_leaf(b, o, e, t, meta);
         if (!(meta & kOccluderBit)) return true;
         if (r < best || (r == best && r < kNoHit && t < bt)) {
             best = r; bt = t;
@@ -356,6 +423,12 @@ __device__ __forceinline__ float bvh_closest(const BvhView& b, V3 o, V3 e, ErrFl
     return best;
 }
 
+__device__ __forceinline__ float bvh_closest(const BvhView& b, V3 o, V3 e, ErrFlag err, int* tri_out)
+{
+    TStack<0> st;
+    return bvh_closest_s(b, o, e, err, tri_out, st);
+}
+
 // Closest hit restricted to one instance's triangles, occluder or not
 // (the per-instance tree of TriTree::OffsetSample, lighter_math.cpp:1024);
 // *local_out = the triangle's index within its instance.
@@ -363,9 +436,10 @@ __device__ __forceinline__ float bvh_closest_inst(const BvhView& b, V3 o, V3 e, 
 {
     float best = kNoHit;
     int bl = -1;
-    walk_segment(b, o, e, err, [&](int t, float& tlimit) {
+    TStack<0> st;
+    walk_segment(b, o, e, err, st, [&](int t, float& tlimit) {
         u32 meta;
-        float r = seg_tri_rec(o, e, b.srec + 4 * (size_t) t, meta);
+        float r = seg_leaf(b, o, e, t, meta);
         if ((meta & kInstMask) != inst) return true;
         u32 local = __float_as_uint(__ldg(&b.tris[3 * (size_t) t + 1]).w);
         if (r < best || (r == best && r < kNoHit && (int) local < bl)) {
@@ -382,15 +456,14 @@ __device__ __forceinline__ float bvh_closest_inst(const BvhView& b, V3 o, V3 e, 
 // (ltr_Scene::Distance + TriTree::GetDistance, lighter.cpp:150-188,
 // lighter_math.cpp:954-989). The reference shrinks a query cube; a sphere
 // test against the child boxes prunes the same triangles.
-__device__ __forceinline__ float bvh_distance(const BvhView& b, V3 p, float d0, ErrFlag err, u32* visits = nullptr,
-                                              u32* tests = nullptr, int* best_leaf = nullptr)
+template <class Stack>
+__device__ __forceinline__ float bvh_distance_s(const BvhView& b, V3 p, float d0, ErrFlag err, Stack& st,
+                                                u32* visits = nullptr, u32* tests = nullptr, int* best_leaf = nullptr)
 {
     u32 nt = 0;
     float dist = d0;
     if (b.n_tris <= 0) return dist;
-    int stack[kStack];
-    float stack_d[kStack];
-    int sp = 0;
+    st.sp = 0;
     int cur = b.root;
     u32 nv = 0;
     for (;;) {
@@ -403,8 +476,7 @@ __device__ __forceinline__ float bvh_distance(const BvhView& b, V3 p, float d0, 
             bool hl = dl <= lim, hr = dr <= lim;
             if (hl && hr) {
                 bool lfirst = dl <= dr;
-                if (sp < kStack) { stack[sp] = lfirst ? nb.r : nb.l; stack_d[sp] = lfirst ? dr : dl; ++sp; }
-                else raise_err(err, 1u);
+                st.push(lfirst ? nb.r : nb.l, lfirst ? dr : dl, err);
                 cur = lfirst ? nb.l : nb.r;
                 continue;
             }
@@ -424,16 +496,184 @@ __device__ __forceinline__ float bvh_distance(const BvhView& b, V3 p, float d0, 
         }
         bool done = false;
         for (;;) {
-            if (sp == 0) { done = true; break; }
-            --sp;
-            if (stack_d[sp] <= dist * dist) break;
+            if (st.sp == 0) { done = true; break; }
+            float k;
+            st.pop(cur, k);
+            if (k <= dist * dist) break;
         }
         if (done) break;
-        cur = stack[sp];
     }
     if (visits) *visits += nv;
     if (tests) *tests += nt;
     return dist;
+}
+
+__device__ __forceinline__ float bvh_distance(const BvhView& b, V3 p, float d0, ErrFlag err, u32* visits = nullptr,
+                                              u32* tests = nullptr, int* best_leaf = nullptr)
+{
+    TStack<0> st;
+    return bvh_distance_s(b, p, d0, err, st, visits, tests, best_leaf);
+}
+
+// ---- warp-cooperative queries. The 32 lanes of a warp walk the binary BVH
+// together: a child is entered when the query of any lane still running
+// reaches its box, node loads are broadcasts, and every lane runs each leaf
+// test of the walk against its own query. The walk visits a superset of the
+// nodes each lane's own walk would visit, and a subtree is dropped only when,
+// for every lane, it lies beyond that lane's current limit, so every lane gets
+// exactly the result of the per-lane query. The stack is warp-uniform and
+// lives in registers spread over the lanes (entry i in lane i % 32, slot
+// i / 32; 64 entries, more than the tree's depth). Every lane of the warp
+// must call these (converged).
+
+// Pushes `n` on the warp's stack (or records error bit 0 past 64 entries).
+__device__ __forceinline__ void wstack_push(int& s0, int& s1, int& sp, int n, ErrFlag err)
+{
+    const int lane = threadIdx.x & 31;
+    if (sp < 64) {
+        if (lane == (sp & 31)) { if (sp < 32) s0 = n; else s1 = n; }
+        ++sp;
+    } else if (lane == 0) {
+        raise_err(err, 1u);
+    }
+}
+
+__device__ __forceinline__ int wstack_pop(int s0, int s1, int& sp)
+{
+    --sp;
+    return __shfl_sync(0xffffffffu, sp < 32 ? s0 : s1, sp & 31);
+}
+
+// The child a warp enters first when the lanes reach both: the one more of
+// those lanes find nearer.
+__device__ __forceinline__ bool warp_left_first(bool hl, bool hr, bool lnear)
+{
+    const unsigned both = __ballot_sync(0xffffffffu, hl && hr);
+    const unsigned ln = __ballot_sync(0xffffffffu, hl && hr && lnear);
+    return 2 * __popc(ln) >= __popc(both);
+}
+
+// bvh_distance for the active lanes: min(d0, min over occluder triangles of
+// the exact point-triangle distance), each lane with its own point and radius.
+__device__ __forceinline__ float warp_distance(const BvhView& b, V3 p, float d0, bool active, ErrFlag err, u32& nv,
+                                               u32& nt)
+{
+    float dist = d0;
+    if (b.n_tris <= 0 || !__any_sync(0xffffffffu, active)) return dist;
+    int s0 = 0, s1 = 0, sp = 0;
+    int cur = b.root;
+    for (;;) {
+        if (cur >= 0) {
+            const NodeBoxes nb = load_node(b, cur);
+            if (active) ++nv;
+            const float lim = dist * dist;
+            const float dl = box_d2(nb.lmin, nb.lmax, p), dr = box_d2(nb.rmin, nb.rmax, p);
+            const bool hl = active && dl <= lim, hr = active && dr <= lim;
+            const unsigned ml = __ballot_sync(0xffffffffu, hl), mr = __ballot_sync(0xffffffffu, hr);
+            if (ml && mr) {
+                const bool lfirst = warp_left_first(hl, hr, dl <= dr);
+                wstack_push(s0, s1, sp, lfirst ? nb.r : nb.l, err);
+                cur = lfirst ? nb.l : nb.r;
+                continue;
+            }
+            if (ml) { cur = nb.l; continue; }
+            if (mr) { cur = nb.r; continue; }
+        } else {
+            const int t = ~cur;
+            const u32 meta = __float_as_uint(__ldg(&b.drec[8 * (size_t) t + 4]).w);
+            if (active && (meta & kOccluderBit)) {
+                const float nd = point_tri_dist_rec(b, t, p);
+                ++nt;
+                if (nd < dist) dist = nd;
+            }
+        }
+        if (sp == 0) break;
+        cur = wstack_pop(s0, s1, sp);
+    }
+    return dist;
+}
+
+// bvh_any_hit for the active lanes' segments: a lane stops searching at its
+// first occluder hit (r < 1); the walk ends when no lane searches any more.
+__device__ __forceinline__ bool warp_any_hit(const BvhView& b, V3 o, V3 e, bool active, ErrFlag err)
+{
+    bool hit = false;
+    bool searching = active && b.n_tris > 0;
+    if (!__any_sync(0xffffffffu, searching)) return false;
+    const V3 d = e - o;
+    const V3 inv = inv_dir(d);
+    const V3 oinv = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+    int s0 = 0, s1 = 0, sp = 0;
+    int cur = b.root;
+    for (;;) {
+        if (cur >= 0) {
+            const NodeBoxes nb = load_node(b, cur);
+            float tl, tr;
+            const bool hl = searching && slab(nb.lmin, nb.lmax, oinv, inv, 1.0f, tl);
+            const bool hr = searching && slab(nb.rmin, nb.rmax, oinv, inv, 1.0f, tr);
+            const unsigned ml = __ballot_sync(0xffffffffu, hl), mr = __ballot_sync(0xffffffffu, hr);
+            if (ml && mr) {
+                const bool lfirst = warp_left_first(hl, hr, tl <= tr);
+                wstack_push(s0, s1, sp, lfirst ? nb.r : nb.l, err);
+                cur = lfirst ? nb.l : nb.r;
+                continue;
+            }
+            if (ml) { cur = nb.l; continue; }
+            if (mr) { cur = nb.r; continue; }
+        } else if (searching) {
+            u32 meta;
+            const float r = seg_leaf(b, o, e, ~cur, meta);
+            if ((meta & kOccluderBit) && r < 1.0f) { hit = true; searching = false; }
+        }
+        if (sp == 0 || !__any_sync(0xffffffffu, searching)) break;
+        cur = wstack_pop(s0, s1, sp);
+    }
+    return hit;
+}
+
+// bvh_closest for the active lanes' segments (the smallest occluder hit
+// fraction, ties to the lower leaf -- a rule that does not depend on the
+// visiting order), each lane shrinking its own limit.
+__device__ __forceinline__ float warp_closest(const BvhView& b, V3 o, V3 e, bool active, ErrFlag err)
+{
+    float best = kNoHit;
+    int bt = -1;
+    if (b.n_tris <= 0 || !__any_sync(0xffffffffu, active)) return best;
+    const V3 d = e - o;
+    const V3 inv = inv_dir(d);
+    const V3 oinv = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+    float tlimit = 1.0f;
+    int s0 = 0, s1 = 0, sp = 0;
+    int cur = b.root;
+    for (;;) {
+        if (cur >= 0) {
+            const NodeBoxes nb = load_node(b, cur);
+            float tl, tr;
+            const bool hl = active && slab(nb.lmin, nb.lmax, oinv, inv, tlimit, tl);
+            const bool hr = active && slab(nb.rmin, nb.rmax, oinv, inv, tlimit, tr);
+            const unsigned ml = __ballot_sync(0xffffffffu, hl), mr = __ballot_sync(0xffffffffu, hr);
+            if (ml && mr) {
+                const bool lfirst = warp_left_first(hl, hr, tl <= tr);
+                wstack_push(s0, s1, sp, lfirst ? nb.r : nb.l, err);
+                cur = lfirst ? nb.l : nb.r;
+                continue;
+            }
+            if (ml) { cur = nb.l; continue; }
+            if (mr) { cur = nb.r; continue; }
+        } else if (active) {
+            const int t = ~cur;
+            u32 meta;
+            const float r = seg_leaf(b, o, e, t, meta);
+            if ((meta & kOccluderBit) && (r < best || (r == best && r < kNoHit && t < bt))) {
+                best = r;
+                bt = t;
+                tlimit = fminf(1.0f, r);
+            }
+        }
+        if (sp == 0) break;
+        cur = wstack_pop(s0, s1, sp);
+    }
+    return best;
 }
 
 #endif  // __CUDACC__
@@ -461,7 +701,7 @@ struct BvhStorage {
     int root4 = 0;
     size_t bytes = 0;
     void* scratch = nullptr;   // build scratch, freed by bvh_free
-    BvhView view() const { BvhView v = {nodes, tris, srec, drec, n_tris, root, nodes4, root4}; return v; }
+    BvhView view() const { BvhView v = {nodes, tris, srec, drec, n_tris, root, nodes4, root4, 0}; return v; }
 };
 
 // Builds into `out` on `stream` (allocations with cudaMallocAsync on that stream).

@@ -115,6 +115,50 @@ HD float seg_tri(V3 L1, V3 L2, V3 P1, V3 P2, V3 P3)
     return r;
 }
 
+// Watertight segment/triangle test (Woop, Benthin and Wald, "Watertight
+// Ray/Triangle Intersection", JCGT 2(1), 2013), the LTRG_ISECT_WATERTIGHT
+// alternative to seg_tri. The triangle is moved to the segment's start,
+// sheared and scaled so that the segment runs along +z over [0, 1], and the
+// signs of the three 2D edge functions U, V, W decide inclusion. An edge
+// function that comes out exactly 0 in FP32 is recomputed from the same FP32
+// coordinates in FP64, where the two products are exact, so its sign is the
+// exact one: a segment through an edge or vertex shared by two triangles hits
+// at least one of them. Both windings count; a degenerate projection (U + V +
+// W = 0) misses. Returns the fraction r in [0, 1] along L1 -> L2, or kNoHit.
+HD float wt_comp(V3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+HD float seg_tri_wt(V3 L1, V3 L2, V3 P1, V3 P2, V3 P3)
+{
+    V3 D = L2 - L1;
+    const float ax = fabsf(D.x), ay = fabsf(D.y), az = fabsf(D.z);
+    const int kz = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+    int kx = kz == 2 ? 0 : kz + 1;
+    int ky = kx == 2 ? 0 : kx + 1;
+    const float dz = wt_comp(D, kz);
+    if (dz == 0.0f) return kNoHit;   // zero-length segment
+    if (dz < 0.0f) { int t = kx; kx = ky; ky = t; }   // keep the winding of the projection
+    const float Sx = wt_comp(D, kx) / dz, Sy = wt_comp(D, ky) / dz, Sz = 1.0f / dz;
+    const V3 A = P1 - L1, B = P2 - L1, C = P3 - L1;
+    const float Ax = wt_comp(A, kx) - Sx * wt_comp(A, kz), Ay = wt_comp(A, ky) - Sy * wt_comp(A, kz);
+    const float Bx = wt_comp(B, kx) - Sx * wt_comp(B, kz), By = wt_comp(B, ky) - Sy * wt_comp(B, kz);
+    const float Cx = wt_comp(C, kx) - Sx * wt_comp(C, kz), Cy = wt_comp(C, ky) - Sy * wt_comp(C, kz);
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float) ((double) Cx * (double) By - (double) Cy * (double) Bx);
+        V = (float) ((double) Ax * (double) Cy - (double) Ay * (double) Cx);
+        W = (float) ((double) Bx * (double) Ay - (double) By * (double) Ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return kNoHit;
+    const float det = U + V + W;
+    if (det == 0.0f) return kNoHit;
+    const float Az = Sz * wt_comp(A, kz), Bz = Sz * wt_comp(B, kz), Cz = Sz * wt_comp(C, kz);
+    const float T = U * Az + V * Bz + W * Cz;
+    if (det > 0.0f ? (T < 0.0f || T > det) : (T > 0.0f || T < det)) return kNoHit;
+    return T / det;   // |T| <= |det| with equal signs: the rounded quotient stays in [0, 1]
+}
+
 // Unsigned point/triangle distance by corner, edge and face regions
 // (lighter_math.cpp:875-913).
 HD float point_tri_dist(V3 pt, V3 t0, V3 t1, V3 t2)

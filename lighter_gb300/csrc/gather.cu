@@ -40,6 +40,7 @@
 #include <mutex>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/lighter_gb300.h"
@@ -104,13 +105,14 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait for the phase of parity `parity`; false (and the error bit) on expiry.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, u32* err, u32 bit)
+// Bounded wait for the phase of parity `parity`: false (and the error bit)
+// after `limit` SM clock cycles.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, u32* err, u32 bit, unsigned long long limit)
 {
     if (mbar_try(bar, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try(bar, parity)) {
-        if (clock64() - t0 > (long long) kWaitCycles) {
+        if (clock64() - t0 > (long long) limit) {
             atomicOr(err, bit);
             return false;
         }
@@ -199,6 +201,8 @@ struct UmmaArgs {
     const u32* rp_first;  // first CTA whose range touches each row block
     float* partial;       // [rp][slot][R][256]
     u32* err;
+    unsigned long long wait_cycles;   // limit of every mbarrier wait (kWaitCycles)
+    u32 issue;            // 0: the producer issues no copies (ltrdbg_GatherStallNextSolve), else 1
 };
 
 // KB: k per pipeline stage (a 64-wide work unit takes 64 / KB stages).
@@ -252,10 +256,11 @@ __global__ void __launch_bounds__(kThreads, 1)
             // producer: stage counter i runs over the units' stages
             uint64_t i = 0;
             bool ok = true;
-            for (uint64_t u = lo; u < hi && ok; ++u) {
+            for (uint64_t u = a.issue ? lo : hi; u < hi && ok; ++u) {
                 for (int q = 0; q < SPU; ++q, ++i) {
                     const u32 s = (u32) (i % a.stages);
-                    if (i >= a.stages && !mbar_wait(&empty[s], (u32) ((i / a.stages) - 1) & 1u, a.err, kErrProducer)) {
+                    if (i >= a.stages &&
+                        !mbar_wait(&empty[s], (u32) ((i / a.stages) - 1) & 1u, a.err, kErrProducer, a.wait_cycles)) {
                         ok = false;
                         break;
                     }
@@ -271,7 +276,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             // wait for the copies still in flight (complete already unless a wait above expired)
             const uint64_t issued = i;
             for (uint64_t j = issued > a.stages ? issued - a.stages : 0; j < issued; ++j)
-                if (!mbar_wait(&full[j % a.stages], (u32) (j / a.stages) & 1u, a.err, kErrDrain)) break;
+                if (!mbar_wait(&full[j % a.stages], (u32) (j / a.stages) & 1u, a.err, kErrDrain, a.wait_cycles)) break;
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -283,10 +288,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const u32 kb = (u32) (u % a.nkb);
                 const bool first = u == lo || kb == 0 || (a.kchunk && kb % a.kchunk == 0);
                 const bool last = u + 1 == hi || kb + 1 == a.nkb || (a.kchunk && (kb + 1) % a.kchunk == 0);
-                if (first && seg > 0 && !mbar_wait(acce, (seg - 1) & 1u, a.err, kErrMma)) break;
+                if (first && seg > 0 && !mbar_wait(acce, (seg - 1) & 1u, a.err, kErrMma, a.wait_cycles)) break;
                 for (int q = 0; q < SPU; ++q, ++i) {
                     const u32 s = (u32) (i % a.stages);
-                    if (!mbar_wait(&full[s], (u32) (i / a.stages) & 1u, a.err, kErrMma)) {
+                    if (!mbar_wait(&full[s], (u32) (i / a.stages) & 1u, a.err, kErrMma, a.wait_cycles)) {
                         ok = false;
                         break;
                     }
@@ -309,7 +314,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (ok && last) { umma_commit(accf); ++seg; }
             }
             umma_commit(done);
-            mbar_wait(done, 0, a.err, kErrDrain);
+            mbar_wait(done, 0, a.err, kErrDrain, a.wait_cycles);
         }
     } else {
         // epilogue: TMEM lanes of quadrant q = rows 32q .. 32q+31 of each 128-row half
@@ -325,7 +330,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             u = min(hi, (uint64_t) rp * a.nkb + kend);
             // every lane waits; the warp goes on only if all of them saw the phase, so the
             // .sync.aligned loads below always run converged
-            const bool ok = mbar_wait(accf, seg & 1u, a.err, kErrEpilogue);
+            const bool ok = mbar_wait(accf, seg & 1u, a.err, kErrEpilogue, a.wait_cycles);
             if (!__all_sync(0xffffffffu, ok)) break;
             tc_fence_after();
             const u32 slot = blockIdx.x - __ldg(&a.rp_first[rp]);
@@ -641,6 +646,87 @@ struct DevBuf {
     template <class T> T* as() const { return reinterpret_cast<T*>(p); }
 };
 
+// Page-locked host buffer kept by a gather (grown, never shrunk).
+struct PinBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    void ensure(size_t b)
+    {
+        if (b <= bytes) return;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        GCK(cudaHostAlloc(&p, b, cudaHostAllocPortable));
+        bytes = b;
+    }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+// Host <-> device copies of the host-buffer entry point through kept
+// page-locked buffers. A copy straight from the caller's pageable memory runs
+// at about 10 GB/s; here the bytes are cut into one slice per host thread,
+// each thread copies its slice into the page-locked buffer and queues that
+// slice's DMA at once, so the DMA of early slices overlaps the host copies of
+// later ones (and the reverse for the result: each slice's DMA is followed by
+// an event its thread waits on before copying the slice out).
+constexpr int kStageThreads = 8;
+constexpr size_t kStageMinSlice = 1 << 20;
+
+int stage_slices(size_t bytes)
+{
+    return (int) std::max<size_t>(1, std::min<size_t>(kStageThreads, bytes / kStageMinSlice));
+}
+
+void stage_h2d(void* dev, const void* host, size_t bytes, PinBuf& pin, cudaStream_t s)
+{
+    if (!bytes) return;
+    pin.ensure(bytes);
+    const int k = stage_slices(bytes);
+    const size_t step = (bytes / k + 255) / 256 * 256;
+    std::vector<std::thread> th;
+    std::vector<cudaError_t> rc(k, cudaSuccess);
+    for (int t = 0; t < k; ++t)
+        th.emplace_back([&, t]() {
+            const size_t a = std::min(bytes, t * step), b = std::min(bytes, a + step);
+            if (a >= b) return;
+            memcpy((char*) pin.p + a, (const char*) host + a, b - a);
+            rc[t] = cudaMemcpyAsync((char*) dev + a, (char*) pin.p + a, b - a, cudaMemcpyHostToDevice, s);
+        });
+    for (auto& x : th) x.join();
+    for (cudaError_t e : rc) GCK(e);
+}
+
+void stage_d2h(void* host, const void* dev, size_t bytes, PinBuf& pin, cudaStream_t s)
+{
+    if (!bytes) return;
+    pin.ensure(bytes);
+    const int k = stage_slices(bytes);
+    const size_t step = (bytes / k + 255) / 256 * 256;
+    std::vector<cudaEvent_t> ev(k, nullptr);
+    for (int t = 0; t < k; ++t) {
+        const size_t a = std::min(bytes, t * step), b = std::min(bytes, a + step);
+        GCK(cudaEventCreateWithFlags(&ev[t], cudaEventDisableTiming | cudaEventBlockingSync));
+        if (a < b) GCK(cudaMemcpyAsync((char*) pin.p + a, (const char*) dev + a, b - a, cudaMemcpyDeviceToHost, s));
+        GCK(cudaEventRecord(ev[t], s));
+    }
+    std::vector<std::thread> th;
+    std::vector<cudaError_t> rc(k, cudaSuccess);
+    for (int t = 0; t < k; ++t)
+        th.emplace_back([&, t]() {
+            const size_t a = std::min(bytes, t * step), b = std::min(bytes, a + step);
+            rc[t] = cudaEventSynchronize(ev[t]);
+            if (rc[t] == cudaSuccess && a < b) memcpy((char*) host + a, (const char*) pin.p + a, b - a);
+        });
+    for (auto& x : th) x.join();
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    for (cudaError_t e : rc) GCK(e);
+}
+
 }  // namespace
 }  // namespace lg
 
@@ -663,8 +749,10 @@ struct ltrg_Gather {
     // solve scratch
     DevBuf partial, xh, xl, x32, btmp, err, emax;
     DevBuf h_alb, h_E, h_out;     // device copies for the host-buffer entry point
+    PinBuf pin_in, pin_out;       // its page-locked staging
     uint64_t links = 0, vis_rays = 0, pairs = 0;
     double ms_build = 0;
+    u32 stall_us = 0;             // ltrdbg_GatherStallNextSolve
     std::string error;
     std::mutex mu;
 
@@ -676,6 +764,8 @@ struct ltrg_Gather {
         DevBuf* all[] = {&G32,  &G16, &G16lo, &rp_tab, &partial, &xh,    &xl,
                          &x32,  &btmp, &err,  &emax,   &h_alb,   &h_E,   &h_out};
         for (DevBuf* b : all) b->release();
+        pin_in.release();
+        pin_out.release();
         cudaStreamDestroy(st);
     }
 
@@ -812,6 +902,13 @@ void ltrg_Gather::solve(const float* alb, const float* E, u32 R, int bounces, in
         ua.rp_first = rp_tab.as<u32>();
         ua.partial = partial.as<float>();
         ua.err = err.as<u32>();
+        ua.wait_cycles = kWaitCycles;
+        ua.issue = 1;
+        if (stall_us) {   // test hook: copies never issued, waits cut short
+            ua.issue = 0;
+            ua.wait_cycles = (unsigned long long) stall_us * 2000ull;
+            stall_us = 0;
+        }
         const u32* rp_cnt = rp_tab.as<u32>() + n_rp;
         emax.ensure(4);
         GCK(cudaMemsetAsync(emax.p, 0, 4, s));
@@ -1014,6 +1111,14 @@ LTRAPI LTRBOOL ltrg_GatherGetG(ltrg_Gather* g, float* out)
 
 LTRAPI const char* ltrg_GatherLastError(ltrg_Gather* g) { return g && !g->error.empty() ? g->error.c_str() : nullptr; }
 
+LTRAPI LTRBOOL ltrdbg_GatherStallNextSolve(ltrg_Gather* g, u32 wait_us)
+{
+    if (!g || wait_us == 0 || wait_us > 2000000u) return 0;
+    std::lock_guard<std::mutex> lk(g->mu);
+    g->stall_us = wait_us;
+    return 1;
+}
+
 LTRAPI LTRBOOL ltrg_GatherSolveDevice(ltrg_Gather* g, const float* albedo_rgb, const float* emission, u32 R,
                                       int bounces, int precision, int refine, float* out, ltrg_GatherStats* stats,
                                       void* stream)
@@ -1030,6 +1135,7 @@ LTRAPI LTRBOOL ltrg_GatherSolveDevice(ltrg_Gather* g, const float* albedo_rgb, c
                  stream ? (cudaStream_t) stream : g->st);
     } catch (const std::exception& e) {
         g->error = e.what();
+        cudaGetLastError();   // the error is reported here; none is left for the caller's next CUDA call
         return 0;
     }
     return 1;
@@ -1052,15 +1158,16 @@ LTRAPI LTRBOOL ltrg_GatherSolve(ltrg_Gather* g, const float* albedo_rgb, const f
         g->h_E.ensure((size_t) n * R * 4);
         g->h_out.ensure((size_t) n * R * 4);
         GCK(cudaMemcpyAsync(g->h_alb.p, albedo_rgb, (size_t) n * 3 * 4, cudaMemcpyHostToDevice, s));
-        GCK(cudaMemcpyAsync(g->h_E.p, emission, (size_t) n * R * 4, cudaMemcpyHostToDevice, s));
+        stage_h2d(g->h_E.p, emission, (size_t) n * R * 4, g->pin_in, s);
         note_h2d((size_t) n * (3 + R) * 4);
         g->solve(g->h_alb.as<float>(), g->h_E.as<float>(), R, bounces, precision, refine, g->h_out.as<float>(), stats,
                  s);
-        GCK(cudaMemcpyAsync(out, g->h_out.p, (size_t) n * R * 4, cudaMemcpyDeviceToHost, s));
+        stage_d2h(out, g->h_out.p, (size_t) n * R * 4, g->pin_out, s);
         note_d2h((size_t) n * R * 4);
         GCK(cudaStreamSynchronize(s));
     } catch (const std::exception& e) {
         g->error = e.what();
+        cudaGetLastError();   // the error is reported here; none is left for the caller's next CUDA call
         return 0;
     }
     return 1;

@@ -13,16 +13,22 @@
 //
 // The scratch array is a file-scope __device__ variable, so every GPU that
 // loads this library holds it (LTRG_NOALLOC_SCRATCH_BYTES, 14 MiB) until the
-// process exits. Host code cannot use the array's name as a device address:
-// the first call on each device looks up the address with
-// cudaGetSymbolAddress while that device is current, and later calls reuse
-// it. That first call should therefore come before any stream capture.
+// process exits. Host code cannot use the array's name as a device address: a
+// call whose stream is not being captured looks the address up with
+// cudaGetSymbolAddress, with the caller's device current, and remembers it for
+// that device and CUDA context; a call on a stream under capture uses the
+// remembered address (looking it up only if there is none yet). So the first
+// call in each context -- on each device, and again after a cudaDeviceReset,
+// which destroys the context that held the array -- should come before any
+// stream capture.
 //
 // All calls share the one array and it keeps the last call's contents, so
 // each call re-initialises both masks before use. Calls whose work overlaps
 // on the GPU (two streams, or two host threads on one device) race on the
 // scratch and must be serialised by the caller.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <cmath>
 #include <mutex>
@@ -47,21 +53,43 @@ struct Taps { float k[2 * kNaMaxExt + 1]; };
 constexpr int kMaxDevices = 64;
 std::mutex g_na_mutex;
 void* g_na_addr[kMaxDevices] = {};
+CUcontext g_na_ctx[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device (looked up once
-// per device); nullptr on failure.
-void* scratch_address(cudaError_t* err)
+// The calling thread's current CUDA context (driver entry point, so the
+// library needs no link-time dependency on the driver library).
+CUcontext current_context()
+{
+    static PFN_cuCtxGetCurrent_v4000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, []() {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPoint("cuCtxGetCurrent", &p, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuCtxGetCurrent_v4000) p;
+    });
+    CUcontext c = nullptr;
+    if (fn) fn(&c);
+    return c;
+}
+
+// Device address of the scratch array for the current device and context:
+// looked up afresh unless `capturing`, in which case the address remembered
+// for this device and context is used; nullptr on failure.
+void* scratch_address(bool capturing, cudaError_t* err)
 {
     int dev = -1;
     *err = cudaGetDevice(&dev);
     if (*err != cudaSuccess) return nullptr;
     if (dev < 0 || dev >= kMaxDevices) { *err = cudaErrorInvalidDevice; return nullptr; }
+    const CUcontext ctx = current_context();
     std::lock_guard<std::mutex> lock(g_na_mutex);
-    if (!g_na_addr[dev]) {
+    if (!capturing || !g_na_addr[dev] || g_na_ctx[dev] != ctx) {
         void* p = nullptr;
         *err = cudaGetSymbolAddress(&p, g_na_scratch);
         if (*err != cudaSuccess) return nullptr;
         g_na_addr[dev] = p;
+        g_na_ctx[dev] = ctx;
     }
     return g_na_addr[dev];
 }
@@ -145,13 +173,15 @@ extern "C" LTRAPI int ltrg_FinalizeLightmapNoAlloc(const float* rgb, const unsig
     if (!rgb || !mask || !out || width == 0 || height == 0) return LTRG_NOALLOC_EINVAL;
     if ((unsigned long long) width * height > kNaMaxTexels) return LTRG_NOALLOC_ETOOBIG;
     if (!(blur_size >= 0.0f) || std::ceil(blur_size) > (float) kNaMaxExt) return LTRG_NOALLOC_EINVAL;
+    cudaStream_t st = (cudaStream_t) stream;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const bool capturing = cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
     cudaError_t e;
-    unsigned char* base = (unsigned char*) scratch_address(&e);
+    unsigned char* base = (unsigned char*) scratch_address(capturing, &e);
     if (!base) return LTRG_NOALLOC_ECUDA;
     unsigned char* ma = base;
     unsigned char* mb = base + kMaskBytes;
     float* tmp = (float*) (base + kImageOffset);
-    cudaStream_t st = (cudaStream_t) stream;
     const unsigned n = width * height;
     const unsigned threads = 256;
     const unsigned blocks = (n + threads - 1) / threads < 152u * 32u ? (n + threads - 1) / threads : 152u * 32u;

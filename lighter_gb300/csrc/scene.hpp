@@ -37,7 +37,14 @@ struct HostLight {
     float range, power, radius;
     int nsamples;
     float out, in, curve;
+    float randoff;   // the light's rand() draw of ltr_LightAdd (lighter.cpp:1300)
 };
+
+// Per-light shadow samples of LTRG_SHADOW_SAMPLED, computed on the host like
+// ltr_LightAdd computes its samples (lighter.cpp:1295-1312): directional
+// lights get nsamples unit ray directions, point and spot lights nsamples
+// disk offsets (x, y, 0) in the plane facing the sample (api.cpp).
+std::vector<V3> light_shadow_samples(const HostLight& L);
 
 // Per-instance copies of the sample arrays, kept when keep_samples is set.
 struct SampleDump {
@@ -97,6 +104,13 @@ struct ltr_Scene {
     std::atomic<const char*> stage{"not started"};
     std::atomic<float> completion{0};
     std::atomic<bool> abort_flag{false};
+    // Page-locked word mapped into the device's address space: ltr_Abort sets it
+    // to 1 and the persistent trace kernels poll it at their work fetches, so an
+    // abort ends a long trace launch within about one fetch. run_bake writes 0
+    // and publishes the pointer before it reads abort_flag once more, so an
+    // abort racing with the start of a bake is never lost.
+    std::atomic<lg::u32*> abort_word{nullptr};
+    void* abort_alloc = nullptr;
     std::atomic<bool> running{false};
     std::thread worker;
     std::mutex join_mu;                     // serialises joins of `worker` (pollers may run on several threads)

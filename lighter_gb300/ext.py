@@ -23,7 +23,9 @@ class Options(C.Structure):
         ("refine_steps", C.c_int),
         ("radiosity_patches", u32),
         ("bvh_builder", u32),
-        ("reserved", u32 * 9),
+        ("shadow_mode", u32),
+        ("intersect_mode", u32),
+        ("reserved", u32 * 7),
     ]
 
 
@@ -33,7 +35,8 @@ class Stats(C.Structure):
         "ms_finalize", "ms_download")] + [(n, C.c_uint64) for n in (
             "texels", "samples", "triangles", "shadow_evals", "distance_queries", "ao_rays", "rad_pairs",
             "rad_vis_rays", "node_visits", "tri_tests", "rad_elements", "kernel_launches", "bytes_h2d",
-            "bytes_d2h")] + [("ms_device", C.c_double), ("reserved", C.c_uint64 * 1)]
+            "bytes_d2h")] + [("ms_device", C.c_double), ("ms_direct_trace", C.c_double), ("ms_ao_trace", C.c_double),
+                             ("shadow_pairs", C.c_uint64), ("reserved", C.c_uint64 * 1)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
@@ -51,7 +54,9 @@ EXT_API = {
 
 class Tuning(C.Structure):
     _fields_ = [("direct_block", u32), ("direct_blocks_per_sm", u32), ("ao_block", u32), ("ao_blocks_per_sm", u32),
-                ("direct_order", u32), ("ao_order", u32), ("direct_regs", u32), ("reserved", u32 * 5)]
+                ("direct_order", u32), ("ao_order", u32), ("direct_regs", u32), ("direct_stack", u32),
+                ("ao_stack", u32), ("ao_chunk", u32), ("direct_packet", u32), ("sampled_regs", u32),
+                ("ao_packet", u32), ("reserved", u32 * 3)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
@@ -62,7 +67,25 @@ EXT_API.update({
     "ltrg_SetTuning": (C.c_int, [C.c_int, C.POINTER(Tuning)]),
     "ltrg_Autotune": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "ltrdbg_GetRadiosity": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)] + [C.c_void_p] * 6),
+    "ltrdbg_TraceSegments": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p, C.c_int]),
 })
+
+LTRG_ISECT_REFERENCE = 0
+LTRG_ISECT_WATERTIGHT = 1
+LTRG_SHADOW_SPHERE = 0
+LTRG_SHADOW_SAMPLED = 1
+
+
+def trace_segments(lib, tri_xyz, seg6, intersect_mode=LTRG_ISECT_REFERENCE, device=0):
+    """ltrdbg_TraceSegments: closest hit fraction of every segment (n, 6) against
+    the triangles (m, 9); 2.0 where a segment hits nothing."""
+    tri = np.ascontiguousarray(tri_xyz, dtype=np.float32).reshape(-1, 9)
+    seg = np.ascontiguousarray(seg6, dtype=np.float32).reshape(-1, 6)
+    out = np.empty(len(seg), np.float32)
+    if not lib.ltrdbg_TraceSegments(tri.ctypes.data, len(tri), seg.ctypes.data, len(seg), intersect_mode,
+                                    out.ctypes.data, device):
+        raise RuntimeError("ltrdbg_TraceSegments failed")
+    return out
 
 
 def get_radiosity(lib, scene, with_F: bool = True):
@@ -138,6 +161,7 @@ EXT_API.update({
     "ltrg_GatherSize": (u32, [C.c_void_p]),
     "ltrg_GatherGetG": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ltrg_GatherLastError": (C.c_char_p, [C.c_void_p]),
+    "ltrdbg_GatherStallNextSolve": (C.c_int, [C.c_void_p, u32]),
     "ltrg_GatherSolve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, u32, C.c_int, C.c_int, C.c_int, C.c_void_p,
                                    C.POINTER(GatherStats)]),
     "ltrg_GatherSolveDevice": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, u32, C.c_int, C.c_int, C.c_int,

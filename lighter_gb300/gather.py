@@ -69,6 +69,11 @@ class Gather:
         if not self.lib.ltrg_GatherSetChunk(self.h, int(k_blocks)):
             raise RuntimeError("ltrg_GatherSetChunk failed")
 
+    def stall_next_solve(self, wait_us: int):
+        """ltrdbg_GatherStallNextSolve: the next 16-bit solve's waits expire after wait_us."""
+        if not self.lib.ltrdbg_GatherStallNextSolve(self.h, int(wait_us)):
+            raise RuntimeError("ltrdbg_GatherStallNextSolve rejected its argument")
+
     def G(self) -> np.ndarray:
         """G_ij = F_ij * area_j (FP32, n x n) as built on the device."""
         out = np.empty((self.n, self.n), np.float32)

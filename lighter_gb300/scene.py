@@ -98,6 +98,7 @@ class BakeResult:
     wall_s: float
     debug: list = field(default_factory=list)   # per instance dict of sample arrays
     final_stage: str = ""
+    radiosity: Optional[dict] = None             # ext.get_radiosity of the bake (bake(..., radiosity=True))
 
 
 def _vec3(v):
@@ -239,6 +240,11 @@ def ingest(lib, desc: SceneDesc, threads: int = 1, gpu_options: Optional[dict] =
                 opts.setdefault("keep_samples", 1)
             if opts:
                 set_options(lib, scene, **opts)
+        elif gpu_options and _has(lib, "orc_SetOptions"):
+            # the oracle port takes the modes it restates; the other fields
+            # (device, tuning, precision) have no meaning on the CPU
+            vals = (abi.u32 * len(abi.ORACLE_OPTIONS))(*[int(gpu_options.get(k, 0)) for k in abi.ORACLE_OPTIONS])
+            lib.orc_SetOptions(scene, vals, len(abi.ORACLE_OPTIONS))
     except BaseException:
         lib.ltr_DestroyScene(scene)
         raise
@@ -247,10 +253,11 @@ def ingest(lib, desc: SceneDesc, threads: int = 1, gpu_options: Optional[dict] =
 
 def bake(lib, desc: SceneDesc, threads: int = 1, debug: bool = True, poll_s: float = 0.001,
          timeout_s: float = 3600.0, before_start: Optional[Callable] = None, gpu_options: Optional[dict] = None,
-         stats: Optional[dict] = None) -> BakeResult:
+         stats: Optional[dict] = None, radiosity: bool = False) -> BakeResult:
     """Replay `desc` through `lib`'s C API and return its outputs. For the GPU
     library, `gpu_options` are ltrg_Options fields and `stats` (a dict) receives
-    ltrg_GetStats; a bake that ends in an error raises RuntimeError."""
+    ltrg_GetStats; the oracle port takes the fields of abi.ORACLE_OPTIONS from
+    the same dict. A bake that ends in an error raises RuntimeError."""
     scene, keep = ingest(lib, desc, threads, gpu_options, debug)
     try:
         is_gpu = _has(lib, "ltrg_SetOptions")
@@ -280,7 +287,14 @@ def bake(lib, desc: SceneDesc, threads: int = 1, debug: bool = True, poll_s: flo
         cfg = abi.Config()
         lib.ltr_GetConfig(C.byref(cfg), scene)
         ao_ns = int(cfg.ao_num_samples) if cfg.ao_distance and cfg.ao_num_samples > 0 else 0
-        return _collect(lib, scene, debug, stages, wall, final, len(desc.lights), ao_ns)
+        res = _collect(lib, scene, debug, stages, wall, final, len(desc.lights), ao_ns)
+        if radiosity and _has(lib, "ltrdbg_GetRadiosity"):
+            # the elements of the radiosity stage; F too while it stays small (n <= 8192)
+            from .ext import get_radiosity
+            n = abi.u32(0)
+            lib.ltrdbg_GetRadiosity(scene, C.byref(n), None, None, None, None, None, None)
+            res.radiosity = get_radiosity(lib, scene, with_F=0 < n.value <= 8192)
+        return res
     finally:
         lib.ltr_DestroyScene(scene)
 
