@@ -20,6 +20,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <functional>
@@ -208,6 +209,50 @@ static float seg_tri(V3 L1, V3 L2, V3 P1, V3 P2, V3 P3)
     float t = (uv * wu - uu * wv) / D;
     if (t < 0.0f || (s + t) > 1.0f) return 2.0f;
     return r;
+}
+
+// Watertight segment/triangle test (Woop, Benthin and Wald, JCGT 2013), the
+// GPU library's LTRG_ISECT_WATERTIGHT mode: shear the triangle into the
+// segment's frame (segment along +z over [0, 1]); the signs of the 2D edge
+// functions decide inclusion, with an FP64 recomputation of any edge function
+// that is exactly 0 in FP32. Fraction r in [0, 1] or 2.
+static float comp3(V3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+static float seg_tri_watertight(V3 L1, V3 L2, V3 P1, V3 P2, V3 P3)
+{
+    V3 D = L2 - L1;
+    float ax = fabsf(D.x), ay = fabsf(D.y), az = fabsf(D.z);
+    int kz = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+    int kx = (kz + 1) % 3, ky = (kx + 1) % 3;
+    float dz = comp3(D, kz);
+    if (dz == 0.0f) return 2.0f;
+    if (dz < 0.0f) std::swap(kx, ky);
+    float Sx = comp3(D, kx) / dz, Sy = comp3(D, ky) / dz, Sz = 1.0f / dz;
+    V3 A = P1 - L1, B = P2 - L1, C = P3 - L1;
+    float Ax = comp3(A, kx) - Sx * comp3(A, kz), Ay = comp3(A, ky) - Sy * comp3(A, kz);
+    float Bx = comp3(B, kx) - Sx * comp3(B, kz), By = comp3(B, ky) - Sy * comp3(B, kz);
+    float Cx = comp3(C, kx) - Sx * comp3(C, kz), Cy = comp3(C, ky) - Sy * comp3(C, kz);
+    float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float) ((double) Cx * (double) By - (double) Cy * (double) Bx);
+        V = (float) ((double) Ax * (double) Cy - (double) Ay * (double) Cx);
+        W = (float) ((double) Bx * (double) Ay - (double) By * (double) Ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return 2.0f;
+    float det = U + V + W;
+    if (det == 0.0f) return 2.0f;
+    float Az = Sz * comp3(A, kz), Bz = Sz * comp3(B, kz), Cz = Sz * comp3(C, kz);
+    float T = U * Az + V * Bz + W * Cz;
+    if (det > 0.0f ? (T < 0.0f || T > det) : (T > 0.0f || T < det)) return 2.0f;
+    return T / det;
+}
+
+// The segment test of the bake in progress: the reference's, or the watertight
+// one when the scene's intersect mode asks for it (set by ltr_Scene::run; the
+// oracle bakes one scene at a time).
+static bool g_watertight = false;
+static float seg_test(V3 L1, V3 L2, V3 P1, V3 P2, V3 P3)
+{
+    return g_watertight ? seg_tri_watertight(L1, L2, P1, P2, P3) : seg_tri(L1, L2, P1, P2, P3);
 }
 
 // Unsigned point/triangle distance via corner/edge/face regions (lighter_math.cpp:875-913).
@@ -405,7 +450,7 @@ struct TriTree {
         bvh.ray_query(r, [&](const i32* ids, i32 n) {
             for (i32 i = 0; i < n; ++i) {
                 const Tri& T = tris[ids[i]];
-                hit = seg_tri(r.o, r.end, T.P1, T.P2, T.P3) < 1.0f;
+                hit = seg_test(r.o, r.end, T.P1, T.P2, T.P3) < 1.0f;
                 if (hit) return false;
             }
             return true;
@@ -419,7 +464,7 @@ struct TriTree {
         bvh.ray_query(r, [&](const i32* ids, i32 n) {
             for (i32 i = 0; i < n; ++i) {
                 const Tri& T = tris[ids[i]];
-                float d = seg_tri(r.o, r.end, T.P1, T.P2, T.P3);
+                float d = seg_test(r.o, r.end, T.P1, T.P2, T.P3);
                 if (d < best) { best = d; hid = ids[i]; }
             }
             return true;
@@ -570,7 +615,7 @@ struct BSP {
         float best = 2.0f;
         const Tri* bt = nullptr;
         for (const Tri& T : tris) {
-            float h = seg_tri(from, to, T.P1, T.P2, T.P3);
+            float h = seg_test(from, to, T.P1, T.P2, T.P3);
             if (h < best) { best = h; bt = &T; }
         }
         if (outn && bt) *outn = tri_normal_rev(*bt);
@@ -681,6 +726,8 @@ struct OInst {
 };
 struct OLight {
     u32 type; V3 pos, dir, up, color; float range, power, radius; int nsamples; float out, in, curve;
+    float randoff;           // the light's randf() of ltr_LightAdd (lighter.cpp:1300)
+    std::vector<V3> smp;     // shadow samples: ray directions (directional) or disk offsets (point, spot)
 };
 struct RadColors { V3 diff, total, out, in; float area; };
 struct RadLink { u32 other; float f; };
@@ -694,9 +741,15 @@ struct ltr_Scene {
     std::vector<ltr_WorkOutput> outputs;
     std::vector<V3> rad_pos, rad_nrm;
     std::vector<RadColors> rad_col;
+    std::vector<V3> rad_emit;   // the emission each element's bounces start from
     std::vector<RadLink> links;
     std::vector<u32> linkmap;
     BVH inst_tree;
+    // modes beyond the reference (orc_SetOptions); 0 everywhere is the reference bake
+    u32 opt_shadow_mode = 0;      // 1: sampled soft shadows
+    u32 opt_isect = 0;            // 1: watertight segment/triangle test
+    u32 opt_patches = 0;          // > 0: patch radiosity over about this many patches
+    u32 opt_links = 0;            // 1: link mutually visible pairs (0: occluded ones, lighter.cpp:751)
     std::atomic<const char*> stage{"not started"};
     std::atomic<float> completion{0};
     std::thread worker;
@@ -755,6 +808,31 @@ struct ltr_Scene {
         }
         return res;
     }
+    // Sampled soft shadows: 1 - (occluded rays) / n over the light's shadow
+    // samples. Directional: rays from `from` along each direction over range
+    // (lighter.cpp:566-584). Point/spot: rays to the disk points around the
+    // light in the plane facing the sample, with the basis of
+    // CreateSpiralDirVector (lighter_int.hpp:465-467) built on `dir` (the
+    // sample-to-light direction).
+    float sampled_vis(const OLight& L, V3 from, V3 dir) const
+    {
+        g_shadow_evals.fetch_add((unsigned long long) L.nsamples, std::memory_order_relaxed);
+        float f = 0.0f;
+        if (L.type == 3) {
+            for (int k = 0; k < L.nsamples; ++k)
+                if (occluded(from, from + L.smp[k] * L.range)) f += 1.0f;
+        } else {
+            V3 diffvec = mk(dir.y, -dir.z, dir.x);
+            V3 up = normalized(cross(dir, diffvec));
+            V3 rt = cross(dir, up);
+            for (int k = 0; k < L.nsamples; ++k) {
+                V3 T = L.pos + rt * L.smp[k].x + up * L.smp[k].y;
+                if (occluded(from, T)) f += 1.0f;
+            }
+        }
+        f /= L.nsamples;
+        return 1.0f - f;
+    }
     float closest_bsp(V3 A, V3 B, V3* outn) const   // lighter.cpp:210-251
     {
         V3 dn = normalized(B - A);
@@ -803,6 +881,7 @@ struct ltr_Scene {
     void render_light(const OLight& L, OInst* mi, size_t li);
     void rad_links();
     void rad_bounce();
+    void rad_patches();
     void ao(OInst* mi, const std::vector<float>& randoff);
     void finalize();
     void run();
@@ -1008,7 +1087,8 @@ void ltr_Scene::render_light(const OLight& L, OInst* mi, size_t li)
             } else if (f_dist * f_ndotl <= 0) {
                 return;
             }
-            float vis = inv_shadow(SP + SN * kShadowOffset, L.pos, L.radius);
+            float vis = opt_shadow_mode == 1 ? sampled_vis(L, SP + SN * kShadowOffset, s2l)
+                                             : inv_shadow(SP + SN * kShadowOffset, L.pos, L.radius);
             dvis[i] = vis;
             float k = L.type == 2 ? f_dist * f_ndotl * f_dir * vis : f_dist * f_ndotl * vis;
             mi->lm[i] += L.color * k;
@@ -1016,6 +1096,18 @@ void ltr_Scene::render_light(const OLight& L, OInst* mi, size_t li)
                 float fac = L.type == 2 ? f_dist * f_dir * vis * f_ndotl * brightness(L.color)
                                         : f_dist * vis * f_ndotl * brightness(L.color);
                 if (fac > 0) { Contrib c = {s2l * fac, (i32) i}; contribs[i] = c; }
+            }
+        } else if (opt_shadow_mode == 1) {
+            // the sampled block of lighter.cpp:566-584 (ray origin SP, N.L averaged)
+            float f_ndotl = 0.0f;
+            for (int k = 0; k < L.nsamples; ++k) f_ndotl += fmax_(0.0f, dot(L.smp[k], SN));
+            f_ndotl /= L.nsamples;
+            float vis = sampled_vis(L, SP, L.dir);
+            dvis[i] = vis;
+            mi->lm[i] += L.color * (f_ndotl * vis);
+            if (want_n) {
+                float fac = vis * f_ndotl * brightness(L.color);
+                if (fac > 0) { Contrib c = {L.dir * fac, (i32) i}; contribs[i] = c; }
             }
         } else {
             float f_ndotl = fmax_(0.0f, dot(L.dir, SN));
@@ -1037,6 +1129,7 @@ void ltr_Scene::render_light(const OLight& L, OInst* mi, size_t li)
 // and for which VisibilityTest() reports an occluder (lighter.cpp:667-765).
 void ltr_Scene::rad_links()
 {
+    rad_pos.clear(); rad_nrm.clear(); rad_col.clear(); rad_emit.clear(); links.clear(); linkmap.clear();
     for (OInst* mi : insts) {
         for (size_t i = 0; i < mi->lm.size(); ++i) {
             V3 P = mi->spos[i];
@@ -1068,6 +1161,7 @@ void ltr_Scene::rad_links()
             }
             RadColors rc = {diffc, emit, emit, mk(0, 0, 0), area};
             rad_col.push_back(rc);
+            rad_emit.push_back(emit);
         }
     }
     const size_t N = rad_pos.size();
@@ -1088,6 +1182,190 @@ void ltr_Scene::rad_links()
             RadLink rl = {(u32) j, f};
             links.push_back(rl);
             linkmap.back()++;
+        }
+    }
+}
+
+// Patch radiosity, the GPU library's radiosity_patches mode (no reference
+// counterpart; the pair factor, link test and bounce are the reference's,
+// lighter.cpp:673-797, over patches instead of samples).
+//  1. Per-sample inputs as rad_links gathers them: position, unit normal,
+//     sample_fn diffuse and emission, sample area (probes: black, area 0).
+//  2. A patch slot per covered sample: (instance, lightmap tile of side t
+//     texels, dominant axis and sign of the unit normal), slots numbered
+//     instance by instance, tile row by row, six axes per tile. The side t
+//     starts at round(sqrt(covered / target)) and moves (at most 8 trials)
+//     towards the side whose occupied-slot count comes closest to the target
+//     in |log(count / target)|, stopping once the count crosses the target.
+//  3. Patches = occupied slots in slot order; a patch's area is the sum of its
+//     samples' areas and its position, normal (renormalised), diffuse and
+//     emission the area-weighted means, summed in sample order in double.
+//  4. Links between patches with the pair factor of lighter.cpp:733-757 and
+//     the predicate opt_links (1: the pair is not occluded, 0: it is, as
+//     lighter.cpp:751), then bounce_count sweeps of lighter.cpp:767-797.
+//  5. Every covered sample receives its own emission plus its patch's
+//     bounced light (total - emission); probes keep their direct light.
+void ltr_Scene::rad_patches()
+{
+    struct SIn { V3 diff, emis; u32 inst; size_t idx; };
+    std::vector<SIn> sin;
+    size_t n_cov = 0;
+    for (u32 ii = 0; ii < insts.size(); ++ii) {
+        OInst* mi = insts[ii];
+        for (size_t i = 0; i < mi->lm.size(); ++i) {
+            V3 P = mi->spos[i];
+            V3 N = normalized(mi->snrm[i]);
+            V3 diffc = mk(1, 1, 1), emis = mk(0, 0, 0);
+            if (mi->container) {
+                diffc = mk(0, 0, 0);
+            } else if (cfg.sample_fn) {
+                u32 L = mi->sloc[i];
+                int lx = (int) (L % mi->w), ly = (int) (L / mi->w);
+                ltr_SampleRequest req;
+                req.position[0] = P.x; req.position[1] = P.y; req.position[2] = P.z;
+                req.normal[0] = N.x; req.normal[1] = N.y; req.normal[2] = N.z;
+                req.tex0u = mi->srad[i].x; req.tex0v = mi->srad[i].y;
+                req.tex1u = (lx + 0.5f) / mi->w; req.tex1v = (ly + 0.5f) / mi->h;
+                req.part_id = (uint32_t) mi->srad[i].z;
+                req.mesh_ident = mi->mesh->ident.c_str(); req.mesh_ident_size = mi->mesh->ident.size();
+                req.inst_ident = mi->ident.c_str(); req.inst_ident_size = mi->ident.size();
+                req.out_diffuse_color[0] = 1; req.out_diffuse_color[1] = 1; req.out_diffuse_color[2] = 1;
+                req.out_emissive_color[0] = 0; req.out_emissive_color[1] = 0; req.out_emissive_color[2] = 0;
+                if (cfg.sample_fn(&cfg, &req)) {
+                    diffc = mk(req.out_diffuse_color[0], req.out_diffuse_color[1], req.out_diffuse_color[2]);
+                    emis = mk(req.out_emissive_color[0], req.out_emissive_color[1], req.out_emissive_color[2]);
+                }
+            }
+            SIn e = {diffc, emis, ii, i};
+            sin.push_back(e);
+            if (!mi->container) ++n_cov;
+        }
+    }
+    // 2. slots
+    const u32 target = opt_patches;
+    std::vector<unsigned long long> slot_base(insts.size() + 1, 0);
+    std::vector<u32> ntx(insts.size(), 0);
+    auto layout = [&](u32 t) {
+        for (size_t i = 0; i < insts.size(); ++i) {
+            const OInst* mi = insts[i];
+            ntx[i] = mi->container ? 0 : (mi->w + t - 1) / t;
+            unsigned long long ns = mi->container ? 0 : (unsigned long long) ntx[i] * ((mi->h + t - 1) / t) * 6;
+            slot_base[i + 1] = slot_base[i] + ns;
+        }
+        return slot_base[insts.size()];
+    };
+    auto slot_of = [&](const SIn& e, u32 t) -> unsigned long long {
+        const OInst* mi = insts[e.inst];
+        u32 L = mi->sloc[e.idx], w = mi->w;
+        u32 tx = (L % w) / t, ty = (L / w) / t;
+        V3 nn = normalized(mi->snrm[e.idx]);
+        float ax = std::fabs(nn.x), ay = std::fabs(nn.y), az = std::fabs(nn.z);
+        u32 axis = (ax >= ay && ax >= az) ? (nn.x >= 0 ? 0 : 1) : (ay >= az ? (nn.y >= 0 ? 2 : 3) : (nn.z >= 0 ? 4 : 5));
+        return slot_base[e.inst] + ((unsigned long long) ty * ntx[e.inst] + tx) * 6 + axis;
+    };
+    auto trial = [&](u32 t) -> u32 {
+        layout(t);
+        std::vector<unsigned long long> sl;
+        for (const SIn& e : sin)
+            if (!insts[e.inst]->container) sl.push_back(slot_of(e, t));
+        std::sort(sl.begin(), sl.end());
+        return (u32) (std::unique(sl.begin(), sl.end()) - sl.begin());
+    };
+    u32 tile = (u32) std::max(1.0, std::floor(std::sqrt(std::max(1.0, (double) n_cov / target)) + 0.5));
+    {
+        auto off = [&](u32 c) { return std::fabs(std::log(std::max(1.0, (double) c) / target)); };
+        u32 c = trial(tile), best = tile;
+        double best_off = off(c);
+        const int dir = c > target ? 1 : -1;
+        for (int k = 0; k < 8; ++k) {
+            if ((dir > 0 && c <= target) || (dir < 0 && (c >= target || tile == 1))) break;
+            u32 t2 = (u32) std::floor(tile * std::sqrt((double) c / target) + 0.5);
+            t2 = dir > 0 ? std::max(t2, tile + 1) : std::max(1u, std::min(t2, tile - 1));
+            tile = t2;
+            c = trial(tile);
+            if (off(c) < best_off) { best_off = off(c); best = tile; }
+        }
+        tile = best;
+    }
+    layout(tile);
+    // 3. patches in slot order, samples in sample order
+    std::vector<unsigned long long> sslot(sin.size(), ~0ull);
+    std::vector<unsigned long long> occ;
+    for (size_t k = 0; k < sin.size(); ++k)
+        if (!insts[sin[k].inst]->container) { sslot[k] = slot_of(sin[k], tile); occ.push_back(sslot[k]); }
+    std::sort(occ.begin(), occ.end());
+    occ.erase(std::unique(occ.begin(), occ.end()), occ.end());
+    const size_t np = occ.size();
+    std::vector<long long> pid(sin.size(), -1);
+    std::vector<std::array<double, 13>> q(np);
+    for (auto& a : q) a.fill(0.0);
+    for (size_t k = 0; k < sin.size(); ++k) {
+        if (sslot[k] == ~0ull) continue;
+        size_t p = (size_t) (std::lower_bound(occ.begin(), occ.end(), sslot[k]) - occ.begin());
+        pid[k] = (long long) p;
+        const OInst* mi = insts[sin[k].inst];
+        size_t i = sin[k].idx;
+        double a = mi->srad[i].w;
+        V3 n = normalized(mi->snrm[i]), P = mi->spos[i], D = sin[k].diff;
+        V3 e = mi->lm[i];
+        e += sin[k].emis;
+        double v[13] = {a, a * P.x, a * P.y, a * P.z, a * n.x, a * n.y, a * n.z, a * D.x, a * D.y, a * D.z,
+                        a * e.x, a * e.y, a * e.z};
+        for (int c = 0; c < 13; ++c) q[p][c] += v[c];
+    }
+    rad_pos.assign(np, mk(0, 0, 0));
+    rad_nrm.assign(np, mk(0, 0, 0));
+    rad_col.assign(np, RadColors());
+    rad_emit.assign(np, mk(0, 0, 0));
+    for (size_t p = 0; p < np; ++p) {
+        double a = q[p][0] > 0 ? q[p][0] : 1.0;
+        rad_pos[p] = mk((float) (q[p][1] / a), (float) (q[p][2] / a), (float) (q[p][3] / a));
+        rad_nrm[p] = normalized(mk((float) (q[p][4] / a), (float) (q[p][5] / a), (float) (q[p][6] / a)));
+        V3 E = mk((float) (q[p][10] / a), (float) (q[p][11] / a), (float) (q[p][12] / a));
+        RadColors rc = {mk((float) (q[p][7] / a), (float) (q[p][8] / a), (float) (q[p][9] / a)), E, E, mk(0, 0, 0),
+                        (float) q[p][0]};
+        rad_col[p] = rc;
+        rad_emit[p] = E;
+    }
+    // 4. links (rows on parallel threads, concatenated in row order), then the sweeps
+    std::vector<std::vector<RadLink>> rows(np);
+    parallel_for(threads(), np, [&](size_t i) {
+        V3 AP = rad_pos[i], AN = rad_nrm[i];
+        for (size_t j = i + 1; j < np; ++j) {
+            V3 BP = rad_pos[j], BN = rad_nrm[j];
+            V3 pd = BP - AP;
+            float dA = dot(AN, pd), dB = dot(BN, -pd);
+            if (dA <= kSmall || dB <= kSmall) continue;
+            float l2 = lensq(pd);
+            float f = dA * dB / (l2 * l2 * (float) M_PI);
+            if (f < kSmall) continue;
+            g_rad_vis.fetch_add(1, std::memory_order_relaxed);
+            bool occ_ij = occluded(AP, BP);
+            if (opt_links == 1 ? occ_ij : !occ_ij) continue;
+            RadLink rl = {(u32) j, f};
+            rows[i].push_back(rl);
+        }
+    });
+    links.clear();
+    linkmap.clear();
+    for (size_t i = 0; i < np; ++i) {
+        linkmap.push_back((u32) links.size());
+        linkmap.push_back((u32) rows[i].size());
+        links.insert(links.end(), rows[i].begin(), rows[i].end());
+    }
+    stage = "bouncing light";
+    for (int b = 0; b < cfg.bounce_count; ++b) rad_bounce();
+    stage = "committing radiosity";
+    // 5. own emission plus the patch's bounced light
+    for (size_t k = 0; k < sin.size(); ++k) {
+        OInst* mi = insts[sin[k].inst];
+        V3& c = mi->lm[sin[k].idx];
+        c += sin[k].emis;
+        if (pid[k] >= 0) {
+            const V3 T = rad_col[(size_t) pid[k]].total, E = rad_emit[(size_t) pid[k]];
+            c.x += T.x - E.x;
+            c.y += T.y - E.y;
+            c.z += T.z - E.z;
         }
     }
 }
@@ -1272,6 +1550,7 @@ void ltr_Scene::finalize()
 // Stage order of Job_MainProc (lighter.cpp:1046-1145).
 void ltr_Scene::run()
 {
+    g_watertight = opt_isect == 1;
     int nt = threads();
     stage = "transforming spatial data"; completion = 0;
     parallel_for(nt, insts.size(), [&](size_t i) { prexform(insts[i]); });
@@ -1305,7 +1584,10 @@ void ltr_Scene::run()
             completion = (li + 1) / float(lights.size());
         }
     }
-    if (cfg.bounce_count) {
+    if (cfg.bounce_count && opt_patches) {
+        stage = "calculating radiosity"; completion = 0;
+        rad_patches();
+    } else if (cfg.bounce_count) {
         stage = "calculating radiosity"; completion = 0;
         rad_links();
         stage = "bouncing light"; completion = 0;
@@ -1452,7 +1734,22 @@ API void ltr_LightAdd(ltr_Scene* s, ltr_LightInfo* li)   // lighter.cpp:1282-131
     L.range = li->range; L.power = li->power; L.radius = li->light_radius;
     L.nsamples = li->shadow_sample_count > 1 ? li->shadow_sample_count : 1;
     L.out = li->spot_angle_out; L.in = li->spot_angle_in; L.curve = li->spot_curve;
-    (void) randf();   // the reference draws one value per light; its samples are never read
+    L.randoff = randf();
+    // Shadow samples, read only in the sampled shadow mode (orc_SetOptions).
+    // Directional: lighter.cpp:1300-1310 (the spiral around -direction pulled
+    // towards +direction). Point and spot: golden-angle disk points of radius
+    // light_radius, the project's definition (the reference leaves a TODO).
+    for (int k = 0; k < L.nsamples; ++k) {
+        if (L.type == 3) {
+            V3 adj = spiral_dir(-L.dir, L.randoff, k, L.nsamples);
+            adj = normalized(adj + (-L.dir) * std::tan((L.radius - 0.5f) * (float) M_PI * 0.999f));
+            L.smp.push_back(adj);
+        } else {
+            float rho = L.radius * std::sqrt((k + 0.5f) / L.nsamples);
+            float phi = (k + L.randoff) * (137.508f / 180.0f * (float) M_PI);
+            L.smp.push_back(mk(rho * std::cos(phi), rho * std::sin(phi), 0.0f));
+        }
+    }
     s->lights.push_back(L);
 }
 
@@ -1520,6 +1817,53 @@ API int ltrdbg_GetRayData(ltr_Scene* s, u32 inst, float* vis, float* ao)
         memcpy(ao, mi->dbg_ao.data(), mi->dbg_ao.size() * sizeof(float));
     }
     return 1;
+}
+
+// The radiosity elements of the last bake (samples, or patches in patch mode)
+// in the layout of the GPU library's ltrdbg_GetRadiosity: float4 position,
+// unit normal, (diffuse rgb, area), emission and total; F (may be NULL) the
+// n x n link factors (0 where two elements are not linked).
+API int ltrdbg_GetRadiosity(ltr_Scene* s, u32* n, float* pos4, float* nrm4, float* diff_area4, float* emit4,
+                            float* total4, float* F)
+{
+    const size_t N = s->rad_col.size();
+    if (n) *n = (u32) N;
+    if (!N) return 0;
+    for (size_t i = 0; i < N; ++i) {
+        const RadColors& c = s->rad_col[i];
+        const float v[5][4] = {{s->rad_pos[i].x, s->rad_pos[i].y, s->rad_pos[i].z, 0},
+                               {s->rad_nrm[i].x, s->rad_nrm[i].y, s->rad_nrm[i].z, 0},
+                               {c.diff.x, c.diff.y, c.diff.z, c.area},
+                               {s->rad_emit[i].x, s->rad_emit[i].y, s->rad_emit[i].z, 0},
+                               {c.total.x, c.total.y, c.total.z, 0}};
+        float* dst[5] = {pos4, nrm4, diff_area4, emit4, total4};
+        for (int k = 0; k < 5; ++k)
+            if (dst[k]) memcpy(dst[k] + 4 * i, v[k], sizeof(v[k]));
+    }
+    if (F) {
+        memset(F, 0, N * N * sizeof(float));
+        for (size_t i = 0; i < N && 2 * i + 1 < s->linkmap.size(); ++i) {
+            size_t b = s->linkmap[2 * i], e = b + s->linkmap[2 * i + 1];
+            for (size_t k = b; k < e; ++k) {
+                size_t j = s->links[k].other;
+                F[i * N + j] = F[j * N + i] = s->links[k].f;
+            }
+        }
+    }
+    return 1;
+}
+
+// Modes beyond the reference bake, matching the GPU library's ltrg_Options
+// fields of the same names: v[0] shadow_mode, v[1] intersect_mode, v[2]
+// radiosity_patches, v[3] radiosity_links (n of them given; the rest keep 0).
+API void orc_SetOptions(ltr_Scene* s, const u32* v, u32 n)
+{
+    u32 o[4] = {0, 0, 0, 0};
+    for (u32 k = 0; k < n && k < 4; ++k) o[k] = v[k];
+    s->opt_shadow_mode = o[0];
+    s->opt_isect = o[1];
+    s->opt_patches = o[2];
+    s->opt_links = o[3];
 }
 
 // out[0..3] = shadow evaluations, sphere-trace steps, AO rays, radiosity visibility tests

@@ -273,3 +273,21 @@ def test_rejects_too_many_rhs(small):
         g.solve(sc["albedo"], E, 1, FP16, REFINE_RHS)
     with pytest.raises(RuntimeError, match="at most 256"):
         g.solve(sc["albedo"], E, 1, BF16, REFINE_FULL)
+
+
+@pytest.mark.gpu
+def test_bounded_wait_expires_and_the_next_solve_succeeds(gpu):
+    """A solve whose copy producer issues nothing: the tensor-core kernel's
+    mbarrier waits give up after 20 ms (test limit), the error word reaches
+    ltrg_GatherLastError, the kernel frees its tensor memory and returns, and
+    the next solve on the same gather matches an untouched one bit for bit."""
+    sc = patches.room(seed=4, n_patches=600, n_configs=2)
+    with Gather(gpu, sc["tri"], sc["pos"], sc["nrm"], sc["area"]) as g:
+        ref, _ = g.solve(sc["albedo"], sc["emission"], 2, FP16, REFINE_RHS)
+        g.stall_next_solve(20000)
+        with pytest.raises(RuntimeError, match="wait expired"):
+            g.solve(sc["albedo"], sc["emission"], 1, FP16, REFINE_RHS)
+        assert b"error word" in gpu.ltrg_GatherLastError(g.h)
+        again, st = g.solve(sc["albedo"], sc["emission"], 2, FP16, REFINE_RHS)
+        assert st["tensor_cores"] == 1 and gpu.ltrg_GatherLastError(g.h) is None
+        np.testing.assert_array_equal(again, ref)

@@ -30,6 +30,12 @@ def test_tuning_defaults_and_validation(gpu):
         assert lib.ltrg_SetTuning(0, C.byref(bad)) == 0
         bad.ao_blocks_per_sm, bad.ao_order = 8, 3   # no such order
         assert lib.ltrg_SetTuning(0, C.byref(bad)) == 0
+        bad.ao_order, bad.direct_stack = 1, 5       # stacks: 0, 4, 8 or 16 shared-memory entries
+        assert lib.ltrg_SetTuning(0, C.byref(bad)) == 0
+        bad.direct_stack, bad.ao_chunk = 8, 9       # 1..8 rays per lane per fetch
+        assert lib.ltrg_SetTuning(0, C.byref(bad)) == 0
+        bad.ao_chunk, bad.direct_packet = 1, 2
+        assert lib.ltrg_SetTuning(0, C.byref(bad)) == 0
         assert lib.ltrg_SetTuning(-1, C.byref(t)) == 0
         ok = ext.Tuning()
         C.memmove(C.byref(ok), C.byref(t), C.sizeof(t))
@@ -56,6 +62,35 @@ def test_results_do_not_depend_on_launch_shape(gpu):
         b = bake(lib, d, debug=False)
         for x, y in zip(a.lightmaps, b.lightmaps):
             np.testing.assert_array_equal(x[3], y[3])
+    finally:
+        lib.ltrg_SetTuning(0, C.byref(saved))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shadow_mode", [0, 1])
+def test_results_do_not_depend_on_stack_split_or_wavefront(gpu, shadow_mode):
+    # the traversal stack's shared-memory part (0, 4, 8, 16 entries), the AO rays per lane
+    # per fetch and the warp-cooperative walks change where entries live, which lane traces
+    # which ray and which nodes a walk visits, not any query's result
+    lib = gpu
+    saved = _get(lib)
+    d = scenes.mid(5, lm=128, n_boxes=24, n_spheres=3, bounces=0, ao_rays=8)
+    opts = {"shadow_mode": shadow_mode}
+    try:
+        t = _get(lib)
+        t.direct_stack, t.ao_stack, t.ao_chunk, t.direct_packet, t.ao_packet = 0, 0, 4, 0, 0
+        assert lib.ltrg_SetTuning(0, C.byref(t))
+        ref = bake(lib, d, gpu_options=opts)
+        for k, chunk, regs, packet in ((4, 1, 0, 0), (8, 2, 1, 1), (16, 8, 0, 1), (0, 4, 0, 1), (0, 1, 1, 1)):
+            t.direct_stack, t.ao_stack, t.ao_chunk, t.direct_packet, t.ao_packet = k, k, chunk, packet, packet
+            t.direct_regs = t.sampled_regs = regs
+            assert lib.ltrg_SetTuning(0, C.byref(t))
+            got = bake(lib, d, gpu_options=opts)
+            for x, y in zip(ref.lightmaps, got.lightmaps):
+                np.testing.assert_array_equal(x[3], y[3])
+            for x, y in zip(ref.debug, got.debug):
+                np.testing.assert_array_equal(x["vis"], y["vis"])
+                np.testing.assert_array_equal(x["ao"], y["ao"])
     finally:
         lib.ltrg_SetTuning(0, C.byref(saved))
 

@@ -8,8 +8,10 @@ the device and writes the finished lightmap, using a fixed scratch array in
 the library instead of cudaMalloc. This test feeds it the per-sample colours
 of a normal bake (ltr_Start, read back through ltrdbg_GetSamples) and checks
 its output against the lightmap that the same bake returned through
-ltr_GetWorkOutput, for two calls in a row on lightmaps of different sizes
-(the second call finds the first one's data in the shared scratch).
+ltr_GetWorkOutput, for calls in a row on lightmaps of different sizes (each
+call finds the previous one's data in the shared scratch): square ones, a
+64 x 32 one (the transposed blur swaps width and height) and a 48 x 80 one
+finished without blur (blur_size 0: dilation only).
 Collected last (file name) so that a failure here cannot hide other tests.
 """
 import ctypes as C
@@ -41,17 +43,24 @@ def _scatter(res, inst):
 def test_finalize_no_alloc_matches_bake(gpu):
     torch = pytest.importorskip("torch")
     assert torch.cuda.is_available(), "the no-alloc entry point needs a CUDA device"
-    # two bakes with different lightmap sizes; blur 0.5 is the default config
+    # bakes with different lightmap sizes; blur 0.5 is the default config
     res_a = bake(gpu, scenes.cornell(11, lm=64, bounces=0, ao=True))
     res_b = bake(gpu, scenes.cornell(12, lm=32, bounces=0, ao=True))
+    d_c = scenes.cornell(13, lm=64, bounces=0, ao=True)
+    d_c.fixed_lm_size = (64, 32)
+    res_c = bake(gpu, d_c)
+    d_d = scenes.cornell(14, lm=64, bounces=0, ao=True)
+    d_d.fixed_lm_size = (48, 80)
+    d_d.config["blur_size"] = 0.0
+    res_d = bake(gpu, d_d)
     stream = torch.cuda.current_stream().cuda_stream
-    for res, inst in ((res_a, 1), (res_b, 7)):
+    for res, inst, blur in ((res_a, 1, 0.5), (res_b, 7, 0.5), (res_c, 3, 0.5), (res_d, 2, 0.0)):
         rgb, mask, want, w, h = _scatter(res, inst)
         d_rgb = torch.from_numpy(rgb).cuda()
         d_mask = torch.from_numpy(mask).cuda()
         d_out = torch.full((h * w, 3), float("nan"), dtype=torch.float32, device="cuda")
         torch.cuda.synchronize()
-        rc = gpu.ltrg_FinalizeLightmapNoAlloc(d_rgb.data_ptr(), d_mask.data_ptr(), d_out.data_ptr(), w, h, 0.5,
+        rc = gpu.ltrg_FinalizeLightmapNoAlloc(d_rgb.data_ptr(), d_mask.data_ptr(), d_out.data_ptr(), w, h, blur,
                                               C.c_void_p(stream))
         assert rc == ext.NOALLOC_OK
         torch.cuda.synchronize()
