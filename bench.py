@@ -139,20 +139,75 @@ def _barrier(dist):
     replicas.barrier(dist)
 
 
-def _oracle_bake(desc, threads):
-    """One bake of `desc` on the CPU oracle port; returns (rays, seconds, counters)."""
+def _oracle_bake(desc, threads, keep=False):
+    """One bake of `desc` on the CPU oracle port; returns (rays, seconds, counters),
+    plus the bake's result when `keep`."""
     import ctypes as C
     from lighter_gb300 import load_library
     from lighter_gb300.scene import bake
     orc = load_library(os.path.join(ROOT, "oracle", "liblighter_oracle.so"),
                        extra={"orc_GetCounters": (None, [C.c_void_p])})
     t0 = time.perf_counter()
-    bake(orc, desc, threads=threads, debug=False)
+    res = bake(orc, desc, threads=threads, debug=False)
     dt = time.perf_counter() - t0
     cnt = (C.c_ulonglong * 4)()
     orc.orc_GetCounters(C.cast(cnt, C.c_void_p))
     rays = cnt[0] + cnt[2] + cnt[3]
+    if keep:
+        return rays, dt, list(cnt), res
     return rays, dt, list(cnt)
+
+
+def _parity(gpu_res, orc_res):
+    """Per-texel agreement of two bakes of the same scene: the largest and the
+    mean |gpu - oracle| over every lightmap relative to that lightmap's peak, and
+    the fraction of texels off by more than 1e-3 of it (the parity tests' bars)."""
+    import numpy as np
+    mx = mean = 0.0
+    over = tot = 0
+    for a, b in zip(gpu_res.lightmaps, orc_res.lightmaps):
+        la, lb = a[3], b[3]
+        peak = max(float(np.abs(lb).max()), 1e-6)
+        d = np.abs(la - lb)
+        mx = max(mx, float(d.max()) / peak)
+        mean = max(mean, float(d.mean()) / peak)
+        over += int((d.max(-1) > 1e-3 * peak).sum())
+        tot += d.shape[0] * d.shape[1]
+    return {"max_abs_rel": mx, "mean_abs_rel": mean, "frac_over_1e-3": over / max(tot, 1),
+            "lightmaps": len(gpu_res.lightmaps), "bars": {"max_abs_rel": 1e-5, "mean_abs_rel": 1e-6, "frac_over_1e-3": 0.0}}
+
+
+def _profile_fields(name):
+    """`measured:` key=value pairs of a committed ncu summary under profiles/ (floats)."""
+    out = {}
+    try:
+        with open(os.path.join(ROOT, "profiles", name)) as f:
+            for line in f:
+                if line.startswith("measured:"):
+                    for kv in line.split(":", 1)[1].split():
+                        k, v = kv.split("=", 1)
+                        out[k] = float(v)
+    except OSError:
+        pass
+    return out
+
+
+def _trace_roofline(kernel, profile, items, ms, sm_mhz, n_sm, unit_name):
+    """Roofline block of a BVH trace kernel against the resource it is bound by:
+    instruction issue (one warp instruction per scheduler and clock, 4 schedulers
+    per SM). achieved = warp instructions per item (ncu, same scene at a quarter
+    of the texels) x items / the kernel's CUDA-event time; the ncu fractions of
+    the captured launch (issue slots, lanes per instruction, L1) come with it."""
+    m = _profile_fields(profile)
+    ipi = m.get("warp_inst_per_item")
+    block = {"kernel": kernel, "bound": "issue", "unit": "warp-instructions/s", "items": items,
+             "item": unit_name, "kernel_ms": ms, "source": "profiles/" + profile, "ncu": m or None}
+    if ipi and ms > 0 and sm_mhz:
+        ach = ipi * items / (ms / 1000.0)
+        peak = 4.0 * n_sm * sm_mhz * 1e6
+        block.update({"achieved": ach, "peak": peak, "frac": ach / peak,
+                      "peak_source": "4 schedulers x %d SMs x the median SM clock sampled during the run" % n_sm})
+    return block
 
 
 def run_reference(args, world, rank, dist):
@@ -466,6 +521,41 @@ def run_headline(args, local, single):
     }
 
 
+SAMPLED_WORKLOAD = ("mid scene as the headline workload (seed 1) with sampled soft shadows: shadow_sample_count = 64 "
+                    "visibility rays per (sample, light) pair on a disk of radius 0.2 m around each point and spot light; "
+                    "one shadow ray counted per (texel, light, sample)")
+
+
+def run_sampled(args, local):
+    """The headline scene with LTRG_SHADOW_SAMPLED: the configured 64 shadow rays per
+    (sample, light) pair. One warm-up bake, then the median of three timed bakes:
+    shadow rays/s over the shadow-trace kernel's CUDA-event time."""
+    from lighter_gb300 import library, scenes
+    from lighter_gb300.ext import get_stats
+    from lighter_gb300.scene import ingest
+    lib = library()
+    desc = scenes.large(seed=1, lm=args.lm) if args.scene == "large" else scenes.mid(seed=1, lm=args.lm)
+    scene, keep = ingest(lib, desc, gpu_options={"device": local, "radiosity_patches": args.patches,
+                                                 "radiosity_links": 1, "shadow_mode": 1})
+    try:
+        _bake_once(lib, scene)
+        st = []
+        for _ in range(3):
+            _bake_once(lib, scene)
+            st.append(get_stats(lib, scene))
+    finally:
+        lib.ltr_DestroyScene(scene)
+        del keep
+    st.sort(key=lambda x: x["ms_direct_trace"])
+    m = st[1]
+    rays = m["shadow_evals"]
+    return {"workload": SAMPLED_WORKLOAD, "shadow_rays": rays, "shadow_pairs": m["shadow_pairs"],
+            "kernel_ms": m["ms_direct_trace"], "stage_ms": m["ms_direct"],
+            "shadow_rays_per_s": rays / (m["ms_direct_trace"] / 1000.0) if m["ms_direct_trace"] > 0 else None,
+            "bake_device_ms": m["ms_device"],
+            "rays_per_s_device": (rays + m["ao_rays"] + m["rad_vis_rays"]) / (m["ms_device"] / 1000.0)}
+
+
 def _bake_once(lib, scene):
     lib.ltr_Start(scene)
     if not lib.ltrg_Wait(scene):
@@ -494,6 +584,7 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-sampled", action="store_true", help="skip the sampled soft-shadow bake")
     ap.add_argument("--headline-scenes", type=int, default=4)
     ap.add_argument("--no-headline", action="store_true",
                     help="skip the batched FP16 mid-scene bake compared with the plain FP32 one")
@@ -569,11 +660,29 @@ def main():
             "frac": (s0["texels"] * TEXEL_STAGE_BYTES / (s0["ms_finalize"] / 1000.0) / 1e9 / peak) if s0["ms_finalize"] > 0 else 0.0,
         },
         "rays_per_step": {"shadow": s0["shadow_evals"], "ao": s0["ao_rays"], "radiosity_visibility": s0["rad_vis_rays"]},
+        # the two trace kernels apart: 97% of the rays above are short AO rays, while the
+        # sphere-traced shadow pairs take the larger share of the device time
+        "shadow_pairs_per_s": s0["shadow_pairs"] / (s0["ms_direct_trace"] / 1000.0) if s0["ms_direct_trace"] > 0 else None,
+        "ao_rays_per_s": s0["ao_rays"] / (s0["ms_ao_trace"] / 1000.0) if s0["ms_ao_trace"] > 0 else None,
+        "trace_kernels_ms": {"k_direct_trace": s0["ms_direct_trace"], "k_ao_rays": s0["ms_ao_trace"]},
         "distance_queries_per_s": s0["distance_queries"] / (s0["ms_device"] / 1000.0),
         "stages_ms": {k: round(s0[k], 3) for k in ("ms_upload", "ms_bvh", "ms_samples", "ms_direct", "ms_rad_links",
                                                     "ms_rad_bounce", "ms_ao", "ms_finalize", "ms_download",
                                                     "ms_device", "ms_total")},
     }
+    try:
+        import torch
+        n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+    except Exception:
+        n_sm = 152
+    line["trace_rooflines"] = {
+        "shadow": _trace_roofline("k_direct_trace", "k_direct_trace_mid512.md", s0["shadow_pairs"],
+                                  s0["ms_direct_trace"], clocks.get("sm_mhz"), n_sm, "(sample, light) pair"),
+        "ao": _trace_roofline("k_ao_rays", "k_ao_rays_mid512.md", s0["ao_rays"], s0["ms_ao_trace"],
+                              clocks.get("sm_mhz"), n_sm, "AO ray"),
+    }
+    if not args.no_sampled:
+        line["sampled_shadows"] = run_sampled(args, local)
     if not args.no_rad_precisions:
         from lighter_gb300 import library, scenes
         desc = scenes.large(seed=1, lm=args.lm) if args.scene == "large" else scenes.mid(seed=1, lm=args.lm)
@@ -607,11 +716,17 @@ def main():
         line["cpu_baseline_note"] = ("not run for the 1.2M-triangle scene: the reference's per-instance BSP "
                                      "(PickSplitPlane, O(points^2) per node) makes its sample stage impractical")
     elif not args.no_cpu_baseline:
-        from lighter_gb300 import scenes
+        from lighter_gb300 import library, scenes
+        from lighter_gb300.scene import bake
         threads = os.cpu_count() or 1
-        r, dt, cnt = _oracle_bake(scenes.mid(seed=1, lm=args.cpu_lm, bounces=0), threads)
+        desc = scenes.mid(seed=1, lm=args.cpu_lm, bounces=0)
+        r, dt, cnt, ores = _oracle_bake(desc, threads, keep=True)
         line["cpu_baseline"] = {"value": r / dt, "unit": "rays/s", "cores": threads, "kind": "port",
                                 "sample": CPU_SAMPLE, "seconds": dt}
+        # the GPU's bake of the same sample against the oracle's output just made
+        gres = bake(library(), desc, debug=False, gpu_options={"device": local})
+        line["parity"] = dict(_parity(gres, ores), sample=CPU_SAMPLE, against="the oracle port's bake of the "
+                              "cpu_baseline leg (the reference's algorithm restated, pinned to the reference's outputs)")
     print(json.dumps(line), flush=True)
     return 0
 
