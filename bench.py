@@ -556,6 +556,53 @@ def run_sampled(args, local):
             "rays_per_s_device": (rays + m["ao_rays"] + m["rad_vis_rays"]) / (m["ms_device"] / 1000.0)}
 
 
+LARGE_WORKLOAD = ("large (C3): fBm terrain 1024x512 quads (1.05M tris) in 16 tiles + 2000 80-tri rocks, ~1.2M tris, "
+                  "16 x 2048^2 lightmaps, 1 directional + 32 point lights, AO 64 rays r=2 m, radiosity 3 bounces over "
+                  "~64k patches; FP32 F, then FP16 F with the last bounce refined")
+
+
+def run_large(args, local):
+    """The large terrain scene: one warm-up bake and one timed bake with FP32 form
+    factors, then one with FP16 F (last of 3 bounces refined in FP32): device and
+    wall times, rays/s, s per bounce and the FP16 bake's largest lightmap
+    difference from the FP32 one (relative to each lightmap's peak)."""
+    import numpy as np
+    from lighter_gb300 import library, scenes
+    from lighter_gb300.ext import get_stats
+    from lighter_gb300.scene import _collect, ingest
+    lib = library()
+    desc = scenes.large(seed=1, lm=2048)
+    out = {"workload": LARGE_WORKLOAD}
+    base = None
+    for name, prec, refine in (("fp32", 0, 0), ("fp16_refine1", 1, 1)):
+        scene, keep = ingest(lib, desc, gpu_options={"device": local, "radiosity_patches": 65536, "radiosity_links": 1,
+                                                     "radiosity_precision": prec, "refine_steps": refine})
+        try:
+            if base is None:
+                _bake_once(lib, scene)
+            t0 = time.perf_counter()
+            _bake_once(lib, scene)
+            wall = time.perf_counter() - t0
+            st = get_stats(lib, scene)
+            lms = [x[3] for x in _collect(lib, scene, False, [], 0.0, "finished").lightmaps]
+        finally:
+            lib.ltr_DestroyScene(scene)
+            del keep
+        rays = st["shadow_evals"] + st["ao_rays"] + st["rad_vis_rays"]
+        rec = {"device_ms": st["ms_device"], "wall_ms": wall * 1000.0, "rays": rays,
+               "rays_per_s_device": rays / (st["ms_device"] / 1000.0), "rays_per_s_e2e": rays / wall,
+               "s_per_bounce": st["ms_rad_bounce"] / 3 / 1000.0, "patches": st["rad_elements"],
+               "ms_direct_trace": st["ms_direct_trace"], "ms_ao_trace": st["ms_ao_trace"],
+               "shadow_pairs": st["shadow_pairs"], "ao_rays": st["ao_rays"], "triangles": st["triangles"]}
+        if base is None:
+            base = lms
+        else:
+            rec["max_rel_err_vs_fp32"] = max(float(np.abs(a - b).max()) / max(float(np.abs(b).max()), 1e-12)
+                                             for a, b in zip(lms, base))
+        out[name] = rec
+    return out
+
+
 def _bake_once(lib, scene):
     lib.ltr_Start(scene)
     if not lib.ltrg_Wait(scene):
@@ -585,6 +632,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-sampled", action="store_true", help="skip the sampled soft-shadow bake")
+    ap.add_argument("--no-large", action="store_true", help="skip the large terrain scene's bakes")
     ap.add_argument("--headline-scenes", type=int, default=4)
     ap.add_argument("--no-headline", action="store_true",
                     help="skip the batched FP16 mid-scene bake compared with the plain FP32 one")
@@ -683,6 +731,8 @@ def main():
     }
     if not args.no_sampled:
         line["sampled_shadows"] = run_sampled(args, local)
+    if not args.no_large and args.scene == "mid":
+        line["large_scene"] = run_large(args, local)
     if not args.no_rad_precisions:
         from lighter_gb300 import library, scenes
         desc = scenes.large(seed=1, lm=args.lm) if args.scene == "large" else scenes.mid(seed=1, lm=args.lm)
