@@ -92,8 +92,9 @@ typedef struct ltrg_Stats {
     uint64_t ao_rays;         /* AO segment queries */
     uint64_t rad_pairs;       /* radiosity pairs i<j examined */
     uint64_t rad_vis_rays;    /* pairs that passed the facing/form-factor tests */
-    uint64_t node_visits;     /* BVH internal nodes visited by the direct-light queries */
-    uint64_t tri_tests;       /* point/triangle distance tests of the direct-light queries */
+    uint64_t node_visits;     /* BVH internal nodes fetched by the direct-light distance queries (a
+                                 walk shared by a warp, ltrg_Tuning.direct_packet, counts a node once) */
+    uint64_t tri_tests;       /* leaf triangles fetched for their point/triangle distance (likewise) */
     uint64_t rad_elements;    /* radiosity elements: samples, or patches in patch mode */
     uint64_t kernel_launches; /* CUDA kernels this library launched for the bake */
     uint64_t bytes_h2d;       /* host->device bytes copied for the bake */
@@ -257,12 +258,12 @@ typedef struct ltrg_Tuning {
                                  0 = sample order, 1 = by lightmap texel (Morton order per instance),
                                  2 = by position (3D Morton order in the scene bounds); default 2 */
     u32 ao_order;             /* the same for the AO rays; default 1 */
-    u32 direct_regs;          /* 0 = the shadow-trace kernel's registers as compiled, 1 = capped at 64
-                                 (more warps per SM, some spills), for sphere-traced shadows;
-                                 default 0 */
+    u32 direct_regs;          /* register budget of the shadow-trace kernel for sphere-traced shadows:
+                                 0 = as compiled (at most 128), 1 = 64, 2 = 72, 3 = 80 per thread (more
+                                 warps per SM, some spills); default 0 */
     u32 direct_stack;         /* traversal-stack entries per thread kept in shared memory by the
-                                 shadow-trace kernel's per-lane walks (0, 4, 8 or 16; deeper entries
-                                 stay in local memory); default 0 */
+                                 shadow-trace kernel's per-lane walks with register budget 0 or 1
+                                 (0, 4, 8 or 16; deeper entries stay in local memory); default 0 */
     u32 ao_stack;             /* the same for the AO-ray kernel; default 0 */
     u32 ao_chunk;             /* AO wavefront: rays per lane per work fetch of a warp (1..8; a warp
                                  takes 32 x ao_chunk rays); default 1 */
@@ -272,13 +273,13 @@ typedef struct ltrg_Tuning {
                                  lane. Same results either way; default 1 */
     u32 sampled_regs;         /* direct_regs for sampled shadows (LTRG_SHADOW_SAMPLED); default 1 */
     u32 ao_packet;            /* 1: the 32 AO rays a warp traces at a step share one BVH walk (each
-                                 lane keeping its own segment and closest hit); default 0 */
+                                 lane keeping its own segment and closest hit); default 1 */
     u32 reserved[3];
 } ltrg_Tuning;
 LTRAPI LTRBOOL ltrg_GetTuning(int device, ltrg_Tuning* out);
 /* Values outside 32..512 threads (multiples of 32), 1..64 blocks per SM, orders above 2,
- * direct_regs, sampled_regs, direct_packet or ao_packet above 1, stacks other than 0, 4, 8 and 16
- * or ao_chunk outside 1..8 are rejected. */
+ * direct_regs or sampled_regs above 3, direct_packet or ao_packet above 1, stacks other than 0, 4, 8
+ * and 16 or ao_chunk outside 1..8 are rejected. */
 LTRAPI LTRBOOL ltrg_SetTuning(int device, const ltrg_Tuning* t);
 /* Autotuner: bakes `scene` (not running; its device) repeatedly, coordinate
  * descent over the candidate shapes of each kernel, each timed by that

@@ -72,6 +72,7 @@ ltrg_Tuning default_tuning()
     t.ao_chunk = 1;
     t.direct_packet = 1;
     t.sampled_regs = 1;
+    t.ao_packet = 1;
     return t;
 }
 
@@ -81,9 +82,9 @@ bool tuning_valid(const ltrg_Tuning& t)
     auto bps_ok = [](u32 k) { return k >= 1 && k <= 64; };
     auto stack_ok = [](u32 k) { return k == 0 || k == 4 || k == 8 || k == 16; };
     return block_ok(t.direct_block) && block_ok(t.ao_block) && bps_ok(t.direct_blocks_per_sm) && bps_ok(t.ao_blocks_per_sm) &&
-           t.direct_order <= 2 && t.ao_order <= 2 && t.direct_regs <= 1 && stack_ok(t.direct_stack) &&
+           t.direct_order <= 2 && t.ao_order <= 2 && t.direct_regs <= 3 && stack_ok(t.direct_stack) &&
            stack_ok(t.ao_stack) && t.ao_chunk >= 1 && t.ao_chunk <= 8 && t.direct_packet <= 1 &&
-           t.sampled_regs <= 1 && t.ao_packet <= 1;
+           t.sampled_regs <= 3 && t.ao_packet <= 1;
 }
 }  // namespace
 
@@ -449,10 +450,10 @@ LTRAPI LTRBOOL ltrg_Autotune(ltr_Scene* scene, ltrg_Tuning* out)
         {&ltrg_Tuning::direct_blocks_per_sm, true, {2, 4, 8, 16, 32}},
         {&ltrg_Tuning::direct_block, true, {64, 128, 256}},
         {&ltrg_Tuning::direct_order, true, {0, 1, 2}},
-        {&ltrg_Tuning::direct_regs, true, {0, 1}},
+        {&ltrg_Tuning::direct_regs, true, {0, 1, 2, 3}},
         {&ltrg_Tuning::direct_stack, true, {0, 4, 8, 16}},
         {&ltrg_Tuning::direct_packet, true, {0, 1}},
-        {&ltrg_Tuning::sampled_regs, true, {0, 1}},
+        {&ltrg_Tuning::sampled_regs, true, {0, 1, 2, 3}},
         {&ltrg_Tuning::ao_blocks_per_sm, false, {4, 8, 16, 32}},
         {&ltrg_Tuning::ao_block, false, {64, 128, 256}},
         {&ltrg_Tuning::ao_order, false, {0, 1, 2}},

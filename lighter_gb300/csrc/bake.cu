@@ -789,12 +789,15 @@ __device__ __forceinline__ void direct_pair_finish(const DirectArgs& a, u32 w, c
 // kMinBlocks 2 caps the registers at 64 (two blocks of 512 threads per SM):
 // more warps in flight for the latency-bound walks, at the price of a few
 // spills; which is faster depends on the scene (tuning direct_regs).
-// kStackK: traversal-stack entries kept in shared memory by the per-lane walks
-// (TStack; tuning direct_stack). kPacket: the shadow traces of a warp's 32
-// pairs run together (inv_shadow_warp, sampled_vis_warp; tuning direct_packet).
-template <int kMinBlocks, int kStackK, bool kPacket>
-__global__ void __launch_bounds__(512, kMinBlocks) k_direct_trace(DirectArgs a, const u32* __restrict__ items, const u32* __restrict__ n_items_dev,
-                               u32* __restrict__ next)
+// kRegCap: registers per thread at most (128: as compiled for blocks of up to
+// 512 threads; 64, 72, 80: more warps per SM for the latency-bound walks, at
+// the price of spills; tuning direct_regs / sampled_regs). kStackK:
+// traversal-stack entries kept in shared memory by the per-lane walks (TStack;
+// tuning direct_stack). kPacket: the shadow traces of a warp's 32 pairs run
+// together (inv_shadow_warp, sampled_vis_warp; tuning direct_packet).
+template <int kRegCap, int kStackK, bool kPacket>
+__global__ void __launch_bounds__(512) __maxnreg__(kRegCap)
+    k_direct_trace(DirectArgs a, const u32* __restrict__ items, const u32* __restrict__ n_items_dev, u32* __restrict__ next)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     TStack<kStackK> st = make_stack<kStackK>(smem);
@@ -1154,31 +1157,36 @@ __global__ void k_ao_rays(AoArgs a, float* __restrict__ hits, unsigned long long
 // Launch of the two trace kernels with the tuning's register budget, stack
 // split, walk sharing and wavefront size. Dynamic shared memory: the short
 // stacks, K entries of 8 bytes per thread.
-template <int kMinBlocks, int K, bool kPacket = false>
+template <int kRegCap, int K, bool kPacket = false>
 void launch_direct_k(unsigned grid, unsigned block, cudaStream_t st, const DirectArgs& da, const u32* items,
                      const u32* n_items, u32* next)
 {
     const size_t smem = (size_t) K * block * 8;
     if (smem > 48 * 1024)
-        CK(cudaFuncSetAttribute(k_direct_trace<kMinBlocks, K, kPacket>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CK(cudaFuncSetAttribute(k_direct_trace<kRegCap, K, kPacket>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int) smem));
-    k_direct_trace<kMinBlocks, K, kPacket><<<grid, block, smem, st>>>(da, items, n_items, next);
+    k_direct_trace<kRegCap, K, kPacket><<<grid, block, smem, st>>>(da, items, n_items, next);
 }
 
-template <int kMinBlocks>
+// The shared-memory stack split is built for the per-lane walks with 128 and
+// 64 registers; the other budgets run the per-lane walks with local stacks.
+template <int kRegCap>
 void launch_direct_r(unsigned stack, bool packet, unsigned grid, unsigned block, cudaStream_t st, const DirectArgs& da,
                      const u32* items, const u32* n_items, u32* next)
 {
     if (packet) {   // the warp's walks share one stack in registers; the shared-memory split does not apply
-        launch_direct_k<kMinBlocks, 0, true>(grid, block, st, da, items, n_items, next);
+        launch_direct_k<kRegCap, 0, true>(grid, block, st, da, items, n_items, next);
         return;
     }
-    switch (stack) {
-    case 4: launch_direct_k<kMinBlocks, 4>(grid, block, st, da, items, n_items, next); break;
-    case 8: launch_direct_k<kMinBlocks, 8>(grid, block, st, da, items, n_items, next); break;
-    case 16: launch_direct_k<kMinBlocks, 16>(grid, block, st, da, items, n_items, next); break;
-    default: launch_direct_k<kMinBlocks, 0>(grid, block, st, da, items, n_items, next); break;
+    if constexpr (kRegCap == 128 || kRegCap == 64) {
+        switch (stack) {
+        case 4: launch_direct_k<kRegCap, 4>(grid, block, st, da, items, n_items, next); return;
+        case 8: launch_direct_k<kRegCap, 8>(grid, block, st, da, items, n_items, next); return;
+        case 16: launch_direct_k<kRegCap, 16>(grid, block, st, da, items, n_items, next); return;
+        default: break;
+        }
     }
+    launch_direct_k<kRegCap, 0>(grid, block, st, da, items, n_items, next);
 }
 
 void launch_direct_trace(const ltrg_Tuning& tu, unsigned grid, cudaStream_t st, const DirectArgs& da, const u32* items,
@@ -1186,8 +1194,12 @@ void launch_direct_trace(const ltrg_Tuning& tu, unsigned grid, cudaStream_t st, 
 {
     const bool packet = tu.direct_packet != 0;
     const u32 regs = da.shadow_mode == LTRG_SHADOW_SAMPLED ? tu.sampled_regs : tu.direct_regs;
-    if (regs == 1) launch_direct_r<2>(tu.direct_stack, packet, grid, tu.direct_block, st, da, items, n_items, next);
-    else launch_direct_r<1>(tu.direct_stack, packet, grid, tu.direct_block, st, da, items, n_items, next);
+    switch (regs) {
+    case 1: launch_direct_r<64>(tu.direct_stack, packet, grid, tu.direct_block, st, da, items, n_items, next); break;
+    case 2: launch_direct_r<72>(tu.direct_stack, packet, grid, tu.direct_block, st, da, items, n_items, next); break;
+    case 3: launch_direct_r<80>(tu.direct_stack, packet, grid, tu.direct_block, st, da, items, n_items, next); break;
+    default: launch_direct_r<128>(tu.direct_stack, packet, grid, tu.direct_block, st, da, items, n_items, next); break;
+    }
 }
 
 template <int K, bool kPacket = false>

@@ -559,13 +559,16 @@ __device__ __forceinline__ float warp_distance(const BvhView& b, V3 p, float d0,
                                                u32& nt)
 {
     float dist = d0;
-    if (b.n_tris <= 0 || !__any_sync(0xffffffffu, active)) return dist;
+    const unsigned am = __ballot_sync(0xffffffffu, active);
+    if (b.n_tris <= 0 || !am) return dist;
+    // the walk's node and leaf fetches are counted once for the warp, by its lowest active lane
+    const bool counter = (int) (threadIdx.x & 31) == __ffs(am) - 1;
     int s0 = 0, s1 = 0, sp = 0;
     int cur = b.root;
     for (;;) {
         if (cur >= 0) {
             const NodeBoxes nb = load_node(b, cur);
-            if (active) ++nv;
+            if (counter) ++nv;
             const float lim = dist * dist;
             const float dl = box_d2(nb.lmin, nb.lmax, p), dr = box_d2(nb.rmin, nb.rmax, p);
             const bool hl = active && dl <= lim, hr = active && dr <= lim;
@@ -581,9 +584,9 @@ __device__ __forceinline__ float warp_distance(const BvhView& b, V3 p, float d0,
         } else {
             const int t = ~cur;
             const u32 meta = __float_as_uint(__ldg(&b.drec[8 * (size_t) t + 4]).w);
+            if (counter && (meta & kOccluderBit)) ++nt;
             if (active && (meta & kOccluderBit)) {
                 const float nd = point_tri_dist_rec(b, t, p);
-                ++nt;
                 if (nd < dist) dist = nd;
             }
         }

@@ -221,10 +221,12 @@ template <int B> struct RawF;
 template <> struct RawF<16> {
     uint4 u;
     __device__ __forceinline__ void load(const void* p) { u = __ldcs(reinterpret_cast<const uint4*>(p)); }
+    __device__ __forceinline__ unsigned bits() const { return u.x | u.y | u.z | u.w; }
 };
 template <> struct RawF<8> {
     uint2 u;
     __device__ __forceinline__ void load(const void* p) { u = __ldcs(reinterpret_cast<const uint2*>(p)); }
+    __device__ __forceinline__ unsigned bits() const { return u.x | u.y; }
 };
 template <class T, int V> __device__ __forceinline__ void unpack(const void* raw, float* v)
 {
@@ -294,6 +296,14 @@ __global__ void __launch_bounds__(256) k_rad_gemv(u32 n, size_t ld, const T* __r
 #pragma unroll
             for (int r = 0; r < kRadRows; ++r) nxt[r].load(rows[r] + (size_t) cn * V);
         }
+        // F is sparse (pairs more than a few metres apart have factors below
+        // SMALL_FLOAT, and occluded pairs are 0): a vector that is zero in all the
+        // warp's rows is skipped with one test (F holds no negative values and its
+        // zeros are +0, so "no bit set" is "all entries zero")
+        unsigned nz = 0;
+#pragma unroll
+        for (int r = 0; r < kRadRows; ++r) nz |= cur[r].bits();
+        if (nz) {
         float f[kRadRows][V];
 #pragma unroll
         for (int r = 0; r < kRadRows; ++r) unpack<T, V>(&cur[r].u, f[r]);
@@ -317,118 +327,6 @@ __global__ void __launch_bounds__(256) k_rad_gemv(u32 n, size_t ld, const T* __r
                 }
             }
         }
-#pragma unroll
-        for (int r = 0; r < kRadRows; ++r) cur[r] = nxt[r];
-        c = cn;
-    }
-#pragma unroll
-    for (int r = 0; r < kRadRows; ++r)
-#pragma unroll
-        for (int q = 0; q < 3; ++q)
-            for (int o = 16; o > 0; o >>= 1) acc[r][q] += __shfl_down_sync(0xffffffffu, acc[r][q], o);
-    if (lane == 0) {
-#pragma unroll
-        for (int r = 0; r < kRadRows; ++r) {
-            if (r0 + r >= n) continue;
-            const float s = (!kExact && up) ? up[r0 + r] : 1.0f;   // row scale of an FP16 F (exact)
-            Y[r0 + r] = make_float4(acc[r][0] * s, acc[r][1] * s, acc[r][2] * s, 0.0f);
-        }
-    }
-}
-
-// Y = F X for a 16-bit F, with X staged per block in shared memory. The split
-// of columns over lanes (V consecutive entries per lane, the lanes of a warp
-// on 32 consecutive vectors, then the next 32), the per-row order of the sums
-// and the warp reduction are k_rad_gemv's, so kExact still reproduces the FP32
-// product bit for bit; only where X_j comes from changes. In k_rad_gemv every
-// lane reads its V values of X straight from global memory at a stride of
-// V x 16 bytes between lanes, which for V = 8 (16-bit F, 16-byte loads) puts
-// the 32 lanes of one load on 32 different cache lines, twice the L1 work per
-// F byte of the FP32 kernel. Here a block of 8 warps (32 rows) walks the
-// columns one tile of 32 V at a time; the block copies the tile of X (and, for
-// kExact, of the positions and normals) into shared memory with coalesced
-// loads, and lanes read it back through an XOR swizzle (slot q ^ ((q >> 3) & 7))
-// that gives the 8 lanes of each 128-byte shared-memory phase distinct banks.
-template <class T, bool kExact>
-__global__ void __launch_bounds__(256) k_rad_gemv16(u32 n, size_t ld, const T* __restrict__ F,
-                                                    const float4* __restrict__ pos, const float4* __restrict__ nrm,
-                                                    const float* __restrict__ up, const float4* __restrict__ X,
-                                                    float4* __restrict__ Y)
-{
-    static_assert(sizeof(T) == 2, "16-bit F only");
-    constexpr int V = kExact ? 4 : 8;
-    constexpr int kTile = 32 * V;
-    constexpr int kArrays = kExact ? 3 : 1;
-    __shared__ float4 xs[kArrays][kTile];
-    using Raw = RawF<V * sizeof(T)>;
-    const int lane = threadIdx.x & 31;
-    const u32 r0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * kRadRows;
-    const T* rows[kRadRows];
-    V3 ap[kRadRows], an[kRadRows];
-    u32 ri[kRadRows];
-#pragma unroll
-    for (int r = 0; r < kRadRows; ++r) {
-        ri[r] = min(r0 + r, n - 1);   // rows past n repeat the last row and are not written
-        rows[r] = F + (size_t) ri[r] * ld;
-        if (kExact) { ap[r] = ld3(pos[ri[r]]); an[r] = ld3(nrm[ri[r]]); }
-    }
-    float acc[kRadRows][3];
-#pragma unroll
-    for (int r = 0; r < kRadRows; ++r) acc[r][0] = acc[r][1] = acc[r][2] = 0.0f;
-    const u32 nv = (u32) (ld / V);
-    const u32 n_tiles = (nv + 31) / 32;
-    Raw cur[kRadRows];
-    u32 c = lane;
-    if (c < nv) {
-#pragma unroll
-        for (int r = 0; r < kRadRows; ++r) cur[r].load(rows[r] + (size_t) c * V);
-    }
-    const float4 zero = make_float4(0, 0, 0, 0);
-    for (u32 tile = 0; tile < n_tiles; ++tile) {
-        const u32 col0 = tile * kTile;
-        __syncthreads();   // every warp is done with the previous tile
-        for (int q = threadIdx.x; q < kTile; q += blockDim.x) {
-            const u32 j = col0 + q;
-            const int slot = q ^ ((q >> 3) & 7);
-            xs[0][slot] = j < n ? X[j] : zero;
-            if (kExact) {
-                xs[1 % kArrays][slot] = j < n ? pos[j] : zero;
-                xs[2 % kArrays][slot] = j < n ? nrm[j] : zero;
-            }
-        }
-        __syncthreads();
-        const u32 cn = c + 32;
-        Raw nxt[kRadRows];
-        if (cn < nv) {
-#pragma unroll
-            for (int r = 0; r < kRadRows; ++r) nxt[r].load(rows[r] + (size_t) cn * V);
-        }
-        if (c < nv) {
-            float f[kRadRows][V];
-#pragma unroll
-            for (int r = 0; r < kRadRows; ++r) unpack<T, V>(&cur[r].u, f[r]);
-#pragma unroll
-            for (int k = 0; k < V; ++k) {
-                bool any = false;
-#pragma unroll
-                for (int r = 0; r < kRadRows; ++r) any |= f[r][k] != 0.0f;
-                if (any) {
-                    const int q = lane * V + k;
-                    const int slot = q ^ ((q >> 3) & 7);
-                    const float4 x = xs[0][slot];
-                    V3 bp, bn;
-                    if (kExact) { bp = ld3(xs[1 % kArrays][slot]); bn = ld3(xs[2 % kArrays][slot]); }
-                    const u32 j = c * V + k;
-#pragma unroll
-                    for (int r = 0; r < kRadRows; ++r) {
-                        if (f[r][k] != 0.0f) {
-                            float fv = f[r][k];
-                            if (kExact) fv = ri[r] < j ? pair_pretest(ap[r], an[r], bp, bn) : pair_pretest(bp, bn, ap[r], an[r]);
-                            acc[r][0] += x.x * fv; acc[r][1] += x.y * fv; acc[r][2] += x.z * fv;
-                        }
-                    }
-                }
-            }
         }
 #pragma unroll
         for (int r = 0; r < kRadRows; ++r) cur[r] = nxt[r];
@@ -589,14 +487,10 @@ RadResult solve_t(const RadDevInputs& in, const RadSettings& rs, const BvhView& 
         // the last refine_steps bounces of a 16-bit F recompute the factors in FP32
         const bool exact = sizeof(T) < 4 && b >= rs.bounces - rs.refine_steps;
         const unsigned grid = (unsigned) ((((size_t) n + kRadRows - 1) / kRadRows * 32 + 255) / 256);
-        if constexpr (sizeof(T) == 2) {
-            if (exact)
-                k_rad_gemv16<T, true><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, up, X, Y);
-            else
-                k_rad_gemv16<T, false><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, up, X, Y);
-        } else {
+        if (exact)
+            k_rad_gemv<T, true><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, up, X, Y);
+        else
             k_rad_gemv<T, false><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, up, X, Y);
-        }
         note_launch();
         k_rad_update<<<(n + 255) / 256, 256, 0, st>>>(n, Y, total, out); note_launch();
         RCK(cudaGetLastError());

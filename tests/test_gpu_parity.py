@@ -249,14 +249,14 @@ def test_abort_between_stages(gpu):
 
 def test_abort_lands_inside_a_long_trace_launch(gpu):
     """ltr_Abort while one shadow-trace launch runs for more than a second (the
-    mid scene at 1024^2 with 4096 sampled shadow rays per pair): the persistent
+    mid scene at 1024^2 with 8192 sampled shadow rays per pair): the persistent
     warps poll the scene's mapped abort word at every work fetch and stop, so
     the bake ends as "aborted" long before the launch would have finished."""
     import time
     from lighter_gb300.scene import ingest
     d = scenes.mid(2, lm=1024, bounces=0, ao_rays=0)
     for L in d.lights:
-        L.shadow_sample_count = 4096
+        L.shadow_sample_count = 8192
     scene, keep = ingest(gpu, d, gpu_options={"shadow_mode": 1})
     try:
         gpu.ltr_Start(scene)

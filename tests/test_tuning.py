@@ -36,6 +36,8 @@ def test_tuning_defaults_and_validation(gpu):
         assert lib.ltrg_SetTuning(0, C.byref(bad)) == 0
         bad.ao_chunk, bad.direct_packet = 1, 2
         assert lib.ltrg_SetTuning(0, C.byref(bad)) == 0
+        bad.direct_packet, bad.direct_regs = 1, 4  # register budgets 0..3
+        assert lib.ltrg_SetTuning(0, C.byref(bad)) == 0
         assert lib.ltrg_SetTuning(-1, C.byref(t)) == 0
         ok = ext.Tuning()
         C.memmove(C.byref(ok), C.byref(t), C.sizeof(t))
@@ -81,7 +83,7 @@ def test_results_do_not_depend_on_stack_split_or_wavefront(gpu, shadow_mode):
         t.direct_stack, t.ao_stack, t.ao_chunk, t.direct_packet, t.ao_packet = 0, 0, 4, 0, 0
         assert lib.ltrg_SetTuning(0, C.byref(t))
         ref = bake(lib, d, gpu_options=opts)
-        for k, chunk, regs, packet in ((4, 1, 0, 0), (8, 2, 1, 1), (16, 8, 0, 1), (0, 4, 0, 1), (0, 1, 1, 1)):
+        for k, chunk, regs, packet in ((4, 1, 0, 0), (8, 2, 1, 1), (16, 8, 0, 1), (0, 4, 2, 1), (0, 1, 3, 0)):
             t.direct_stack, t.ao_stack, t.ao_chunk, t.direct_packet, t.ao_packet = k, k, chunk, packet, packet
             t.direct_regs = t.sampled_regs = regs
             assert lib.ltrg_SetTuning(0, C.byref(t))
