@@ -81,14 +81,18 @@ class Gather:
             raise RuntimeError("ltrg_GatherGetG failed")
         return out
 
-    def solve(self, albedo, emission, bounces, precision=FP16, refine=REFINE_RHS):
-        """B (n x R) from host arrays; returns (B, stats dict)."""
+    def solve(self, albedo, emission, bounces, precision=FP16, refine=REFINE_RHS, out=None):
+        """B (n x R) from host arrays; returns (B, stats dict). `out` (n x R float32,
+        C order) receives B when given, so a caller can reuse one host buffer."""
         albedo = _f32(albedo, (self.n, 3))
         emission = _f32(emission)
         if emission.ndim != 2 or emission.shape[0] != self.n:
             raise ValueError("emission must be n x R")
         R = emission.shape[1]
-        out = np.empty((self.n, R), np.float32)
+        if out is None:
+            out = np.empty((self.n, R), np.float32)
+        elif out.shape != (self.n, R) or out.dtype != np.float32 or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a C-ordered n x R float32 array")
         st = ext.GatherStats()
         if not self.lib.ltrg_GatherSolve(self.h, _ptr(albedo), _ptr(emission), R, bounces, precision, refine,
                                          _ptr(out), C.byref(st)):
