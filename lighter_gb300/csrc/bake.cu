@@ -789,15 +789,16 @@ __device__ __forceinline__ void direct_pair_finish(const DirectArgs& a, u32 w, c
 // kMinBlocks 2 caps the registers at 64 (two blocks of 512 threads per SM):
 // more warps in flight for the latency-bound walks, at the price of a few
 // spills; which is faster depends on the scene (tuning direct_regs).
-// kRegCap: registers per thread at most (128: as compiled for blocks of up to
-// 512 threads; 64, 72, 80: more warps per SM for the latency-bound walks, at
-// the price of spills; tuning direct_regs / sampled_regs). kStackK:
+// The shadow-trace kernel: k_direct_trace as compiled for blocks of up to 512
+// threads, k_direct_trace_capped with at most kRegCap registers per thread (64,
+// 72, 80: more warps per SM for the latency-bound walks, at the price of
+// spills; tuning direct_regs / sampled_regs). kStackK:
 // traversal-stack entries kept in shared memory by the per-lane walks (TStack;
 // tuning direct_stack). kPacket: the shadow traces of a warp's 32 pairs run
 // together (inv_shadow_warp, sampled_vis_warp; tuning direct_packet).
-template <int kRegCap, int kStackK, bool kPacket>
-__global__ void __launch_bounds__(512) __maxnreg__(kRegCap)
-    k_direct_trace(DirectArgs a, const u32* __restrict__ items, const u32* __restrict__ n_items_dev, u32* __restrict__ next)
+template <int kStackK, bool kPacket>
+__device__ __forceinline__ void direct_trace_body(const DirectArgs& a, const u32* __restrict__ items,
+                                                  const u32* __restrict__ n_items_dev, u32* __restrict__ next)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     TStack<kStackK> st = make_stack<kStackK>(smem);
@@ -843,6 +844,21 @@ __global__ void __launch_bounds__(512) __maxnreg__(kRegCap)
         warp_add(&a.counters->node_visits, c_nv);
         warp_add(&a.counters->tri_tests, c_nt);
     }
+}
+
+template <int kRegCap, int kStackK, bool kPacket>
+__global__ void __launch_bounds__(512) __maxnreg__(kRegCap)
+    k_direct_trace_capped(DirectArgs a, const u32* __restrict__ items, const u32* __restrict__ n_items_dev,
+                          u32* __restrict__ next)
+{
+    direct_trace_body<kStackK, kPacket>(a, items, n_items_dev, next);
+}
+
+template <int kStackK, bool kPacket>
+__global__ void __launch_bounds__(512, 1)
+    k_direct_trace(DirectArgs a, const u32* __restrict__ items, const u32* __restrict__ n_items_dev, u32* __restrict__ next)
+{
+    direct_trace_body<kStackK, kPacket>(a, items, n_items_dev, next);
 }
 
 // Per sample, ambient plus every light's term in light order (lighter.cpp:504, 542, 589).
@@ -1162,10 +1178,16 @@ void launch_direct_k(unsigned grid, unsigned block, cudaStream_t st, const Direc
                      const u32* n_items, u32* next)
 {
     const size_t smem = (size_t) K * block * 8;
-    if (smem > 48 * 1024)
-        CK(cudaFuncSetAttribute(k_direct_trace<kRegCap, K, kPacket>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int) smem));
-    k_direct_trace<kRegCap, K, kPacket><<<grid, block, smem, st>>>(da, items, n_items, next);
+    if constexpr (kRegCap == 128) {
+        if (smem > 48 * 1024)
+            CK(cudaFuncSetAttribute(k_direct_trace<K, kPacket>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+        k_direct_trace<K, kPacket><<<grid, block, smem, st>>>(da, items, n_items, next);
+    } else {
+        if (smem > 48 * 1024)
+            CK(cudaFuncSetAttribute(k_direct_trace_capped<kRegCap, K, kPacket>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+        k_direct_trace_capped<kRegCap, K, kPacket><<<grid, block, smem, st>>>(da, items, n_items, next);
+    }
 }
 
 // The shared-memory stack split is built for the per-lane walks with 128 and
@@ -1256,13 +1278,17 @@ __device__ __forceinline__ int find_job(const unsigned long long* __restrict__ o
     return lo;
 }
 
+// Job k's items take [off[k], off[k] + count_k) of the batch's item space, and
+// off[k + 1] - off[k] is count_k rounded up to a multiple of 32: a warp's 32
+// items (the kernel hands out 32 at a time) then always come from one job, so
+// its lanes can share a BVH walk; the items of the padding are skipped.
 __global__ void k_direct_batch_offsets(const DirectJob* __restrict__ jobs, int n, unsigned long long* __restrict__ off)
 {
     if (blockIdx.x || threadIdx.x) return;
     unsigned long long acc = 0;
     for (int k = 0; k < n; ++k) {
         off[k] = acc;
-        acc += jobs[k].count ? *jobs[k].count : 0u;
+        acc += ((jobs[k].count ? *jobs[k].count : 0u) + 31ull) / 32ull * 32ull;
     }
     off[n] = acc;
 }
@@ -1280,6 +1306,9 @@ __device__ __forceinline__ void flush_direct(Counters* c, unsigned long long& tr
     tr = nq = nv = nt = np = 0;
 }
 
+// kPacket: a warp's 32 pairs (all of one scene) share their walks
+// (direct_pair_warp), as in k_direct_trace; otherwise each lane walks alone.
+template <bool kPacket>
 __global__ void k_direct_trace_batch(const DirectJob* __restrict__ jobs, int n, const unsigned long long* __restrict__ off,
                                      unsigned long long* __restrict__ next)
 {
@@ -1289,28 +1318,36 @@ __global__ void k_direct_trace_batch(const DirectJob* __restrict__ jobs, int n, 
     DirectArgs a;
     const u32* items = nullptr;
     unsigned long long base = 0;
+    u32 count = 0;
     const int lane = threadIdx.x & 31;
     for (;;) {
         unsigned long long wb = 0;
         if (lane == 0) wb = atomicAdd(next, 32ull);
         wb = __shfl_sync(0xffffffffu, wb, 0);
         if (wb >= total) break;
-        const unsigned long long g = wb + lane;
-        if (g >= total) continue;
-        const int k = find_job(off, n, g);
+        const int k = find_job(off, n, wb);   // the warp's job (job ranges are multiples of 32)
         if (k != cur) {
             if (cur >= 0) flush_direct(a.counters, c_traced, c_nq, c_nv, c_nt, c_pairs);
             cur = k;
             a = jobs[k].args;
             items = jobs[k].items;
             base = off[k];
+            count = jobs[k].count ? *jobs[k].count : 0u;
         }
+        const unsigned long long i = wb + lane - base;
+        const bool has = i < count;
         u32 nq = 0, nv = 0, nt = 0;
-        const u32 w = items[g - base];
-        TStack<0> st;
-        direct_pair(a, w, nq, nv, nt, st);
-        c_traced += a.shadow_mode == 1 ? (unsigned) a.lights[w / a.n_samples].ns : 1u;
-        c_pairs += 1;
+        const u32 w = has ? items[i] : 0u;
+        if (kPacket) {
+            direct_pair_warp(a, has, w, nq, nv, nt);
+        } else if (has) {
+            TStack<0> st;
+            direct_pair(a, w, nq, nv, nt, st);
+        }
+        if (has) {
+            c_traced += a.shadow_mode == 1 ? (unsigned) a.lights[w / a.n_samples].ns : 1u;
+            c_pairs += 1;
+        }
         c_nq += nq;
         c_nv += nv;
         c_nt += nt;
@@ -1318,6 +1355,9 @@ __global__ void k_direct_trace_batch(const DirectJob* __restrict__ jobs, int n, 
     if (cur >= 0) flush_direct(a.counters, c_traced, c_nq, c_nv, c_nt, c_pairs);
 }
 
+// Job ranges are ao_items long, a multiple of 32: a warp's 32 rays of a step
+// are one scene's, so with kPacket they share one walk (ao_ray_warp).
+template <bool kPacket>
 __global__ void k_ao_rays_batch(const AoJob* __restrict__ jobs, int n, const unsigned long long* __restrict__ off,
                                 unsigned long long* __restrict__ next)
 {
@@ -1334,9 +1374,10 @@ __global__ void k_ao_rays_batch(const AoJob* __restrict__ jobs, int n, const uns
         wb = __shfl_sync(0xffffffffu, wb, 0);
         if (wb >= total) break;
         for (unsigned kk = 0; kk < kAoChunk; ++kk) {
-            const unsigned long long g = wb + 32ull * kk + lane;
-            if (g >= total) continue;
-            const int k = find_job(off, n, g);
+            const unsigned long long gw = wb + 32ull * kk;   // the warp's first item of this step
+            if (gw >= total) break;
+            const unsigned long long g = gw + lane;
+            const int k = find_job(off, n, gw);
             if (k != cur) {
                 if (cur >= 0 && a.counters && c_rays) atomicAdd(&a.counters->ao_rays, c_rays);
                 c_rays = 0;
@@ -1344,6 +1385,10 @@ __global__ void k_ao_rays_batch(const AoJob* __restrict__ jobs, int n, const uns
                 a = jobs[k].args;
                 hits = jobs[k].hits;
                 job0 = off[k];
+            }
+            if (kPacket) {
+                if (ao_ray_warp(a, hits, g - job0, off[k + 1] - job0)) ++c_rays;
+                continue;
             }
             unsigned long long i;
             if (ao_item(g - job0, a.n_samples, a.ns, a.order, i)) {
@@ -1597,6 +1642,8 @@ struct StageClock {
 };
 
 
+thread_local bool t_blocking_waits = false;
+
 void check_abort(ltr_Scene* s)
 {
     if (s->abort_flag.load()) throw std::runtime_error("aborted by ltr_Abort");
@@ -1777,6 +1824,23 @@ std::vector<float> gauss_taps(int ext, float radius)
 
 }  // namespace
 
+void set_blocking_waits(bool on) { t_blocking_waits = on; }
+
+void sync_stream(void* stream)
+{
+    cudaStream_t s = (cudaStream_t) stream;
+    if (!t_blocking_waits) {
+        CK(cudaStreamSynchronize(s));
+        return;
+    }
+    cudaEvent_t e = nullptr;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming | cudaEventBlockingSync));
+    cudaError_t r = cudaEventRecord(e, s);
+    if (r == cudaSuccess) r = cudaEventSynchronize(e);
+    cudaEventDestroy(e);
+    CK(r);
+}
+
 void build_refs_host(const std::vector<float>& xyz, std::vector<u32>& ref_tri, std::vector<float>& ref_box, float* cmin,
                      float* cmax)
 {
@@ -1804,7 +1868,9 @@ struct BatchCtx {
         : n(n_), device(device_), rand_done(n_, 0), member(n_, 0), started(n_, 0), cv_turn(n_), cv_start(n_)
     {
         for (Phase& p : phase) p.expected = n_;
-        slots = std::max(2, std::min(16, (int) std::thread::hardware_concurrency()));
+        // scenes spend much of their host part waiting on the GPU (blocking waits):
+        // up to four per host core work at a time
+        slots = std::max(2, std::min(64, 4 * (int) std::thread::hardware_concurrency()));
         trace = getenv("LTRG_TRACE") != nullptr;
         t0 = std::chrono::steady_clock::now();
     }
@@ -2018,8 +2084,13 @@ struct BatchCtx {
                     CK(cudaMemcpyAsync(d_jobs, ph.djobs.data(), jb, cudaMemcpyHostToDevice, bst));
                     k_direct_batch_offsets<<<1, 32, 0, bst>>>((const DirectJob*) d_jobs, nj, d_off); note_launch();
                     const ltrg_Tuning tu = get_tuning(device);
-                    k_direct_trace_batch<<<(unsigned) sms * tu.direct_blocks_per_sm, tu.direct_block, 0, bst>>>(
-                        (const DirectJob*) d_jobs, nj, d_off, d_next);
+                    const unsigned grid = (unsigned) sms * tu.direct_blocks_per_sm;
+                    if (tu.direct_packet)
+                        k_direct_trace_batch<true><<<grid, tu.direct_block, 0, bst>>>((const DirectJob*) d_jobs, nj, d_off,
+                                                                                      d_next);
+                    else
+                        k_direct_trace_batch<false><<<grid, tu.direct_block, 0, bst>>>((const DirectJob*) d_jobs, nj, d_off,
+                                                                                       d_next);
                     note_launch();
                 } else {
                     std::vector<unsigned long long> off(nj + 1, 0);
@@ -2029,8 +2100,11 @@ struct BatchCtx {
                                        cudaMemcpyHostToDevice, bst));
                     // the pageable copies above are staged before they return, so `off` may go
                     const ltrg_Tuning tu = get_tuning(device);
-                    k_ao_rays_batch<<<(unsigned) sms * tu.ao_blocks_per_sm, tu.ao_block, 0, bst>>>((const AoJob*) d_jobs, nj,
-                                                                                                 d_off, d_next);
+                    const unsigned grid = (unsigned) sms * tu.ao_blocks_per_sm;
+                    if (tu.ao_packet)
+                        k_ao_rays_batch<true><<<grid, tu.ao_block, 0, bst>>>((const AoJob*) d_jobs, nj, d_off, d_next);
+                    else
+                        k_ao_rays_batch<false><<<grid, tu.ao_block, 0, bst>>>((const AoJob*) d_jobs, nj, d_off, d_next);
                     note_launch();
                 }
                 CK(cudaGetLastError());
@@ -2091,6 +2165,7 @@ void run_bake(ltr_Scene* S)
     // member of a batch (ltrg_StartBatch): leaves it however the bake ends
     BatchCtx* batch = S->batch.get();
     const int bidx = S->batch_index;
+    set_blocking_waits(batch != nullptr);
     struct BatchLeave {
         BatchCtx* b; int i; bool slot = false;
         ~BatchLeave() { if (b) { b->leave(i); if (slot) b->release(); } }
@@ -2459,7 +2534,7 @@ void run_bake(ltr_Scene* S)
     const bool validate = getenv("LTRG_VALIDATE") && getenv("LTRG_VALIDATE")[0] == '1';
     auto checkpoint = [&](const char* where) {
         if (!validate) return;
-        CK(cudaStreamSynchronize(st));
+        sync_stream(st);
         std::string e = bvh_validate(bvh, st);
         if (!e.empty()) throw std::runtime_error(std::string("BVH corrupted after ") + where + ": " + e);
     };
@@ -2500,7 +2575,7 @@ void run_bake(ltr_Scene* S)
     for (int i = 1; i <= n_inst; ++i)
         CK(cudaMemcpyAsync(&inst_sbeg[i], d_scan + tex_off[i == n_inst ? n_inst : i], sizeof(u32),
                            cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    sync_stream(st);
     const u32 n_cov = inst_sbeg[n_inst];
     TRACE("sample counts read");
     const u32 n_samples = n_probe + n_cov;
@@ -2569,7 +2644,7 @@ void run_bake(ltr_Scene* S)
         CK(cudaMemcpyAsync(d_snrm, pn.data(), n_probe * sizeof(float4), cudaMemcpyHostToDevice, st)); note_h2d(n_probe * sizeof(float4));
         CK(cudaMemcpyAsync(d_sloc, pl.data(), n_probe * sizeof(u32), cudaMemcpyHostToDevice, st)); note_h2d(n_probe * sizeof(u32));
         CK(cudaMemcpyAsync(d_sinst, pi.data(), n_probe * sizeof(u32), cudaMemcpyHostToDevice, st)); note_h2d(n_probe * sizeof(u32));
-        CK(cudaStreamSynchronize(st));
+        sync_stream(st);
     }
     if (ntex) {
         k_compact<<<blocks_for(ntex), kThreads, 0, st>>>(ntex, d_flags, d_scan, d_R1, d_R2, d_R3, d_tex_off, n_inst,
@@ -2754,7 +2829,7 @@ void run_bake(ltr_Scene* S)
     cudaEvent_t e_rad_links = e_direct, e_rad_bounce = e_direct;
     if (do_rad) {
         S->stage = "calculating radiosity";
-        CK(cudaStreamSynchronize(st2));
+        sync_stream(st2);
         TRACE("sample copies done");
         float4* d_diff = A.alloc<float4>(n_samples);
         float4* d_emis = A.alloc<float4>(n_samples);
@@ -2852,7 +2927,7 @@ void run_bake(ltr_Scene* S)
                 dst[k]->resize(4 * (size_t) n);
                 CK(cudaMemcpyAsync(dst[k]->data(), src[k], n * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n * sizeof(float4));
             }
-            CK(cudaStreamSynchronize(st));
+            sync_stream(st);
         };
         if (S->opt.radiosity_patches == 0) {
             cudaEvent_t up = nullptr;
@@ -2900,7 +2975,7 @@ void run_bake(ltr_Scene* S)
                 CK(cudaGetLastError());
                 u32 c = 0;
                 CK(cudaMemcpyAsync(&c, d_count, sizeof(u32), cudaMemcpyDeviceToHost, st)); note_d2h(4);
-                CK(cudaStreamSynchronize(st));
+                sync_stream(st);
                 return c;
             };
             u32 tile = (u32) std::max(1.0, std::floor(std::sqrt(std::max(1.0, (double) n_cov / target)) + 0.5));
@@ -2950,7 +3025,7 @@ void run_bake(ltr_Scene* S)
                 void* tmp = A.alloc<char>(tb);
                 CK(cub::DeviceRadixSort::SortPairs(tmp, tb, d_keys_in, d_keys_out, d_vals_in, d_csr_idx, (int) n_cov, 0, 32, st));
             }
-            CK(cudaStreamSynchronize(st));
+            sync_stream(st);
             u32* d_csr_off = A.alloc<u32>(np + 1);
             k_patch_offsets<<<(n_cov + kThreads - 1) / kThreads, kThreads, 0, st>>>(n_cov, np, d_keys_out, d_csr_off); note_launch();
             CK(cudaGetLastError());
@@ -3161,7 +3236,7 @@ void run_bake(ltr_Scene* S)
         CK(cudaMemcpyAsync(dloc.data(), d_sloc, n_samples * sizeof(u32), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(u32));
     }
     cudaEvent_t e_down = clock.mark();
-    CK(cudaStreamSynchronize(st));
+    sync_stream(st);
     TRACE("readback done");
     // the host queues the whole bake and waits here; an ltr_Abort during that
     // wait stopped the trace kernels early, so their outputs are incomplete

@@ -245,6 +245,7 @@ template <class T, int V> __device__ __forceinline__ void unpack(const void* raw
 }
 
 constexpr int kRadRows = 4;   // rows of F per warp in the bounce product
+constexpr int kRadDepth = 4;  // steps of F a lane has in flight in the bounce product
 
 // Y = F X (one bounce's gather). F is streamed once per bounce, so the kernel is
 // HBM-bound: a warp takes kRadRows rows and reads them V entries per lane per
@@ -259,7 +260,7 @@ constexpr int kRadRows = 4;   // rows of F per warp in the bounce product
 // the FP32 one. kExact reads 4 entries per lane (8-byte loads of a 16-bit F),
 // the FP32 kernel's split of columns over lanes, so both sum in the same order:
 // the kExact product of a 16-bit F is the FP32 product.
-template <class T, bool kExact>
+template <class T, bool kExact, int kDepth = 2>
 __global__ void __launch_bounds__(256) k_rad_gemv(u32 n, size_t ld, const T* __restrict__ F,
                                                   const float4* __restrict__ pos, const float4* __restrict__ nrm,
                                                   const float* __restrict__ up, const float4* __restrict__ X,
@@ -283,54 +284,61 @@ __global__ void __launch_bounds__(256) k_rad_gemv(u32 n, size_t ld, const T* __r
 #pragma unroll
     for (int r = 0; r < kRadRows; ++r) acc[r][0] = acc[r][1] = acc[r][2] = 0.0f;
     const u32 nv = (u32) (ld / V);
-    Raw cur[kRadRows];
-    u32 c = lane;
-    if (c < nv) {
+    // software pipeline kDepth steps deep: the loads of step c + 32 (kDepth - 1)
+    // are issued before step c's arithmetic (each lane still walks its columns
+    // in increasing order, so the sums keep their order)
+    Raw buf[kDepth][kRadRows];
 #pragma unroll
-        for (int r = 0; r < kRadRows; ++r) cur[r].load(rows[r] + (size_t) c * V);
-    }
-    while (c < nv) {
-        const u32 cn = c + 32;
-        Raw nxt[kRadRows];
-        if (cn < nv) {
+    for (int d = 0; d < kDepth - 1; ++d) {
+        const u32 cc = lane + 32u * d;
+        if (cc < nv) {
 #pragma unroll
-            for (int r = 0; r < kRadRows; ++r) nxt[r].load(rows[r] + (size_t) cn * V);
+            for (int r = 0; r < kRadRows; ++r) buf[d][r].load(rows[r] + (size_t) cc * V);
         }
-        // F is sparse (pairs more than a few metres apart have factors below
-        // SMALL_FLOAT, and occluded pairs are 0): a vector that is zero in all the
-        // warp's rows is skipped with one test (F holds no negative values and its
-        // zeros are +0, so "no bit set" is "all entries zero")
-        unsigned nz = 0;
+    }
+    for (u32 base = lane; base < nv; base += 32u * kDepth) {
 #pragma unroll
-        for (int r = 0; r < kRadRows; ++r) nz |= cur[r].bits();
-        if (nz) {
-        float f[kRadRows][V];
+        for (int d = 0; d < kDepth; ++d) {
+            const u32 c = base + 32u * d;
+            const u32 cl = c + 32u * (kDepth - 1);
+            if (cl < nv) {
 #pragma unroll
-        for (int r = 0; r < kRadRows; ++r) unpack<T, V>(&cur[r].u, f[r]);
+                for (int r = 0; r < kRadRows; ++r) buf[(d + kDepth - 1) % kDepth][r].load(rows[r] + (size_t) cl * V);
+            }
+            if (c >= nv) break;
+            const Raw* cur = buf[d];
+            // F is sparse (pairs more than a few metres apart have factors below
+            // SMALL_FLOAT, and occluded pairs are 0): a vector that is zero in all the
+            // warp's rows is skipped with one test (F holds no negative values and its
+            // zeros are +0, so "no bit set" is "all entries zero")
+            unsigned nz = 0;
 #pragma unroll
-        for (int k = 0; k < V; ++k) {
-            bool any = false;
+            for (int r = 0; r < kRadRows; ++r) nz |= cur[r].bits();
+            if (!nz) continue;
+            float f[kRadRows][V];
 #pragma unroll
-            for (int r = 0; r < kRadRows; ++r) any |= f[r][k] != 0.0f;
-            if (any) {
-                const u32 j = c * V + k;
-                const float4 x = __ldg(&X[j]);
-                V3 bp, bn;
-                if (kExact) { bp = ld3(pos[j]); bn = ld3(nrm[j]); }
+            for (int r = 0; r < kRadRows; ++r) unpack<T, V>(&cur[r].u, f[r]);
 #pragma unroll
-                for (int r = 0; r < kRadRows; ++r) {
-                    if (f[r][k] != 0.0f) {
-                        float fv = f[r][k];
-                        if (kExact) fv = ri[r] < j ? pair_pretest(ap[r], an[r], bp, bn) : pair_pretest(bp, bn, ap[r], an[r]);
-                        acc[r][0] += x.x * fv; acc[r][1] += x.y * fv; acc[r][2] += x.z * fv;
+            for (int k = 0; k < V; ++k) {
+                bool any = false;
+#pragma unroll
+                for (int r = 0; r < kRadRows; ++r) any |= f[r][k] != 0.0f;
+                if (any) {
+                    const u32 j = c * V + k;
+                    const float4 x = __ldg(&X[j]);
+                    V3 bp, bn;
+                    if (kExact) { bp = ld3(pos[j]); bn = ld3(nrm[j]); }
+#pragma unroll
+                    for (int r = 0; r < kRadRows; ++r) {
+                        if (f[r][k] != 0.0f) {
+                            float fv = f[r][k];
+                            if (kExact) fv = ri[r] < j ? pair_pretest(ap[r], an[r], bp, bn) : pair_pretest(bp, bn, ap[r], an[r]);
+                            acc[r][0] += x.x * fv; acc[r][1] += x.y * fv; acc[r][2] += x.z * fv;
+                        }
                     }
                 }
             }
         }
-        }
-#pragma unroll
-        for (int r = 0; r < kRadRows; ++r) cur[r] = nxt[r];
-        c = cn;
     }
 #pragma unroll
     for (int r = 0; r < kRadRows; ++r)
@@ -488,9 +496,9 @@ RadResult solve_t(const RadDevInputs& in, const RadSettings& rs, const BvhView& 
         const bool exact = sizeof(T) < 4 && b >= rs.bounces - rs.refine_steps;
         const unsigned grid = (unsigned) ((((size_t) n + kRadRows - 1) / kRadRows * 32 + 255) / 256);
         if (exact)
-            k_rad_gemv<T, true><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, up, X, Y);
+            k_rad_gemv<T, true, kRadDepth><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, up, X, Y);
         else
-            k_rad_gemv<T, false><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, up, X, Y);
+            k_rad_gemv<T, false, kRadDepth><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, up, X, Y);
         note_launch();
         k_rad_update<<<(n + 255) / 256, 256, 0, st>>>(n, Y, total, out); note_launch();
         RCK(cudaGetLastError());
