@@ -1642,8 +1642,6 @@ struct StageClock {
 };
 
 
-thread_local bool t_blocking_waits = false;
-
 void check_abort(ltr_Scene* s)
 {
     if (s->abort_flag.load()) throw std::runtime_error("aborted by ltr_Abort");
@@ -1824,23 +1822,6 @@ std::vector<float> gauss_taps(int ext, float radius)
 
 }  // namespace
 
-void set_blocking_waits(bool on) { t_blocking_waits = on; }
-
-void sync_stream(void* stream)
-{
-    cudaStream_t s = (cudaStream_t) stream;
-    if (!t_blocking_waits) {
-        CK(cudaStreamSynchronize(s));
-        return;
-    }
-    cudaEvent_t e = nullptr;
-    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming | cudaEventBlockingSync));
-    cudaError_t r = cudaEventRecord(e, s);
-    if (r == cudaSuccess) r = cudaEventSynchronize(e);
-    cudaEventDestroy(e);
-    CK(r);
-}
-
 void build_refs_host(const std::vector<float>& xyz, std::vector<u32>& ref_tri, std::vector<float>& ref_box, float* cmin,
                      float* cmax)
 {
@@ -1869,7 +1850,8 @@ struct BatchCtx {
     {
         for (Phase& p : phase) p.expected = n_;
         // more scenes at a time measured slower (64 on 16 cores: 0.87 -> 1.21 s for
-        // 256 scenes; each scene's small kernels and waits queue behind the others')
+        // 256 scenes; each scene's small kernels and waits queue behind the others'),
+        // and so did blocking instead of spinning waits (0.77 -> 0.79 s)
         slots = std::max(2, std::min(16, (int) std::thread::hardware_concurrency()));
         trace = getenv("LTRG_TRACE") != nullptr;
         t0 = std::chrono::steady_clock::now();
@@ -2165,7 +2147,6 @@ void run_bake(ltr_Scene* S)
     // member of a batch (ltrg_StartBatch): leaves it however the bake ends
     BatchCtx* batch = S->batch.get();
     const int bidx = S->batch_index;
-    set_blocking_waits(batch != nullptr);
     struct BatchLeave {
         BatchCtx* b; int i; bool slot = false;
         ~BatchLeave() { if (b) { b->leave(i); if (slot) b->release(); } }
@@ -2534,7 +2515,7 @@ void run_bake(ltr_Scene* S)
     const bool validate = getenv("LTRG_VALIDATE") && getenv("LTRG_VALIDATE")[0] == '1';
     auto checkpoint = [&](const char* where) {
         if (!validate) return;
-        sync_stream(st);
+        CK(cudaStreamSynchronize(st));
         std::string e = bvh_validate(bvh, st);
         if (!e.empty()) throw std::runtime_error(std::string("BVH corrupted after ") + where + ": " + e);
     };
@@ -2575,7 +2556,7 @@ void run_bake(ltr_Scene* S)
     for (int i = 1; i <= n_inst; ++i)
         CK(cudaMemcpyAsync(&inst_sbeg[i], d_scan + tex_off[i == n_inst ? n_inst : i], sizeof(u32),
                            cudaMemcpyDeviceToHost, st));
-    sync_stream(st);
+    CK(cudaStreamSynchronize(st));
     const u32 n_cov = inst_sbeg[n_inst];
     TRACE("sample counts read");
     const u32 n_samples = n_probe + n_cov;
@@ -2644,7 +2625,7 @@ void run_bake(ltr_Scene* S)
         CK(cudaMemcpyAsync(d_snrm, pn.data(), n_probe * sizeof(float4), cudaMemcpyHostToDevice, st)); note_h2d(n_probe * sizeof(float4));
         CK(cudaMemcpyAsync(d_sloc, pl.data(), n_probe * sizeof(u32), cudaMemcpyHostToDevice, st)); note_h2d(n_probe * sizeof(u32));
         CK(cudaMemcpyAsync(d_sinst, pi.data(), n_probe * sizeof(u32), cudaMemcpyHostToDevice, st)); note_h2d(n_probe * sizeof(u32));
-        sync_stream(st);
+        CK(cudaStreamSynchronize(st));
     }
     if (ntex) {
         k_compact<<<blocks_for(ntex), kThreads, 0, st>>>(ntex, d_flags, d_scan, d_R1, d_R2, d_R3, d_tex_off, n_inst,
@@ -2829,7 +2810,7 @@ void run_bake(ltr_Scene* S)
     cudaEvent_t e_rad_links = e_direct, e_rad_bounce = e_direct;
     if (do_rad) {
         S->stage = "calculating radiosity";
-        sync_stream(st2);
+        CK(cudaStreamSynchronize(st2));
         TRACE("sample copies done");
         float4* d_diff = A.alloc<float4>(n_samples);
         float4* d_emis = A.alloc<float4>(n_samples);
@@ -2927,7 +2908,7 @@ void run_bake(ltr_Scene* S)
                 dst[k]->resize(4 * (size_t) n);
                 CK(cudaMemcpyAsync(dst[k]->data(), src[k], n * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n * sizeof(float4));
             }
-            sync_stream(st);
+            CK(cudaStreamSynchronize(st));
         };
         if (S->opt.radiosity_patches == 0) {
             cudaEvent_t up = nullptr;
@@ -2975,7 +2956,7 @@ void run_bake(ltr_Scene* S)
                 CK(cudaGetLastError());
                 u32 c = 0;
                 CK(cudaMemcpyAsync(&c, d_count, sizeof(u32), cudaMemcpyDeviceToHost, st)); note_d2h(4);
-                sync_stream(st);
+                CK(cudaStreamSynchronize(st));
                 return c;
             };
             u32 tile = (u32) std::max(1.0, std::floor(std::sqrt(std::max(1.0, (double) n_cov / target)) + 0.5));
@@ -3025,7 +3006,7 @@ void run_bake(ltr_Scene* S)
                 void* tmp = A.alloc<char>(tb);
                 CK(cub::DeviceRadixSort::SortPairs(tmp, tb, d_keys_in, d_keys_out, d_vals_in, d_csr_idx, (int) n_cov, 0, 32, st));
             }
-            sync_stream(st);
+            CK(cudaStreamSynchronize(st));
             u32* d_csr_off = A.alloc<u32>(np + 1);
             k_patch_offsets<<<(n_cov + kThreads - 1) / kThreads, kThreads, 0, st>>>(n_cov, np, d_keys_out, d_csr_off); note_launch();
             CK(cudaGetLastError());
@@ -3236,7 +3217,7 @@ void run_bake(ltr_Scene* S)
         CK(cudaMemcpyAsync(dloc.data(), d_sloc, n_samples * sizeof(u32), cudaMemcpyDeviceToHost, st)); note_d2h(n_samples * sizeof(u32));
     }
     cudaEvent_t e_down = clock.mark();
-    sync_stream(st);
+    CK(cudaStreamSynchronize(st));
     TRACE("readback done");
     // the host queues the whole bake and waits here; an ltr_Abort during that
     // wait stopped the trace kernels early, so their outputs are incomplete

@@ -486,7 +486,7 @@ void bvh_build(const BvhBuildInput& in, BvhStorage& out, void* stream)
             int hs[2] = {0, 0};
             BVH_CHECK(cudaMemcpyAsync(hs, state, sizeof(hs), cudaMemcpyDeviceToHost, st));
             note_d2h(sizeof(hs));
-            sync_stream(st);
+            BVH_CHECK(cudaStreamSynchronize(st));
             // every merge takes one cluster and one node number, so the next
             // number is count - 1; with more than one cluster every iteration merges
             if (hs[0] < 1 || hs[0] >= count || hs[1] != hs[0] - 1) { fail = "bvh: clustering step inconsistent"; break; }
@@ -500,7 +500,7 @@ void bvh_build(const BvhBuildInput& in, BvhStorage& out, void* stream)
             k_max_depth<<<(n_int + B - 1) / B, B, 0, st>>>(n_int, parent_int, maxd); note_launch();
             BVH_CHECK(cudaGetLastError());
             BVH_CHECK(cudaMemcpyAsync(&depth, maxd, sizeof(int), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(int));
-            sync_stream(st);
+            BVH_CHECK(cudaStreamSynchronize(st));
         }
         void* pp[] = {cl, ncl, cbox, ncbox, nn, flags, scan, maxd, ptmp, state};
         for (void* p : pp) BVH_CHECK(cudaFreeAsync(p, st));
@@ -570,7 +570,7 @@ std::string bvh_validate(const BvhStorage& s, void* stream)
     std::vector<float4> nodes(4 * (size_t) n_int);
     BVH_CHECK(cudaMemcpyAsync(nodes.data(), s.nodes, nodes.size() * sizeof(float4), cudaMemcpyDeviceToHost,
                               (cudaStream_t) stream));
-    sync_stream(stream);
+    BVH_CHECK(cudaStreamSynchronize((cudaStream_t) stream));
     std::vector<int> seen_int(n_int, 0), seen_leaf(n, 0);
     std::vector<int> stack(1, s.root);
     while (!stack.empty()) {

@@ -213,11 +213,5 @@ inline void note_launch() { host_counters().launches++; }
 inline void note_h2d(size_t b) { host_counters().h2d += b; }
 inline void note_d2h(size_t b) { host_counters().d2h += b; }
 
-// Waits until the work queued on `stream` so far is done. A bake of a batch
-// sets blocking waits for its thread (many scenes wait at once, and spinning
-// waiters would take the host cores the other scenes' host steps need); a
-// lone bake spins, which wakes up sooner (bake.cu).
-void set_blocking_waits(bool on);
-void sync_stream(void* stream);
 
 }  // namespace lg
