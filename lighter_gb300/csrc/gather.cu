@@ -37,6 +37,9 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <condition_variable>
+#include <functional>
+#include <memory>
 #include <mutex>
 #include <stdexcept>
 #include <string>
@@ -667,62 +670,113 @@ struct PinBuf {
     }
 };
 
+// Host threads kept by a gather for its host-buffer copies: run(k, f) calls
+// f(0 .. k-1) on the workers (and the caller) and returns when all are done.
+struct StagePool {
+    std::vector<std::thread> th;
+    std::mutex mu;
+    std::condition_variable cv_go, cv_done;
+    std::function<void(int)> job;
+    int n_job = 0, next = 0, done = 0;
+    unsigned long long gen = 0;
+    bool quit = false;
+
+    void start(int workers)
+    {
+        for (int w = 0; w < workers; ++w)
+            th.emplace_back([this]() {
+                unsigned long long seen = 0;
+                std::unique_lock<std::mutex> lk(mu);
+                for (;;) {
+                    cv_go.wait(lk, [&] { return quit || gen != seen; });
+                    if (quit) return;
+                    seen = gen;
+                    drain(lk);
+                }
+            });
+    }
+    // takes items until none are left; called with the lock held
+    void drain(std::unique_lock<std::mutex>& lk)
+    {
+        while (next < n_job) {
+            const int t = next++;
+            lk.unlock();
+            job(t);
+            lk.lock();
+            if (++done == n_job) cv_done.notify_all();
+        }
+    }
+    void run(int k, std::function<void(int)> f)
+    {
+        std::unique_lock<std::mutex> lk(mu);
+        job = std::move(f);
+        n_job = k;
+        next = done = 0;
+        ++gen;
+        cv_go.notify_all();
+        drain(lk);
+        cv_done.wait(lk, [&] { return done == n_job; });
+    }
+    ~StagePool()
+    {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            quit = true;
+        }
+        cv_go.notify_all();
+        for (auto& t : th) t.join();
+    }
+};
+
 // Host <-> device copies of the host-buffer entry point through kept
 // page-locked buffers. A copy straight from the caller's pageable memory runs
-// at about 10 GB/s; here the bytes are cut into one slice per host thread,
-// each thread copies its slice into the page-locked buffer and queues that
-// slice's DMA at once, so the DMA of early slices overlaps the host copies of
-// later ones (and the reverse for the result: each slice's DMA is followed by
-// an event its thread waits on before copying the slice out).
-constexpr int kStageThreads = 8;
+// at about 10 GB/s; here the bytes are cut into slices, the pool's threads
+// copy the slices into the page-locked buffer and each queues its slice's
+// DMA at once, so the DMA of early slices overlaps the host copies of later
+// ones (and the reverse for the result: each slice's DMA is followed by an
+// event its thread waits on before copying the slice out).
 constexpr size_t kStageMinSlice = 1 << 20;
 
-int stage_slices(size_t bytes)
+int stage_slices(size_t bytes, int threads)
 {
-    return (int) std::max<size_t>(1, std::min<size_t>(kStageThreads, bytes / kStageMinSlice));
+    return (int) std::max<size_t>(1, std::min<size_t>((size_t) threads, bytes / kStageMinSlice));
 }
 
-void stage_h2d(void* dev, const void* host, size_t bytes, PinBuf& pin, cudaStream_t s)
+void stage_h2d(void* dev, const void* host, size_t bytes, PinBuf& pin, cudaStream_t s, StagePool& pool, int threads)
 {
     if (!bytes) return;
     pin.ensure(bytes);
-    const int k = stage_slices(bytes);
+    const int k = stage_slices(bytes, threads);
     const size_t step = (bytes / k + 255) / 256 * 256;
-    std::vector<std::thread> th;
     std::vector<cudaError_t> rc(k, cudaSuccess);
-    for (int t = 0; t < k; ++t)
-        th.emplace_back([&, t]() {
-            const size_t a = std::min(bytes, t * step), b = std::min(bytes, a + step);
-            if (a >= b) return;
-            memcpy((char*) pin.p + a, (const char*) host + a, b - a);
-            rc[t] = cudaMemcpyAsync((char*) dev + a, (char*) pin.p + a, b - a, cudaMemcpyHostToDevice, s);
-        });
-    for (auto& x : th) x.join();
+    pool.run(k, [&](int t) {
+        const size_t a = std::min(bytes, t * step), b = std::min(bytes, a + step);
+        if (a >= b) return;
+        memcpy((char*) pin.p + a, (const char*) host + a, b - a);
+        rc[t] = cudaMemcpyAsync((char*) dev + a, (char*) pin.p + a, b - a, cudaMemcpyHostToDevice, s);
+    });
     for (cudaError_t e : rc) GCK(e);
 }
 
-void stage_d2h(void* host, const void* dev, size_t bytes, PinBuf& pin, cudaStream_t s)
+void stage_d2h(void* host, const void* dev, size_t bytes, PinBuf& pin, cudaStream_t s, StagePool& pool, int threads)
 {
     if (!bytes) return;
     pin.ensure(bytes);
-    const int k = stage_slices(bytes);
+    const int k = stage_slices(bytes, threads);
     const size_t step = (bytes / k + 255) / 256 * 256;
     std::vector<cudaEvent_t> ev(k, nullptr);
     for (int t = 0; t < k; ++t) {
         const size_t a = std::min(bytes, t * step), b = std::min(bytes, a + step);
-        GCK(cudaEventCreateWithFlags(&ev[t], cudaEventDisableTiming | cudaEventBlockingSync));
+        GCK(cudaEventCreateWithFlags(&ev[t], cudaEventDisableTiming));
         if (a < b) GCK(cudaMemcpyAsync((char*) pin.p + a, (const char*) dev + a, b - a, cudaMemcpyDeviceToHost, s));
         GCK(cudaEventRecord(ev[t], s));
     }
-    std::vector<std::thread> th;
     std::vector<cudaError_t> rc(k, cudaSuccess);
-    for (int t = 0; t < k; ++t)
-        th.emplace_back([&, t]() {
-            const size_t a = std::min(bytes, t * step), b = std::min(bytes, a + step);
-            rc[t] = cudaEventSynchronize(ev[t]);
-            if (rc[t] == cudaSuccess && a < b) memcpy((char*) host + a, (const char*) pin.p + a, b - a);
-        });
-    for (auto& x : th) x.join();
+    pool.run(k, [&](int t) {
+        const size_t a = std::min(bytes, t * step), b = std::min(bytes, a + step);
+        rc[t] = cudaEventSynchronize(ev[t]);
+        if (rc[t] == cudaSuccess && a < b) memcpy((char*) host + a, (const char*) pin.p + a, b - a);
+    });
     for (cudaEvent_t e : ev) cudaEventDestroy(e);
     for (cudaError_t e : rc) GCK(e);
 }
@@ -750,6 +804,8 @@ struct ltrg_Gather {
     DevBuf partial, xh, xl, x32, btmp, err, emax;
     DevBuf h_alb, h_E, h_out;     // device copies for the host-buffer entry point
     PinBuf pin_in, pin_out;       // its page-locked staging
+    std::unique_ptr<StagePool> pool;   // its host copy threads (started by the first host-buffer solve)
+    int pool_threads = 0;
     uint64_t links = 0, vis_rays = 0, pairs = 0;
     double ms_build = 0;
     u32 stall_us = 0;             // ltrdbg_GatherStallNextSolve
@@ -1158,11 +1214,16 @@ LTRAPI LTRBOOL ltrg_GatherSolve(ltrg_Gather* g, const float* albedo_rgb, const f
         g->h_E.ensure((size_t) n * R * 4);
         g->h_out.ensure((size_t) n * R * 4);
         GCK(cudaMemcpyAsync(g->h_alb.p, albedo_rgb, (size_t) n * 3 * 4, cudaMemcpyHostToDevice, s));
-        stage_h2d(g->h_E.p, emission, (size_t) n * R * 4, g->pin_in, s);
+        if (!g->pool) {
+            g->pool_threads = std::max(1, std::min(16, (int) std::thread::hardware_concurrency()));
+            g->pool.reset(new StagePool);
+            g->pool->start(g->pool_threads - 1);   // the calling thread works too
+        }
+        stage_h2d(g->h_E.p, emission, (size_t) n * R * 4, g->pin_in, s, *g->pool, g->pool_threads);
         note_h2d((size_t) n * (3 + R) * 4);
         g->solve(g->h_alb.as<float>(), g->h_E.as<float>(), R, bounces, precision, refine, g->h_out.as<float>(), stats,
                  s);
-        stage_d2h(out, g->h_out.p, (size_t) n * R * 4, g->pin_out, s);
+        stage_d2h(out, g->h_out.p, (size_t) n * R * 4, g->pin_out, s, *g->pool, g->pool_threads);
         note_d2h((size_t) n * R * 4);
         GCK(cudaStreamSynchronize(s));
     } catch (const std::exception& e) {
