@@ -393,11 +393,20 @@ def run_gather(args, local):
         # end to end through the host-buffer entry point (inputs and result cross the
         # CPU-GPU link), into one host output buffer the caller keeps, as an application would
         hout = np.empty((n, R), np.float32)
-        g.solve(sc["albedo"], sc["emission"], bounces, 1, 1, out=hout)
-        t0 = time.perf_counter()
-        for _ in range(args.gather_steps):
+
+        def e2e_time():
             g.solve(sc["albedo"], sc["emission"], bounces, 1, 1, out=hout)
-        e2e = (time.perf_counter() - t0) / args.gather_steps
+            t0 = time.perf_counter()
+            for _ in range(args.gather_steps):
+                g.solve(sc["albedo"], sc["emission"], bounces, 1, 1, out=hout)
+            return (time.perf_counter() - t0) / args.gather_steps
+
+        host_path = {1: "staged", 2: "direct"}
+        g.host_path(1)
+        e2e_staged = e2e_time()
+        g.host_path(0)
+        e2e = e2e_time()
+        path = host_path[g.host_path()]
         dev_fp16_rhs = modes["fp16_rhs"]["s_per_bounce"] * bounces
         st0 = g.solve_device(alb.data_ptr(), E.data_ptr(), R, 0, B.data_ptr(), 1, 1)
         out.update({
@@ -406,6 +415,7 @@ def run_gather(args, local):
             "modes": modes,
             "e2e_s_per_solve_fp16_rhs": e2e, "e2e_bytes": {"h2d": int(n * (R + 3) * 4), "d2h": int(n * R * 4)},
             "device_s_per_solve_fp16_rhs": dev_fp16_rhs, "e2e_over_device_fp16_rhs": e2e / dev_fp16_rhs,
+            "e2e_host_path": path, "e2e_s_per_solve_fp16_rhs_staged": e2e_staged,
             "speedup_fp16_rhs_vs_fp32": modes["fp32"]["s_per_bounce"] / modes["fp16_rhs"]["s_per_bounce"],
             "speedup_fp16_vs_fp32": modes["fp32"]["s_per_bounce"] / modes["fp16"]["s_per_bounce"],
             "fp32_cublas_sgemm_s_per_bounce": cublas_s,

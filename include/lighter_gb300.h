@@ -224,6 +224,16 @@ LTRAPI const char* ltrg_GatherLastError(ltrg_Gather* g);
  * fails with the error word in ltrg_GatherLastError, and later solves run
  * normally. No GPU fault or hang is involved. wait_us in 1..2000000. */
 LTRAPI LTRBOOL ltrdbg_GatherStallNextSolve(ltrg_Gather* g, u32 wait_us);
+/* How ltrg_GatherSolve moves its host buffers (test and measurement hook).
+ * mode 0: by device (the default): where kernels may address pageable host
+ * memory (cudaDevAttrPageableMemoryAccess, e.g. Grace systems), copy kernels
+ * read the inputs and write the result over the CPU-GPU link; elsewhere the
+ * buffers go through page-locked staging filled by host threads. mode 1: the
+ * staging always; mode 2: the copy kernels (returns 0 where the device
+ * cannot address pageable memory). The results are the same. */
+LTRAPI LTRBOOL ltrdbg_GatherHostPath(ltrg_Gather* g, int mode);
+/* The path the next ltrg_GatherSolve takes: 1 staged, 2 direct. */
+LTRAPI int ltrdbg_GatherHostPathUsed(ltrg_Gather* g);
 /* B after `bounces` sweeps for R right-hand sides; host buffers:
  *   albedo_rgb n x 3, emission n x R, out n x R (row-major).
  * precision LTRG_F_*, refine LTRG_REFINE_*; for FP16/BF16 R <= 256.

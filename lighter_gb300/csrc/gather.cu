@@ -670,6 +670,41 @@ struct PinBuf {
     }
 };
 
+// Copy of `n` floats by the GPU where the host's pageable memory is directly
+// addressable by kernels (cudaDevAttrPageableMemoryAccess, e.g. Grace systems:
+// the GPU walks the host page tables over the CPU-GPU link): one of src and
+// dst is the caller's pageable host buffer. 16-byte vectors when both are
+// aligned, single floats otherwise.
+__global__ void k_copy_floats(float* __restrict__ dst, const float* __restrict__ src, size_t n)
+{
+    const size_t stride = (size_t) gridDim.x * blockDim.x;
+    const size_t t0 = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
+    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15u) == 0) {
+        const size_t n4 = n / 4;
+        float4* d4 = reinterpret_cast<float4*>(dst);
+        const float4* s4 = reinterpret_cast<const float4*>(src);
+        for (size_t i = t0; i < n4; i += stride) d4[i] = s4[i];
+        for (size_t i = 4 * n4 + t0; i < n; i += stride) dst[i] = src[i];
+    } else {
+        for (size_t i = t0; i < n; i += stride) dst[i] = src[i];
+    }
+}
+
+// Whether kernels on `device` may address pageable host memory (queried once).
+bool pageable_access(int device)
+{
+    static std::mutex mu;
+    static int known[64] = {};   // 0 unknown, 1 no, 2 yes
+    if (device < 0 || device >= 64) return false;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!known[device]) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) v = 0;
+        known[device] = v ? 2 : 1;
+    }
+    return known[device] == 2;
+}
+
 // Host threads kept by a gather for its host-buffer copies: run(k, f) calls
 // f(0 .. k-1) on the workers (and the caller) and returns when all are done.
 struct StagePool {
@@ -809,6 +844,7 @@ struct ltrg_Gather {
     uint64_t links = 0, vis_rays = 0, pairs = 0;
     double ms_build = 0;
     u32 stall_us = 0;             // ltrdbg_GatherStallNextSolve
+    int host_path = 0;            // ltrdbg_GatherHostPath: 0 by device, 1 staged, 2 direct
     std::string error;
     std::mutex mu;
 
@@ -1175,6 +1211,22 @@ LTRAPI LTRBOOL ltrdbg_GatherStallNextSolve(ltrg_Gather* g, u32 wait_us)
     return 1;
 }
 
+LTRAPI LTRBOOL ltrdbg_GatherHostPath(ltrg_Gather* g, int mode)
+{
+    if (!g || mode < 0 || mode > 2) return 0;
+    std::lock_guard<std::mutex> lk(g->mu);
+    if (mode == 2 && !pageable_access(g->device)) return 0;
+    g->host_path = mode;
+    return 1;
+}
+
+LTRAPI int ltrdbg_GatherHostPathUsed(ltrg_Gather* g)
+{
+    if (!g) return 0;
+    std::lock_guard<std::mutex> lk(g->mu);
+    return g->host_path ? g->host_path : (pageable_access(g->device) ? 2 : 1);
+}
+
 LTRAPI LTRBOOL ltrg_GatherSolveDevice(ltrg_Gather* g, const float* albedo_rgb, const float* emission, u32 R,
                                       int bounces, int precision, int refine, float* out, ltrg_GatherStats* stats,
                                       void* stream)
@@ -1213,17 +1265,31 @@ LTRAPI LTRBOOL ltrg_GatherSolve(ltrg_Gather* g, const float* albedo_rgb, const f
         g->h_alb.ensure((size_t) n * 3 * 4);
         g->h_E.ensure((size_t) n * R * 4);
         g->h_out.ensure((size_t) n * R * 4);
-        GCK(cudaMemcpyAsync(g->h_alb.p, albedo_rgb, (size_t) n * 3 * 4, cudaMemcpyHostToDevice, s));
-        if (!g->pool) {
-            g->pool_threads = std::max(1, std::min(16, (int) std::thread::hardware_concurrency()));
-            g->pool.reset(new StagePool);
-            g->pool->start(g->pool_threads - 1);   // the calling thread works too
+        const bool direct = g->host_path ? g->host_path == 2 : pageable_access(g->device);
+        const unsigned cgrid = (unsigned) g->sm_count * 8;
+        if (direct) {
+            // the GPU reads the caller's arrays over the CPU-GPU link: no host copies
+            k_copy_floats<<<cgrid, 256, 0, s>>>(g->h_alb.as<float>(), albedo_rgb, (size_t) n * 3); note_launch();
+            k_copy_floats<<<cgrid, 256, 0, s>>>(g->h_E.as<float>(), emission, (size_t) n * R); note_launch();
+            GCK(cudaGetLastError());
+        } else {
+            GCK(cudaMemcpyAsync(g->h_alb.p, albedo_rgb, (size_t) n * 3 * 4, cudaMemcpyHostToDevice, s));
+            if (!g->pool) {
+                g->pool_threads = std::max(1, std::min(16, (int) std::thread::hardware_concurrency()));
+                g->pool.reset(new StagePool);
+                g->pool->start(g->pool_threads - 1);   // the calling thread works too
+            }
+            stage_h2d(g->h_E.p, emission, (size_t) n * R * 4, g->pin_in, s, *g->pool, g->pool_threads);
         }
-        stage_h2d(g->h_E.p, emission, (size_t) n * R * 4, g->pin_in, s, *g->pool, g->pool_threads);
         note_h2d((size_t) n * (3 + R) * 4);
         g->solve(g->h_alb.as<float>(), g->h_E.as<float>(), R, bounces, precision, refine, g->h_out.as<float>(), stats,
                  s);
-        stage_d2h(out, g->h_out.p, (size_t) n * R * 4, g->pin_out, s, *g->pool, g->pool_threads);
+        if (direct) {
+            k_copy_floats<<<cgrid, 256, 0, s>>>(out, g->h_out.as<float>(), (size_t) n * R); note_launch();
+            GCK(cudaGetLastError());
+        } else {
+            stage_d2h(out, g->h_out.p, (size_t) n * R * 4, g->pin_out, s, *g->pool, g->pool_threads);
+        }
         note_d2h((size_t) n * R * 4);
         GCK(cudaStreamSynchronize(s));
     } catch (const std::exception& e) {

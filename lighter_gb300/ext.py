@@ -162,6 +162,8 @@ EXT_API.update({
     "ltrg_GatherGetG": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ltrg_GatherLastError": (C.c_char_p, [C.c_void_p]),
     "ltrdbg_GatherStallNextSolve": (C.c_int, [C.c_void_p, u32]),
+    "ltrdbg_GatherHostPath": (C.c_int, [C.c_void_p, C.c_int]),
+    "ltrdbg_GatherHostPathUsed": (C.c_int, [C.c_void_p]),
     "ltrg_GatherSolve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, u32, C.c_int, C.c_int, C.c_int, C.c_void_p,
                                    C.POINTER(GatherStats)]),
     "ltrg_GatherSolveDevice": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, u32, C.c_int, C.c_int, C.c_int,

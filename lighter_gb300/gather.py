@@ -69,6 +69,13 @@ class Gather:
         if not self.lib.ltrg_GatherSetChunk(self.h, int(k_blocks)):
             raise RuntimeError("ltrg_GatherSetChunk failed")
 
+    def host_path(self, mode: int | None = None) -> int:
+        """ltrdbg_GatherHostPath: how solve() moves its host arrays (0 by device, 1 staged,
+        2 read/written by the GPU in place); returns the path the next solve takes."""
+        if mode is not None and not self.lib.ltrdbg_GatherHostPath(self.h, int(mode)):
+            raise RuntimeError(f"host path {mode} is not available on this device")
+        return int(self.lib.ltrdbg_GatherHostPathUsed(self.h))
+
     def stall_next_solve(self, wait_us: int):
         """ltrdbg_GatherStallNextSolve: the next 16-bit solve's waits expire after wait_us."""
         if not self.lib.ltrdbg_GatherStallNextSolve(self.h, int(wait_us)):

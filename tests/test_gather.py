@@ -266,6 +266,40 @@ def test_device_entry_point_matches_host(small):
 
 
 @pytest.mark.gpu
+def test_host_paths_agree(small):
+    """The host-buffer solve through page-locked staging and through copy
+    kernels that address the caller's pageable arrays directly (where the
+    device can) return the same bits, for 16-byte aligned and misaligned
+    arrays; the default path is the direct one on such devices."""
+    sc, g = small
+    E = sc["emission"]
+    n, R = E.shape
+    ref, _ = g.solve(sc["albedo"], E, 2, FP16, REFINE_RHS)
+    # misaligned copies: views 4 bytes into larger arrays
+    alb_buf = np.zeros(n * 3 + 1, np.float32)
+    alb_buf[1:] = sc["albedo"].ravel()
+    E_buf = np.zeros(n * R + 1, np.float32)
+    E_buf[1:] = E.ravel()
+    out_buf = np.full(n * R + 1, np.nan, np.float32)
+    alb_m, E_m, out_m = alb_buf[1:].reshape(n, 3), E_buf[1:].reshape(n, R), out_buf[1:].reshape(n, R)
+    assert alb_m.ctypes.data % 16 and out_m.ctypes.data % 16
+    direct_ok = bool(g.lib.ltrdbg_GatherHostPath(g.h, 2))
+    paths = [1, 2] if direct_ok else [1]
+    try:
+        for mode in paths:
+            assert g.host_path(mode) == mode
+            a, _ = g.solve(sc["albedo"], E, 2, FP16, REFINE_RHS)
+            np.testing.assert_array_equal(a, ref)
+            out_m[...] = np.nan
+            g.solve(alb_m, E_m, 2, FP16, REFINE_RHS, out=out_m)
+            np.testing.assert_array_equal(out_m, ref)
+            assert np.isnan(out_buf[0])
+    finally:
+        g.host_path(0)
+    assert g.host_path() == (2 if direct_ok else 1)
+
+
+@pytest.mark.gpu
 def test_rejects_too_many_rhs(small):
     sc, g = small
     E = np.zeros((g.n, 300), np.float32)
