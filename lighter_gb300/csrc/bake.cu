@@ -3226,7 +3226,7 @@ void run_bake(ltr_Scene* S)
     for (int k = 0; k < 4; ++k) {
         if (!err_words[k]) continue;
         char msg[160];
-        snprintf(msg, sizeof(msg), "%s kernel reported error word 0x%08x (bit 0: traversal stack overflow)", kStageName[k], err_words[k]);
+        snprintf(msg, sizeof(msg), "%s kernel reported error word 0x%08x (bit 0: traversal stack overflow; bit 1 (radiosity): a bounded wait for staged form factors expired)", kStageName[k], err_words[k]);
         throw std::runtime_error(msg);
     }
 

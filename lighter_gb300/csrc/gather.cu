@@ -48,6 +48,7 @@
 
 #include "../../include/lighter_gb300.h"
 #include "bvh.cuh"
+#include "async.cuh"
 #include "radiosity.cuh"
 
 namespace lg {
@@ -77,51 +78,6 @@ constexpr unsigned long long kWaitCycles = 4000000000ull;   // about 2 s at 2 GH
 constexpr u32 kErrProducer = 1u, kErrMma = 2u, kErrEpilogue = 4u, kErrDrain = 8u;
 
 // ----------------------------------------------------------------------------- PTX helpers
-
-__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t) __cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(bar)) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(saddr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait for the phase of parity `parity`: false (and the error bit)
-// after `limit` SM clock cycles.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, u32* err, u32 bit, unsigned long long limit)
-{
-    if (mbar_try(bar, parity)) return true;
-    const long long t0 = clock64();
-    while (!mbar_try(bar, parity)) {
-        if (clock64() - t0 > (long long) limit) {
-            atomicOr(err, bit);
-            return false;
-        }
-    }
-    return true;
-}
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y)
 {

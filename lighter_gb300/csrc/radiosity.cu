@@ -8,6 +8,7 @@
 #include <string>
 #include <type_traits>
 
+#include "async.cuh"
 #include "radiosity.cuh"
 
 namespace lg {
@@ -216,58 +217,128 @@ __global__ void k_rad_x(u32 n, const float4* __restrict__ out, const float4* __r
     X[j] = st4(x, 0.0f);
 }
 
-// One vector load of V entries of F (16 or 8 bytes), and its entries as floats.
-template <int B> struct RawF;
-template <> struct RawF<16> {
-    uint4 u;
-    __device__ __forceinline__ void load(const void* p) { u = __ldcs(reinterpret_cast<const uint4*>(p)); }
-    __device__ __forceinline__ unsigned bits() const { return u.x | u.y | u.z | u.w; }
-};
-template <> struct RawF<8> {
+// Four entries of a 16-bit F (one 8-byte load, streamed once) and their values.
+struct Raw4x16 {
     uint2 u;
     __device__ __forceinline__ void load(const void* p) { u = __ldcs(reinterpret_cast<const uint2*>(p)); }
     __device__ __forceinline__ unsigned bits() const { return u.x | u.y; }
 };
-template <class T, int V> __device__ __forceinline__ void unpack(const void* raw, float* v)
+template <class T> __device__ __forceinline__ void unpack4(const uint2& raw, float* v)
 {
-    if constexpr (sizeof(T) == 4) {
 #pragma unroll
-        for (int k = 0; k < V; ++k) v[k] = reinterpret_cast<const float*>(raw)[k];
-    } else {
+    for (int k = 0; k < 2; ++k) {
+        float2 f;
+        if constexpr (std::is_same<T, __half>::value) f = __half22float2(reinterpret_cast<const __half2*>(&raw)[k]);
+        else f = __bfloat1622float2(reinterpret_cast<const __nv_bfloat162*>(&raw)[k]);
+        v[2 * k] = f.x; v[2 * k + 1] = f.y;
+    }
+}
+// Bits of entry k of a 16-byte vector of F (entries of type T) held in words w.
+template <class T> __device__ __forceinline__ unsigned entry_bits(const unsigned* w, int k)
+{
+    if constexpr (sizeof(T) == 4) return w[k];
+    else return (w[k >> 1] >> (16 * (k & 1))) & 0xffffu;
+}
+template <class T> __device__ __forceinline__ float entry_f(const unsigned* w, int k)
+{
+    if constexpr (sizeof(T) == 4) return __uint_as_float(w[k]);
+    else if constexpr (std::is_same<T, __half>::value)
+        return __half2float(__ushort_as_half((unsigned short) entry_bits<T>(w, k)));
+    else return __uint_as_float(entry_bits<T>(w, k) << 16);   // bf16 is the high half of a float
+}
+
+constexpr int kRadRows = 4;   // rows of F per warp in the bounce products
+constexpr int kRadDepth = 4;  // steps of F a lane has in flight in the refined bounce
+
+// One 16-byte vector (entries c V .. c V + V - 1) of each of a warp's rows,
+// raw words w, added to the row sums of an F that is not refined. An entry's X
+// is loaded when the entry is non-zero in any of the rows; the rows then add
+// x * f without testing f: a zero entry adds +0 to a sum of non-negative terms,
+// which leaves it unchanged bit for bit. A 16-bit F uses fused multiply-adds (its
+// rounding is not the FP32 F's); FP32 keeps the separate multiply and add of the
+// refined product, so both sum the same values in the same order.
+template <class T>
+__device__ __forceinline__ void plain_vector(const unsigned (&w)[kRadRows][4], u32 c, const float4* __restrict__ X,
+                                             float (&acc)[kRadRows][3])
+{
+    constexpr int V = 16 / (int) sizeof(T);
+    unsigned m[4];
 #pragma unroll
-        for (int k = 0; k < V / 2; ++k) {
-            float2 f;
-            if constexpr (std::is_same<T, __half>::value) f = __half22float2(reinterpret_cast<const __half2*>(raw)[k]);
-            else f = __bfloat1622float2(reinterpret_cast<const __nv_bfloat162*>(raw)[k]);
-            v[2 * k] = f.x; v[2 * k + 1] = f.y;
+    for (int q = 0; q < 4; ++q) {
+        m[q] = w[0][q];
+#pragma unroll
+        for (int r = 1; r < kRadRows; ++r) m[q] |= w[r][q];
+    }
+    // F is sparse (pairs more than a few metres apart have factors below
+    // SMALL_FLOAT, and occluded pairs are 0): a vector that is zero in all the
+    // rows is skipped with one test (F holds no negative values and its zeros
+    // are +0, so "no bit set" is "all entries zero")
+    if (!(m[0] | m[1] | m[2] | m[3])) return;
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+        if (!entry_bits<T>(m, k)) continue;
+        const float4 x = __ldg(&X[c * V + k]);
+#pragma unroll
+        for (int r = 0; r < kRadRows; ++r) {
+            const float fv = entry_f<T>(w[r], k);
+            if constexpr (sizeof(T) == 4) {
+                acc[r][0] += x.x * fv; acc[r][1] += x.y * fv; acc[r][2] += x.z * fv;
+            } else {
+                acc[r][0] = fmaf(x.x, fv, acc[r][0]);
+                acc[r][1] = fmaf(x.y, fv, acc[r][1]);
+                acc[r][2] = fmaf(x.z, fv, acc[r][2]);
+            }
         }
     }
 }
 
-constexpr int kRadRows = 4;   // rows of F per warp in the bounce product
-constexpr int kRadDepth = 4;  // steps of F a lane has in flight in the bounce product
-
-// Y = F X (one bounce's gather). F is streamed once per bounce, so the kernel is
-// HBM-bound: a warp takes kRadRows rows and reads them V entries per lane per
-// row (16 bytes; the next step's loads issued before this step's arithmetic),
-// and each X_j it loads serves all its rows. A zero entry (no link) skips its X
-// load. Rows are ld entries apart, ld a multiple of 8 with zeros past n, so
-// every row starts on a 16-byte boundary.
-// kExact: F serves only as the link mask and the factor of every linked pair is
-// recomputed in FP32 with pair_pretest, lower index first as k_ff_pretest
-// computes it, i.e. bit-for-bit the value an FP32 F holds. A linked factor is
-// >= SMALL_FLOAT, which neither FP16 nor BF16 rounds to 0, so a 16-bit mask is
-// the FP32 one. kExact reads 4 entries per lane (8-byte loads of a 16-bit F),
-// the FP32 kernel's split of columns over lanes, so both sum in the same order:
-// the kExact product of a 16-bit F is the FP32 product.
-template <class T, bool kExact, int kDepth = 2>
-__global__ void __launch_bounds__(256) k_rad_gemv(u32 n, size_t ld, const T* __restrict__ F,
-                                                  const float4* __restrict__ pos, const float4* __restrict__ nrm,
-                                                  const float* __restrict__ up, const float4* __restrict__ X,
-                                                  float4* __restrict__ Y)
+// Warp sums of the row sums and the bounce's updates (lane 0 writes).
+__device__ __forceinline__ void bounce_epilogue(u32 n, u32 r0, float (&acc)[kRadRows][3], const float* __restrict__ up,
+                                                const float4* __restrict__ da, float4* __restrict__ total,
+                                                float4* __restrict__ out, float4* __restrict__ Xn)
 {
-    constexpr int V = kExact ? 4 : 16 / (int) sizeof(T);
-    using Raw = RawF<V * sizeof(T)>;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int r = 0; r < kRadRows; ++r)
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+            for (int o = 16; o > 0; o >>= 1) acc[r][q] += __shfl_down_sync(0xffffffffu, acc[r][q], o);
+    if (lane == 0) {
+#pragma unroll
+        for (int r = 0; r < kRadRows; ++r) {
+            const u32 j = r0 + r;
+            if (j >= n) continue;
+            const float s = up ? up[j] : 1.0f;   // row scale of an FP16 F (exact)
+            const float4 y = make_float4(acc[r][0] * s, acc[r][1] * s, acc[r][2] * s, 0.0f);
+            const float4 t = total[j], d = da[j];
+            total[j] = make_float4(t.x + y.x, t.y + y.y, t.z + y.z, 0.0f);
+            out[j] = y;
+            Xn[j] = st4((mk(y.x, y.y, y.z) * mk(d.x, d.y, d.z)) * d.w, 0.0f);
+        }
+    }
+}
+
+// A refined bounce of a 16-bit F (lighter.cpp:767-797): Y = F X with F serving
+// only as the link mask; the factor of every linked pair is recomputed in FP32
+// with pair_pretest, lower index first as k_ff_pretest computes it, i.e. bit for
+// bit the value an FP32 F holds (a linked factor is >= SMALL_FLOAT, which
+// neither FP16 nor BF16 rounds to 0, so a 16-bit mask is the FP32 one). Then
+// total += Y, out = Y and the next bounce's X in the epilogue. A warp takes
+// kRadRows rows and reads them 4 entries per lane per row (8-byte loads, the
+// loads of the next kDepth - 1 steps issued before a step's arithmetic); lane l
+// takes the 4-entry vectors l, l + 32, ... in order, as k_rad_stream does for
+// an FP32 F, so the refined product of a 16-bit F is the FP32 product. The
+// recomputed factors make this kernel arithmetic-bound, not HBM-bound.
+template <class T, int kDepth>
+__global__ void __launch_bounds__(256) k_rad_refined(u32 n, size_t ld, const T* __restrict__ F,
+                                                     const float4* __restrict__ pos, const float4* __restrict__ nrm,
+                                                     const float4* __restrict__ X, const float4* __restrict__ da,
+                                                     float4* __restrict__ total, float4* __restrict__ out,
+                                                     float4* __restrict__ Xn)
+{
+    static_assert(sizeof(T) == 2, "the refined bounce reads a 16-bit F");
+    constexpr int V = 4;
+    using Raw = Raw4x16;
     const int lane = threadIdx.x & 31;
     const u32 r0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kRadRows;
     if (r0 >= n) return;
@@ -278,15 +349,13 @@ __global__ void __launch_bounds__(256) k_rad_gemv(u32 n, size_t ld, const T* __r
     for (int r = 0; r < kRadRows; ++r) {
         ri[r] = min(r0 + r, n - 1);   // rows past n repeat the last row and are not written
         rows[r] = F + (size_t) ri[r] * ld;
-        if (kExact) { ap[r] = ld3(pos[ri[r]]); an[r] = ld3(nrm[ri[r]]); }
+        ap[r] = ld3(pos[ri[r]]);
+        an[r] = ld3(nrm[ri[r]]);
     }
     float acc[kRadRows][3];
 #pragma unroll
     for (int r = 0; r < kRadRows; ++r) acc[r][0] = acc[r][1] = acc[r][2] = 0.0f;
     const u32 nv = (u32) (ld / V);
-    // software pipeline kDepth steps deep: the loads of step c + 32 (kDepth - 1)
-    // are issued before step c's arithmetic (each lane still walks its columns
-    // in increasing order, so the sums keep their order)
     Raw buf[kDepth][kRadRows];
 #pragma unroll
     for (int d = 0; d < kDepth - 1; ++d) {
@@ -307,17 +376,13 @@ __global__ void __launch_bounds__(256) k_rad_gemv(u32 n, size_t ld, const T* __r
             }
             if (c >= nv) break;
             const Raw* cur = buf[d];
-            // F is sparse (pairs more than a few metres apart have factors below
-            // SMALL_FLOAT, and occluded pairs are 0): a vector that is zero in all the
-            // warp's rows is skipped with one test (F holds no negative values and its
-            // zeros are +0, so "no bit set" is "all entries zero")
-            unsigned nz = 0;
+            unsigned nz = 0;   // all four rows unlinked over these 4 columns: nothing to add
 #pragma unroll
             for (int r = 0; r < kRadRows; ++r) nz |= cur[r].bits();
             if (!nz) continue;
             float f[kRadRows][V];
 #pragma unroll
-            for (int r = 0; r < kRadRows; ++r) unpack<T, V>(&cur[r].u, f[r]);
+            for (int r = 0; r < kRadRows; ++r) unpack4<T>(cur[r].u, f[r]);
 #pragma unroll
             for (int k = 0; k < V; ++k) {
                 bool any = false;
@@ -326,13 +391,12 @@ __global__ void __launch_bounds__(256) k_rad_gemv(u32 n, size_t ld, const T* __r
                 if (any) {
                     const u32 j = c * V + k;
                     const float4 x = __ldg(&X[j]);
-                    V3 bp, bn;
-                    if (kExact) { bp = ld3(pos[j]); bn = ld3(nrm[j]); }
+                    const V3 bp = ld3(pos[j]), bn = ld3(nrm[j]);
 #pragma unroll
                     for (int r = 0; r < kRadRows; ++r) {
                         if (f[r][k] != 0.0f) {
-                            float fv = f[r][k];
-                            if (kExact) fv = ri[r] < j ? pair_pretest(ap[r], an[r], bp, bn) : pair_pretest(bp, bn, ap[r], an[r]);
+                            const float fv = ri[r] < j ? pair_pretest(ap[r], an[r], bp, bn)
+                                                       : pair_pretest(bp, bn, ap[r], an[r]);
                             acc[r][0] += x.x * fv; acc[r][1] += x.y * fv; acc[r][2] += x.z * fv;
                         }
                     }
@@ -340,19 +404,109 @@ __global__ void __launch_bounds__(256) k_rad_gemv(u32 n, size_t ld, const T* __r
             }
         }
     }
+    bounce_epilogue(n, r0, acc, nullptr, da, total, out, Xn);
+}
+
+constexpr u32 kErrWait = 2u;   // radiosity error word: a bounded wait for staged F expired
+constexpr unsigned long long kStreamWaitCycles = 4000000000ull;   // about 2 s at 2 GHz
+
+// Launch shape of k_rad_stream: warps per CTA, ring stages per warp, and
+// 16-byte vectors per lane, row and stage.
+constexpr int kStreamWarps = 4, kStreamStages = 3, kStreamVec = 4;
+
+constexpr size_t stream_smem_bytes(int warps, int stages, int vec)
+{
+    return (size_t) warps * stages * kRadRows * vec * 512 + (size_t) warps * stages * 8;
+}
+
+// The bounce of an F that is not refined, with F staged through shared memory
+// by bulk asynchronous copies (cp.async.bulk, completing on an mbarrier per
+// stage) instead of through registers: a warp keeps kStages stages of its
+// kRadRows rows in flight (kStages x kRadRows x kVec x 512 bytes), far more
+// than registers hold, which is what an HBM stream of this many independent
+// rows needs to reach the memory's bandwidth. Each warp owns its rows and its
+// ring; lane 0 issues the copies and refills a stage once the warp has read it.
+// Lane l reads vectors l, l + 32, l + 64, ... of each row in increasing order,
+// the register kernel's order, so both give the same bits.
+template <class T, int kWarps, int kStages, int kVec>
+__global__ void __launch_bounds__(kWarps * 32) k_rad_stream(u32 n, size_t ld, const T* __restrict__ F,
+                                                            const float* __restrict__ up,
+                                                            const float4* __restrict__ X,
+                                                            const float4* __restrict__ da,
+                                                            float4* __restrict__ total, float4* __restrict__ out,
+                                                            float4* __restrict__ Xn, u32* err,
+                                                            unsigned long long wait_cycles)
+{
+    constexpr int V = 16 / (int) sizeof(T);       // entries per 16-byte vector
+    constexpr u32 kPart = kVec * 512u;            // bytes of one row in one stage
+    constexpr u32 kPer = 32u * kVec;              // vectors of one row in one stage
+    extern __shared__ __align__(128) unsigned char smem[];
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const u32 r0 = (blockIdx.x * kWarps + w) * kRadRows;
+    if (r0 >= n) return;   // the whole warp
+    unsigned char* ring = smem + (size_t) w * kStages * kRadRows * kPart;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + (size_t) kWarps * kStages * kRadRows * kPart) + w * kStages;
+    const T* rows[kRadRows];
 #pragma unroll
-    for (int r = 0; r < kRadRows; ++r)
-#pragma unroll
-        for (int q = 0; q < 3; ++q)
-            for (int o = 16; o > 0; o >>= 1) acc[r][q] += __shfl_down_sync(0xffffffffu, acc[r][q], o);
+    for (int r = 0; r < kRadRows; ++r) rows[r] = F + (size_t) min(r0 + r, n - 1) * ld;   // rows past n: not written
+    const u32 nv = (u32) (ld / V);               // vectors per row (ld V-aligned: rows on 16-byte boundaries)
+    const u32 nch = (nv + kPer - 1) / kPer;      // stages per row sweep
+    uint64_t policy = 0;
     if (lane == 0) {
 #pragma unroll
-        for (int r = 0; r < kRadRows; ++r) {
-            if (r0 + r >= n) continue;
-            const float s = (!kExact && up) ? up[r0 + r] : 1.0f;   // row scale of an FP16 F (exact)
-            Y[r0 + r] = make_float4(acc[r][0] * s, acc[r][1] * s, acc[r][2] * s, 0.0f);
-        }
+        for (int q = 0; q < kStages; ++q) mbar_init(&bar[q], 1);
+        mbar_init_fence();
+        policy = l2_evict_first_policy();
     }
+    __syncwarp();
+    // lane 0: chunk k of every row into stage k % kStages
+    auto issue = [&](u32 k) {
+        const u32 q = k % kStages;
+        const u32 v0 = k * kPer;
+        const u32 bytes = min(kPer, nv - v0) * 16u;
+        mbar_expect_tx(&bar[q], bytes * kRadRows);
+#pragma unroll
+        for (int r = 0; r < kRadRows; ++r)
+            bulk_g2s(ring + (size_t) (q * kRadRows + r) * kPart, rows[r] + (size_t) v0 * V, bytes, &bar[q], policy);
+    };
+    if (lane == 0)
+        for (u32 k = 0; k < nch && k < (u32) kStages; ++k) issue(k);
+    float acc[kRadRows][3];
+#pragma unroll
+    for (int r = 0; r < kRadRows; ++r) acc[r][0] = acc[r][1] = acc[r][2] = 0.0f;
+    u32 k = 0;
+    bool ok = true;
+    for (; k < nch; ++k) {
+        const u32 q = k % kStages;
+        ok = __all_sync(full, mbar_wait(&bar[q], (k / kStages) & 1u, err, kErrWait, wait_cycles));
+        if (!ok) break;
+#pragma unroll
+        for (int e = 0; e < kVec; ++e) {
+            const u32 c = k * kPer + 32u * e + lane;
+            if (c < nv) {
+                unsigned wv[kRadRows][4];
+#pragma unroll
+                for (int r = 0; r < kRadRows; ++r) {
+                    const uint4 u = *reinterpret_cast<const uint4*>(ring + (size_t) (q * kRadRows + r) * kPart +
+                                                                    512u * e + 16u * lane);
+                    wv[r][0] = u.x; wv[r][1] = u.y; wv[r][2] = u.z; wv[r][3] = u.w;
+                }
+                plain_vector<T>(wv, c, X, acc);
+            }
+        }
+        __syncwarp();   // every lane has read stage q before it is refilled
+        if (lane == 0 && k + kStages < nch) issue(k + kStages);
+    }
+    if (!ok) {
+        // a wait expired (error bit set): wait, bounded again, for the copies still
+        // issued into this warp's ring before the CTA's shared memory is released
+        if (lane == 0)
+            for (u32 j = k; j < nch && j < k + kStages; ++j)
+                if (!mbar_wait(&bar[j % kStages], (j / kStages) & 1u, err, kErrWait, wait_cycles)) break;
+        return;
+    }
+    bounce_epilogue(n, r0, acc, up, da, total, out, Xn);
 }
 
 // F (n x ld, stored type) widened to n x n floats (debug copy).
@@ -365,21 +519,16 @@ __global__ void k_f_widen(u32 n, size_t ld, const T* __restrict__ F, const float
     out[k] = to_f(F[(k / n) * ld + k % n]) * (up ? up[k / n] : 1.0f);
 }
 
-// total += Y, out = Y (lighter.cpp:784-796).
-__global__ void k_rad_update(u32 n, const float4* __restrict__ Y, float4* __restrict__ total, float4* __restrict__ out)
-{
-    u32 j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    float4 y = Y[j], t = total[j];
-    total[j] = make_float4(t.x + y.x, t.y + y.y, t.z + y.z, 0.0f);
-    out[j] = y;
-}
-
-// Both passes on `st`; returns the link and visibility-ray counts (synchronises
-// the stream once after the first pass, to size the pair list).
+// Both passes on `st`; returns the visibility-ray count and, when `counts_keep`
+// is null, the link count (synchronises the stream after the first pass, to size
+// the pair list, and then after the second for the link count). With
+// `counts_keep` (3 device words the caller owns) the link count stays in
+// counts_keep[1] and the function returns with the second pass still queued, so
+// the caller's next kernels are enqueued behind it.
 template <class T>
 RadFormFactors build_ff(u32 n, size_t ld, const float4* pos, const float4* nrm, const BvhView& bvh, ErrFlag err,
-                        int links, T* F, unsigned* rowmax, float* up, cudaStream_t st)
+                        int links, T* F, unsigned* rowmax, float* up, cudaStream_t st,
+                        unsigned long long* counts_keep = nullptr)
 {
     RadFormFactors out;
     if (n == 0) return out;
@@ -390,11 +539,13 @@ RadFormFactors build_ff(u32 n, size_t ld, const float4* pos, const float4* nrm, 
     unsigned long long cap = std::min<unsigned long long>(pairs, std::max<unsigned long long>(1ull << 24, pairs / 16));
     unsigned long long* counts = nullptr;   // [0] pairs that passed, [1] links kept, [2] work counter
     PairRef* cand = nullptr;
-    RCK(cudaMallocAsync(&counts, 3 * sizeof(unsigned long long), st));
+    unsigned long long* own_counts = nullptr;
+    if (counts_keep) counts = counts_keep;
+    else RCK(cudaMallocAsync(&own_counts, 3 * sizeof(unsigned long long), st)), counts = own_counts;
     struct Free {
         cudaStream_t st; void** p[2];
         ~Free() { for (void** q : p) if (*q) cudaFreeAsync(*q, st); }
-    } guard{st, {(void**) &counts, (void**) &cand}};
+    } guard{st, {(void**) &own_counts, (void**) &cand}};
     unsigned long long n_cand = 0;
     for (int attempt = 0; attempt < 2; ++attempt) {
         RCK(cudaMallocAsync(&cand, std::max<unsigned long long>(cap, 1) * sizeof(PairRef), st));
@@ -430,11 +581,13 @@ RadFormFactors build_ff(u32 n, size_t ld, const float4* pos, const float4* nrm, 
         note_launch();
         RCK(cudaGetLastError());
     }
-    unsigned long long hc[2] = {0, 0};
-    RCK(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(hc));
-    RCK(cudaStreamSynchronize(st));
     out.vis_rays = n_cand;
-    out.links = hc[1];
+    if (!counts_keep) {
+        unsigned long long hc[2] = {0, 0};
+        RCK(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(hc));
+        RCK(cudaStreamSynchronize(st));
+        out.links = hc[1];
+    }
     return out;
 }
 
@@ -453,14 +606,16 @@ RadResult solve_t(const RadDevInputs& in, const RadSettings& rs, const BvhView& 
                                  std::to_string(fbytes >> 20) + " MiB, more than the free device memory");
     T* F = nullptr;
     float4 *out, *X, *Y;
+    unsigned long long* counts;   // the form-factor build's counters, read after the bounces
     RCK(cudaMallocAsync(&F, fbytes ? fbytes : 1, st));
     RCK(cudaMallocAsync(&out, n * sizeof(float4), st));
     RCK(cudaMallocAsync(&X, n * sizeof(float4), st));
     RCK(cudaMallocAsync(&Y, n * sizeof(float4), st));
+    RCK(cudaMallocAsync(&counts, 3 * sizeof(unsigned long long), st));
     struct Free {
-        cudaStream_t st; void* p[4];
+        cudaStream_t st; void* p[5];
         ~Free() { for (void* q : p) if (q) cudaFreeAsync(q, st); }
-    } guard{st, {F, out, X, Y}};
+    } guard{st, {F, out, X, Y, counts}};
     float4* total = total_out;
     RCK(cudaMemcpyAsync(out, in.emit, n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
     if (total != in.emit) RCK(cudaMemcpyAsync(total, in.emit, n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
@@ -478,7 +633,8 @@ RadResult solve_t(const RadDevInputs& in, const RadSettings& rs, const BvhView& 
         RCK(cudaMallocAsync(&up, n * sizeof(float), st));
         RCK(cudaMallocAsync(&rowmax, n * sizeof(unsigned), st));
     }
-    RadFormFactors ff = build_ff<T>(n, ld, in.pos, in.nrm, bvh, err, rs.links, F, rowmax, up, st);
+    // the bounces are enqueued behind the visibility pass (no host wait between them)
+    RadFormFactors ff = build_ff<T>(n, ld, in.pos, in.nrm, bvh, err, rs.links, F, rowmax, up, st, counts);
     RCK(cudaEventRecord(e1, st));
     if (rs.f_host) {
         const size_t nn = (size_t) n * n;
@@ -489,22 +645,38 @@ RadResult solve_t(const RadDevInputs& in, const RadSettings& rs, const BvhView& 
         RCK(cudaMemcpyAsync(rs.f_host, wide, nn * sizeof(float), cudaMemcpyDeviceToHost, st)); note_d2h(nn * sizeof(float));
         RCK(cudaFreeAsync(wide, st));
     }
+    if (rs.bounces > 0) {
+        k_rad_x<<<(n + 255) / 256, 256, 0, st>>>(n, out, in.diff_area, X); note_launch();
+    }
     for (int b = 0; b < rs.bounces; ++b) {
         if (abort_flag && abort_flag->load()) break;
-        k_rad_x<<<(n + 255) / 256, 256, 0, st>>>(n, out, in.diff_area, X); note_launch();
+        const float4* Xb = (b & 1) ? Y : X;   // X of this bounce; the kernel writes the next one's
+        float4* Xnext = (b & 1) ? X : Y;
         // the last refine_steps bounces of a 16-bit F recompute the factors in FP32
         const bool exact = sizeof(T) < 4 && b >= rs.bounces - rs.refine_steps;
         const unsigned grid = (unsigned) ((((size_t) n + kRadRows - 1) / kRadRows * 32 + 255) / 256);
-        if (exact)
-            k_rad_gemv<T, true, kRadDepth><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, up, X, Y);
-        else
-            k_rad_gemv<T, false, kRadDepth><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, up, X, Y);
+        if constexpr (sizeof(T) == 2) {
+            if (exact) {
+                k_rad_refined<T, kRadDepth><<<grid, 256, 0, st>>>(n, ld, F, in.pos, in.nrm, Xb, in.diff_area, total,
+                                                                   out, Xnext);
+            }
+        }
+        if (!exact) {
+            auto kern = k_rad_stream<T, kStreamWarps, kStreamStages, kStreamVec>;
+            const size_t sm = stream_smem_bytes(kStreamWarps, kStreamStages, kStreamVec);
+            RCK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm));
+            const unsigned sgrid = (unsigned) (((size_t) n + kRadRows * kStreamWarps - 1) / (kRadRows * kStreamWarps));
+            kern<<<sgrid, kStreamWarps * 32, sm, st>>>(n, ld, F, up, Xb, in.diff_area, total, out, Xnext, err.word,
+                                                       kStreamWaitCycles);
+        }
         note_launch();
-        k_rad_update<<<(n + 255) / 256, 256, 0, st>>>(n, Y, total, out); note_launch();
         RCK(cudaGetLastError());
     }
     RCK(cudaEventRecord(e2, st));
+    unsigned long long hc[3] = {0, 0, 0};
+    RCK(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(hc));
     RCK(cudaStreamSynchronize(st));
+    ff.links = n ? hc[1] : 0;
     float m1 = 0, m2 = 0;
     cudaEventElapsedTime(&m1, e0, e1);
     cudaEventElapsedTime(&m2, e1, e2);
