@@ -253,6 +253,7 @@ struct FixupArgs {
     const int4* ref_inst;      // per instance: node offset, item offset, triangle offset, node count
     const float4* inst_box;    // per instance: (root mn.xyz, 0), (root mx.xyz, 0); inverted when empty
     const float* tri_xyz;      // shadow-part triangles, instance by instance in local order
+    const float4* tri_box;     // per triangle: (box mn.xyz, 0), (box mx.xyz, 0); unbounded for slivers
     int n_inst;
     u32 n_probe, n_samples;
     float max_correct_dist, corr_min_dot;
@@ -284,37 +285,104 @@ __device__ __forceinline__ void offset_one(const FixupArgs& a, V3 P1, V3 P2, V3 
     if (r >= 0.9f || hit_local == local) P = Pnew;
 }
 
-// One instance of the concave-edge pass: a depth-first walk (node items, left
-// subtree, right subtree) of its reference-shaped tree with the query box
-// P +- dist fixed at the start, while P moves.
-__device__ __forceinline__ void fixup_instance(const FixupArgs& a, int k, V3& P, V3 N, float dist)
+// Boxes of the concave-edge pass's triangles, for its exact rejection test: the
+// box of a well-shaped triangle (height at least 1% of its longest edge); an
+// unbounded box for a thinner one, which the test then never rejects.
+__global__ void k_tri_boxes(const float* __restrict__ tri_xyz, u32 n, float4* __restrict__ box)
 {
-    int4 ri = a.ref_inst[k];
+    const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* p = tri_xyz + 9 * (size_t) i;
+    const V3 a = mk(p[0], p[1], p[2]), b = mk(p[3], p[4], p[5]), c = mk(p[6], p[7], p[8]);
+    const V3 cr = cross(b - a, c - a);
+    const float l2 = fmaxf(dot(b - a, b - a), fmaxf(dot(c - b, c - b), dot(a - c, a - c)));
+    if (dot(cr, cr) >= 1e-4f * l2 * l2 && l2 > 0.0f) {
+        box[2 * i] = make_float4(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)), 0.0f);
+        box[2 * i + 1] = make_float4(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)), 0.0f);
+    } else {
+        box[2 * i] = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
+        box[2 * i + 1] = make_float4(INFINITY, INFINITY, INFINITY, 0.0f);
+    }
+}
+
+// Whether the concave-edge push of a triangle with box (bmn, bmx) surely does
+// nothing at P: the box lies more than r beyond P along an axis, r being dist
+// plus a margin (1 mm + 1e-5 of P's largest coordinate) far above the rounding
+// of point_tri_dist on a well-shaped triangle. The exact distance is at least
+// the box's separation, the computed one within rounding of it, so it is not
+// below dist and offset_one would return at its first test.
+__device__ __forceinline__ bool fixup_rejects(float4 bmn, float4 bmx, V3 P, float dist)
+{
+    const float scale = fmaxf(fabsf(P.x), fmaxf(fabsf(P.y), fabsf(P.z)));
+    const float r = dist * 1.0001f + 1e-3f + 1e-5f * scale;
+    return P.x + r < bmn.x || P.x - r > bmx.x || P.y + r < bmn.y || P.y - r > bmx.y || P.z + r < bmn.z ||
+           P.z - r > bmx.z;
+}
+
+// One instance of the concave-edge pass for the 32 lanes of a warp (every lane
+// calls it with the same instance; `active` marks the lanes with a sample). A
+// lane's pass is a depth-first walk of the instance's reference-shaped tree
+// (node items, then node + 1's subtree, then the other child's) with the query
+// box P +- dist fixed at the start while P moves. The warp walks the tree once
+// in that order, a node's lanes being those whose box meets the node and all
+// its ancestors -- the lanes whose own walk reaches it -- so each lane handles
+// exactly its own walk's triangles in its own walk's order. Node and triangle
+// loads are broadcasts; the stack (node, lane mask) is warp-uniform, entry i in
+// lane i % 32.
+__device__ __forceinline__ void fixup_instance_warp(const FixupArgs& a, int k, bool active, V3& P, V3 N, float dist)
+{
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int4 ri = a.ref_inst[k];
     if (ri.w == 0) return;
-    V3 qmn = P - splat(dist), qmx = P + splat(dist);
-    int stack[40];
-    int sp = 0;
-    stack[sp++] = 0;
-    while (sp > 0) {
-        int node = stack[--sp];
-        float4 n0 = __ldg(&a.ref_nodes[2 * (ri.x + node)]);
-        float4 n1 = __ldg(&a.ref_nodes[2 * (ri.x + node) + 1]);
-        if (qmn.x > n0.w || qmx.x < n0.x || qmn.y > n1.x || qmx.y < n0.y || qmn.z > n1.y || qmx.z < n0.z) continue;
-        int ch = __float_as_int(n1.z), ido = __float_as_int(n1.w);
-        if (ido != -1) {
-            const int* it = a.ref_items + ri.y + ido;
-            int cnt = it[0];
-            for (int i = 0; i < cnt; ++i) {
-                int id = it[1 + i];
-                const float* p = a.tri_xyz + 9 * (size_t) (ri.z + id);
-                offset_one(a, mk(p[0], p[1], p[2]), mk(p[3], p[4], p[5]), mk(p[6], p[7], p[8]), id, (u32) k, P, N,
-                           dist);
+    const V3 qmn = P - splat(dist), qmx = P + splat(dist);
+    int s0 = 0, s1 = 0, sp = 0;          // pending subtrees
+    unsigned m0 = 0, m1 = 0;             // the lanes that reached their parents
+    int node = 0;
+    unsigned in = __ballot_sync(full, active);
+    for (;;) {
+        bool ov = false;
+        if (in) {
+            const float4 n0 = __ldg(&a.ref_nodes[2 * (ri.x + node)]);
+            const float4 n1 = __ldg(&a.ref_nodes[2 * (ri.x + node) + 1]);
+            ov = ((in >> lane) & 1u) &&
+                 !(qmn.x > n0.w || qmx.x < n0.x || qmn.y > n1.x || qmx.y < n0.y || qmn.z > n1.y || qmx.z < n0.z);
+            const unsigned m = __ballot_sync(full, ov);
+            if (m) {
+                const int ch = __float_as_int(n1.z), ido = __float_as_int(n1.w);
+                if (ido != -1) {
+                    const int* it = a.ref_items + ri.y + ido;
+                    const int cnt = __ldg(it);
+                    for (int i = 0; i < cnt; ++i) {
+                        const int id = __ldg(it + 1 + i);
+                        if (ov && !fixup_rejects(__ldg(&a.tri_box[2 * (size_t) (ri.z + id)]),
+                                                 __ldg(&a.tri_box[2 * (size_t) (ri.z + id) + 1]), P, dist)) {
+                            const float* p = a.tri_xyz + 9 * (size_t) (ri.z + id);
+                            offset_one(a, mk(p[0], p[1], p[2]), mk(p[3], p[4], p[5]), mk(p[6], p[7], p[8]), id,
+                                       (u32) k, P, N, dist);
+                        }
+                    }
+                }
+                if (ch != -1) {
+                    // the lane's own walk pushes ch, then node + 1, and pops node + 1 first
+                    if (sp < 64) {
+                        if (lane == (sp & 31)) {
+                            if (sp < 32) { s0 = ch; m0 = m; } else { s1 = ch; m1 = m; }
+                        }
+                        ++sp;
+                    } else if (lane == 0) {
+                        raise_err(a.err, 1u);
+                    }
+                    node = node + 1;
+                    in = m;
+                    continue;
+                }
             }
         }
-        if (ch != -1) {
-            if (sp + 2 <= 40) { stack[sp++] = ch; stack[sp++] = node + 1; }
-            else raise_err(a.err, 1u);
-        }
+        if (sp == 0) break;
+        --sp;
+        node = __shfl_sync(full, sp < 32 ? s0 : s1, sp & 31);
+        in = __shfl_sync(full, sp < 32 ? m0 : m1, sp & 31);
     }
 }
 
@@ -385,7 +453,7 @@ __global__ void __launch_bounds__(kFixupThreads) k_fixup(FixupArgs a)
         } else if (k >= a.n_inst) {
             break;
         }
-        if (active) fixup_instance(a, k, P, N, dist);
+        fixup_instance_warp(a, k, active, P, N, dist);
         const bool far = fabsf(P.x - P0.x) > M || fabsf(P.y - P0.y) > M || fabsf(P.z - P0.z) > M;
         if (!slow && __any_sync(full, far)) slow = true;
         ++k;
@@ -2683,6 +2751,12 @@ void run_bake(ltr_Scene* S)
         fa.ref_inst = d_ref_inst;
         fa.inst_box = d_fix_box;
         fa.tri_xyz = d_tri_xyz;
+        const u32 n_fix_tris = (u32) (tri_xyz.size() / 9);
+        float4* d_tri_box = A.alloc<float4>(2 * (size_t) std::max<u32>(n_fix_tris, 1));
+        if (n_fix_tris) {
+            k_tri_boxes<<<(n_fix_tris + 255) / 256, 256, 0, st>>>(d_tri_xyz, n_fix_tris, d_tri_box); note_launch();
+        }
+        fa.tri_box = d_tri_box;
         fa.n_inst = n_inst;
         fa.n_probe = n_probe;
         fa.n_samples = n_samples;
