@@ -263,26 +263,27 @@ struct FixupArgs {
 };
 
 // Concave-edge push of TriTree::OffsetSample (lighter_math.cpp:991-1044) for
-// one triangle (instance-local index `local`) of instance `inst`.
-__device__ __forceinline__ void offset_one(const FixupArgs& a, V3 P1, V3 P2, V3 P3, int local, u32 inst, V3& P, V3 N,
-                                           float dist)
+// one triangle, up to its visibility query: whether the push is a candidate,
+// and then the query segment [qo, qe] (qe = the pushed position). The push
+// applies when the query's closest hit among the instance's triangles is at
+// 0.9 or beyond, or is this triangle.
+__device__ __forceinline__ bool offset_candidate(V3 P1, V3 P2, V3 P3, V3 P, V3 N, float dist, V3& qo, V3& qe)
 {
     float nd = point_tri_dist(P, P1, P2, P3);
-    if (!(nd < dist)) return;
+    if (!(nd < dist)) return false;
     V3 TPN = -tri_normal_rev(P1, P2, P3);
     float TPD = dot(TPN, P1);
     float sig = dot(TPN, P) - TPD;
-    if (!(sig <= kSmall)) return;
+    if (!(sig <= kSmall)) return false;
     V3 Pextr = P + normalized(TPN + N) * -sig * 1.41f;
-    if (!point_proj_on_tri(Pextr, P1, P2, P3)) return;
+    if (!point_proj_on_tri(Pextr, P1, P2, P3)) return false;
     float pdot = dot(TPN, N);
-    if (!(fabsf(pdot) < 0.95f)) return;
+    if (!(fabsf(pdot) < 0.95f)) return false;
     V3 proj = normalized(TPN - N * pdot);
     float df = 1.0f - fabsf(pdot);
-    V3 Pnew = P + proj * (-sig / df + kSmall);
-    int hit_local = -1;
-    float r = bvh_closest_inst(a.bvh, P + (N + proj) * kSmall, Pnew, inst, a.err, &hit_local);
-    if (r >= 0.9f || hit_local == local) P = Pnew;
+    qe = P + proj * (-sig / df + kSmall);
+    qo = P + (N + proj) * kSmall;
+    return true;
 }
 
 // Boxes of the concave-edge pass's triangles, for its exact rejection test: the
@@ -310,7 +311,7 @@ __global__ void k_tri_boxes(const float* __restrict__ tri_xyz, u32 n, float4* __
 // plus a margin (1 mm + 1e-5 of P's largest coordinate) far above the rounding
 // of point_tri_dist on a well-shaped triangle. The exact distance is at least
 // the box's separation, the computed one within rounding of it, so it is not
-// below dist and offset_one would return at its first test.
+// below dist and offset_candidate would return at its first test.
 __device__ __forceinline__ bool fixup_rejects(float4 bmn, float4 bmx, V3 P, float dist)
 {
     const float scale = fmaxf(fabsf(P.x), fmaxf(fabsf(P.y), fabsf(P.z)));
@@ -355,11 +356,19 @@ __device__ __forceinline__ void fixup_instance_warp(const FixupArgs& a, int k, b
                     const int cnt = __ldg(it);
                     for (int i = 0; i < cnt; ++i) {
                         const int id = __ldg(it + 1 + i);
+                        bool want = false;
+                        V3 qo = mk(0, 0, 0), qe = mk(0, 0, 0);
                         if (ov && !fixup_rejects(__ldg(&a.tri_box[2 * (size_t) (ri.z + id)]),
                                                  __ldg(&a.tri_box[2 * (size_t) (ri.z + id) + 1]), P, dist)) {
                             const float* p = a.tri_xyz + 9 * (size_t) (ri.z + id);
-                            offset_one(a, mk(p[0], p[1], p[2]), mk(p[3], p[4], p[5]), mk(p[6], p[7], p[8]), id,
-                                       (u32) k, P, N, dist);
+                            want = offset_candidate(mk(p[0], p[1], p[2]), mk(p[3], p[4], p[5]), mk(p[6], p[7], p[8]),
+                                                    P, N, dist, qo, qe);
+                        }
+                        // the candidates' visibility queries, one walk shared by the warp
+                        if (__any_sync(full, want)) {
+                            int hit_local = -1;
+                            const float r = warp_closest_inst(a.bvh, qo, qe, (u32) k, want, a.err, &hit_local);
+                            if (want && (r >= 0.9f || hit_local == id)) P = qe;
                         }
                     }
                 }

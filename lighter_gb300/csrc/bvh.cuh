@@ -429,29 +429,6 @@ __device__ __forceinline__ float bvh_closest(const BvhView& b, V3 o, V3 e, ErrFl
     return bvh_closest_s(b, o, e, err, tri_out, st);
 }
 
-// Closest hit restricted to one instance's triangles, occluder or not
-// (the per-instance tree of TriTree::OffsetSample, lighter_math.cpp:1024);
-// *local_out = the triangle's index within its instance.
-__device__ __forceinline__ float bvh_closest_inst(const BvhView& b, V3 o, V3 e, u32 inst, ErrFlag err, int* local_out)
-{
-    float best = kNoHit;
-    int bl = -1;
-    TStack<0> st;
-    walk_segment(b, o, e, err, st, [&](int t, float& tlimit) {
-        u32 meta;
-        float r = seg_leaf(b, o, e, t, meta);
-        if ((meta & kInstMask) != inst) return true;
-        u32 local = __float_as_uint(__ldg(&b.tris[3 * (size_t) t + 1]).w);
-        if (r < best || (r == best && r < kNoHit && (int) local < bl)) {
-            best = r; bl = (int) local;
-            tlimit = fminf(1.0f, r);
-        }
-        return true;
-    });
-    if (local_out) *local_out = bl;
-    return best;
-}
-
 // Distance from p to the nearest occluder triangle, capped at d0
 // (ltr_Scene::Distance + TriTree::GetDistance, lighter.cpp:150-188,
 // lighter_math.cpp:954-989). The reference shrinks a query cube; a sphere
@@ -676,6 +653,61 @@ __device__ __forceinline__ float warp_closest(const BvhView& b, V3 o, V3 e, bool
         if (sp == 0) break;
         cur = wstack_pop(s0, s1, sp);
     }
+    return best;
+}
+
+// Closest hit restricted to one instance's triangles, occluder or not (the
+// per-instance tree query of TriTree::OffsetSample, lighter_math.cpp:1024),
+// for the active lanes' segments: the smallest hit fraction, ties to the lower
+// instance-local index (a rule that does not depend on the visiting order);
+// *local_out gets the lane's triangle within its instance (or -1).
+__device__ __forceinline__ float warp_closest_inst(const BvhView& b, V3 o, V3 e, u32 inst, bool active, ErrFlag err,
+                                                   int* local_out)
+{
+    float best = kNoHit;
+    int bl = -1;
+    if (b.n_tris <= 0 || !__any_sync(0xffffffffu, active)) {
+        *local_out = bl;
+        return best;
+    }
+    const V3 d = e - o;
+    const V3 inv = inv_dir(d);
+    const V3 oinv = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+    float tlimit = 1.0f;
+    int s0 = 0, s1 = 0, sp = 0;
+    int cur = b.root;
+    for (;;) {
+        if (cur >= 0) {
+            const NodeBoxes nb = load_node(b, cur);
+            float tl, tr;
+            const bool hl = active && slab(nb.lmin, nb.lmax, oinv, inv, tlimit, tl);
+            const bool hr = active && slab(nb.rmin, nb.rmax, oinv, inv, tlimit, tr);
+            const unsigned ml = __ballot_sync(0xffffffffu, hl), mr = __ballot_sync(0xffffffffu, hr);
+            if (ml && mr) {
+                const bool lfirst = warp_left_first(hl, hr, tl <= tr);
+                wstack_push(s0, s1, sp, lfirst ? nb.r : nb.l, err);
+                cur = lfirst ? nb.l : nb.r;
+                continue;
+            }
+            if (ml) { cur = nb.l; continue; }
+            if (mr) { cur = nb.r; continue; }
+        } else if (active) {
+            const int t = ~cur;
+            u32 meta;
+            const float r = seg_leaf(b, o, e, t, meta);
+            if ((meta & kInstMask) == inst) {
+                const int local = (int) __float_as_uint(__ldg(&b.tris[3 * (size_t) t + 1]).w);
+                if (r < best || (r == best && r < kNoHit && local < bl)) {
+                    best = r;
+                    bl = local;
+                    tlimit = fminf(1.0f, r);
+                }
+            }
+        }
+        if (sp == 0) break;
+        cur = wstack_pop(s0, s1, sp);
+    }
+    *local_out = bl;
     return best;
 }
 
