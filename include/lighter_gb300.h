@@ -224,6 +224,14 @@ LTRAPI const char* ltrg_GatherLastError(ltrg_Gather* g);
  * fails with the error word in ltrg_GatherLastError, and later solves run
  * normally. No GPU fault or hang is involved. wait_us in 1..2000000. */
 LTRAPI LTRBOOL ltrdbg_GatherStallNextSolve(ltrg_Gather* g, u32 wait_us);
+/* Test hook for the bounded waits of the bake's radiosity bounce: in the next
+ * bounce over an unrefined F (any bake of this process), the copy producer
+ * issues nothing and every mbarrier wait gives up after about wait_us
+ * microseconds (instead of about 2 s). The waits expire, the kernel records
+ * bit 1 in the radiosity stage's error word and returns; that bake fails with
+ * the error word in ltrg_LastError, and later bakes run normally. No GPU
+ * fault or hang is involved. wait_us in 1..2000000. */
+LTRAPI LTRBOOL ltrdbg_RadiosityStallNextBounce(u32 wait_us);
 /* How ltrg_GatherSolve moves its host buffers (test and measurement hook).
  * mode 0: by device (the default): where kernels may address pageable host
  * memory (cudaDevAttrPageableMemoryAccess, e.g. Grace systems), copy kernels

@@ -4,10 +4,12 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
 
+#include "../../include/lighter_gb300.h"
 #include "async.cuh"
 #include "radiosity.cuh"
 
@@ -408,6 +410,10 @@ __global__ void __launch_bounds__(256) k_rad_refined(u32 n, size_t ld, const T* 
 }
 
 constexpr u32 kErrWait = 2u;   // radiosity error word: a bounded wait for staged F expired
+
+// ltrdbg_RadiosityStallNextBounce: wait limit (us) of the next unrefined bounce
+// whose copy producer issues nothing; 0 = none pending.
+std::atomic<uint32_t> g_stall_next_bounce{0};
 constexpr unsigned long long kStreamWaitCycles = 4000000000ull;   // about 2 s at 2 GHz
 
 // Launch shape of k_rad_stream: warps per CTA, ring stages per warp, and
@@ -435,7 +441,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_rad_stream(u32 n, size_t ld, co
                                                             const float4* __restrict__ da,
                                                             float4* __restrict__ total, float4* __restrict__ out,
                                                             float4* __restrict__ Xn, u32* err,
-                                                            unsigned long long wait_cycles)
+                                                            unsigned long long wait_cycles, u32 issue)
 {
     constexpr int V = 16 / (int) sizeof(T);       // entries per 16-byte vector
     constexpr u32 kPart = kVec * 512u;            // bytes of one row in one stage
@@ -460,8 +466,9 @@ __global__ void __launch_bounds__(kWarps * 32) k_rad_stream(u32 n, size_t ld, co
         policy = l2_evict_first_policy();
     }
     __syncwarp();
-    // lane 0: chunk k of every row into stage k % kStages
-    auto issue = [&](u32 k) {
+    // lane 0: chunk k of every row into stage k % kStages (`issue` 0: never, the
+    // test of the bounded waits)
+    auto fill = [&](u32 k) {
         const u32 q = k % kStages;
         const u32 v0 = k * kPer;
         const u32 bytes = min(kPer, nv - v0) * 16u;
@@ -470,8 +477,8 @@ __global__ void __launch_bounds__(kWarps * 32) k_rad_stream(u32 n, size_t ld, co
         for (int r = 0; r < kRadRows; ++r)
             bulk_g2s(ring + (size_t) (q * kRadRows + r) * kPart, rows[r] + (size_t) v0 * V, bytes, &bar[q], policy);
     };
-    if (lane == 0)
-        for (u32 k = 0; k < nch && k < (u32) kStages; ++k) issue(k);
+    if (lane == 0 && issue)
+        for (u32 k = 0; k < nch && k < (u32) kStages; ++k) fill(k);
     float acc[kRadRows][3];
 #pragma unroll
     for (int r = 0; r < kRadRows; ++r) acc[r][0] = acc[r][1] = acc[r][2] = 0.0f;
@@ -496,12 +503,12 @@ __global__ void __launch_bounds__(kWarps * 32) k_rad_stream(u32 n, size_t ld, co
             }
         }
         __syncwarp();   // every lane has read stage q before it is refilled
-        if (lane == 0 && k + kStages < nch) issue(k + kStages);
+        if (lane == 0 && issue && k + kStages < nch) fill(k + kStages);
     }
     if (!ok) {
         // a wait expired (error bit set): wait, bounded again, for the copies still
         // issued into this warp's ring before the CTA's shared memory is released
-        if (lane == 0)
+        if (lane == 0 && issue)
             for (u32 j = k; j < nch && j < k + kStages; ++j)
                 if (!mbar_wait(&bar[j % kStages], (j / kStages) & 1u, err, kErrWait, wait_cycles)) break;
         return;
@@ -666,8 +673,10 @@ RadResult solve_t(const RadDevInputs& in, const RadSettings& rs, const BvhView& 
             const size_t sm = stream_smem_bytes(kStreamWarps, kStreamStages, kStreamVec);
             RCK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm));
             const unsigned sgrid = (unsigned) (((size_t) n + kRadRows * kStreamWarps - 1) / (kRadRows * kStreamWarps));
+            const uint32_t stall_us = g_stall_next_bounce.exchange(0);
+            const unsigned long long wait = stall_us ? (unsigned long long) stall_us * 2000ull : kStreamWaitCycles;
             kern<<<sgrid, kStreamWarps * 32, sm, st>>>(n, ld, F, up, Xb, in.diff_area, total, out, Xnext, err.word,
-                                                       kStreamWaitCycles);
+                                                       wait, stall_us ? 0u : 1u);
         }
         note_launch();
         RCK(cudaGetLastError());
@@ -724,3 +733,10 @@ RadResult radiosity_solve(const RadInputs& in, const RadSettings& rs, const BvhV
 }
 
 }  // namespace lg
+
+extern "C" LTRAPI LTRBOOL ltrdbg_RadiosityStallNextBounce(u32 wait_us)
+{
+    if (wait_us == 0 || wait_us > 2000000u) return 0;
+    lg::g_stall_next_bounce.store(wait_us);
+    return 1;
+}

@@ -164,6 +164,7 @@ EXT_API.update({
     "ltrdbg_GatherStallNextSolve": (C.c_int, [C.c_void_p, u32]),
     "ltrdbg_GatherHostPath": (C.c_int, [C.c_void_p, C.c_int]),
     "ltrdbg_GatherHostPathUsed": (C.c_int, [C.c_void_p]),
+    "ltrdbg_RadiosityStallNextBounce": (C.c_int, [u32]),
     "ltrg_GatherSolve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, u32, C.c_int, C.c_int, C.c_int, C.c_void_p,
                                    C.POINTER(GatherStats)]),
     "ltrg_GatherSolveDevice": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, u32, C.c_int, C.c_int, C.c_int,

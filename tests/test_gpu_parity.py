@@ -189,6 +189,22 @@ def test_patch_radiosity_runs_and_adds_light(gpu):
     assert gain > 0
 
 
+def test_bounce_wait_expiry_fails_the_bake_and_the_next_bake_matches(gpu):
+    """The bounce kernel's bounded waits: a bounce whose copy producer issues nothing
+    gives up after 20 ms (test limit), the radiosity error word (bit 1) ends that bake
+    with an error, and the next bake equals an untouched one bit for bit."""
+    d = scenes.cornell(2, lm=32, bounces=2, ao=False)
+    opts = {"radiosity_patches": 256, "radiosity_links": 1}
+    ref = bake(gpu, d, gpu_options=opts)
+    assert gpu.ltrdbg_RadiosityStallNextBounce(20000)
+    with pytest.raises(RuntimeError, match="error word 0x00000002"):
+        bake(gpu, d, gpu_options=opts)
+    again = bake(gpu, d, gpu_options=opts)
+    for a, b in zip(ref.lightmaps, again.lightmaps):
+        np.testing.assert_array_equal(a[3], b[3])
+    assert not gpu.ltrdbg_RadiosityStallNextBounce(0)
+
+
 @pytest.mark.parametrize("precision,tol", [(1, 1e-3), (2, 4e-3)])
 def test_half_precision_form_factors_and_refinement(gpu, precision, tol):
     # 16-bit F: with refine_steps = bounces every bounce recomputes its factors in FP32 (F is
