@@ -464,25 +464,51 @@ void bvh_build(const BvhBuildInput& in, BvhStorage& out, void* stream)
             const int init[2] = {n, n_int};
             BVH_CHECK(cudaMemcpyAsync(state, init, sizeof(init), cudaMemcpyHostToDevice, st));
         }
-        int count = n, base = n_int;   // as last read back; count bounds the launches
+        int count = n, base = n_int;   // as last read back
         std::string fail;
+        // Clustering steps run in blocks of kItersPerRead between reads of the
+        // cluster count. A block is launched as one CUDA graph, captured once per
+        // build with launch bounds for all n clusters: the kernels take the live
+        // count from `state` (threads past it exit or write zero flags), so the
+        // same graph serves every block; the even number of steps per block
+        // returns the cluster buffers to their roles at its start. One graph
+        // launch replaces 48 small launches (with the scan's two) and their gaps.
         constexpr int kItersPerRead = 8;
-        for (int it = 0; count > 1;) {
-            if (it >= 4 * n + 64) { fail = "bvh: clustering made no progress"; break; }
-            const int ub = count;
-            for (int k = 0; k < kItersPerRead; ++k, ++it) {
-                k_ploc_nn<<<(ub + kPlocB - 1) / kPlocB, kPlocB, 0, st>>>(state, cbox, nn); note_launch();
-                k_ploc_flags<<<(ub + 1 + B - 1) / B, B, 0, st>>>(state, ub, nn, flags); note_launch();
-                BVH_CHECK(cudaGetLastError());
+        static_assert(kItersPerRead % 2 == 0, "a block must end with the cluster buffers in their starting roles");
+        cudaGraphExec_t block = nullptr;
+        struct BlockGuard {
+            cudaGraphExec_t& g;
+            ~BlockGuard() { if (g) cudaGraphExecDestroy(g); }
+        } block_guard{block};
+        {
+            const int ub = n;
+            BVH_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            cudaError_t ce = cudaSuccess;
+            for (int k = 0; k < kItersPerRead && ce == cudaSuccess; ++k) {
+                k_ploc_nn<<<(ub + kPlocB - 1) / kPlocB, kPlocB, 0, st>>>(state, cbox, nn);
+                k_ploc_flags<<<(ub + 1 + B - 1) / B, B, 0, st>>>(state, ub, nn, flags);
                 size_t tb2 = tb;
-                BVH_CHECK(cub::DeviceScan::ExclusiveSum(ptmp, tb2, flags, scan, ub + 1, st));
+                if (ce == cudaSuccess) ce = cudaGetLastError();
+                if (ce == cudaSuccess) ce = cub::DeviceScan::ExclusiveSum(ptmp, tb2, flags, scan, ub + 1, st);
                 k_ploc_merge<<<(ub + B - 1) / B, B, 0, st>>>(state, nn, flags, scan, cl, cbox, ncl, ncbox, left, right,
-                                                             parent_int, int_box); note_launch();
-                k_ploc_state<<<1, 1, 0, st>>>(state, scan, ub); note_launch();
-                BVH_CHECK(cudaGetLastError());
+                                                             parent_int, int_box);
+                k_ploc_state<<<1, 1, 0, st>>>(state, scan, ub);
+                if (ce == cudaSuccess) ce = cudaGetLastError();
                 std::swap(cl, ncl);
                 std::swap(cbox, ncbox);
             }
+            cudaGraph_t graph = nullptr;
+            const cudaError_t ee = cudaStreamEndCapture(st, &graph);
+            if (ce == cudaSuccess) ce = ee;
+            if (ce == cudaSuccess) ce = cudaGraphInstantiate(&block, graph, 0);
+            if (graph) cudaGraphDestroy(graph);
+            BVH_CHECK(ce);
+        }
+        for (int it = 0; count > 1;) {
+            if (it >= 4 * n + 64) { fail = "bvh: clustering made no progress"; break; }
+            BVH_CHECK(cudaGraphLaunch(block, st));
+            for (int k = 0; k < 4 * kItersPerRead; ++k) note_launch();   // the graph's own kernels
+            it += kItersPerRead;
             int hs[2] = {0, 0};
             BVH_CHECK(cudaMemcpyAsync(hs, state, sizeof(hs), cudaMemcpyDeviceToHost, st));
             note_d2h(sizeof(hs));
