@@ -3,6 +3,8 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <exception>
+#include <thread>
 
 namespace lg {
 namespace {
@@ -12,10 +14,28 @@ struct Box { V3 mn, mx; };
 inline float volume(const Box& b) { return (b.mx.x - b.mn.x) * (b.mx.y - b.mn.y) * (b.mx.z - b.mn.z); }
 inline V3 centre(const Box& b) { return (b.mn + b.mx) * 0.5f; }
 
+// Subtrees of at least kParItems items above depth kParDepth are built on a
+// second thread into a separate tree and spliced in afterwards (node and item
+// offsets shifted), which gives the sequential build's layout exactly.
+constexpr size_t kParItems = 1024;
+constexpr int kParDepth = 4;
+
 struct Builder {
     const Box* boxes;
     RefTree* t;
-    std::vector<float> key;   // per item: centre along the current split axis
+
+    // Appends `sub` (built with its root at index 0 and its own item list) as the
+    // subtree whose root gets the next node index.
+    void splice(const RefTree& sub)
+    {
+        const int32_t nb = (int32_t) t->nodes.size(), ib = (int32_t) t->items.size();
+        for (RefNode nd : sub.nodes) {
+            if (nd.ch != -1) nd.ch += nb;
+            if (nd.ido != -1) nd.ido += ib;
+            t->nodes.push_back(nd);
+        }
+        t->items.insert(t->items.end(), sub.items.begin(), sub.items.end());
+    }
 
     void emit(int32_t node, const int32_t* ids, size_t n)
     {
@@ -54,11 +74,45 @@ struct Builder {
                 }
                 if (!self.empty()) emit(node, self.data(), self.size());
                 // the keys are the values the comparison dot(axis, centre(a)) < dot(axis,
-                // centre(b)) would compute, so std::sort sees the same comparisons
-                for (int32_t id : split) key[id] = dot(axis, centre(boxes[id]));
-                const float* kv = key.data();
-                std::sort(split.begin(), split.end(), [kv](int32_t a, int32_t b) { return kv[a] < kv[b]; });
+                // centre(b)) would compute, so std::sort sees the same comparisons;
+                // sorting (key, id) pairs makes the same comparisons in the same
+                // sequence, so it gives the same order, without the indirection
+                std::vector<std::pair<float, int32_t>> kp(split.size());
+                for (size_t i = 0; i < split.size(); ++i) kp[i] = {dot(axis, centre(boxes[split[i]])), split[i]};
+                std::sort(kp.begin(), kp.end(), [](const std::pair<float, int32_t>& a, const std::pair<float, int32_t>& b) {
+                    return a.first < b.first;
+                });
+                for (size_t i = 0; i < split.size(); ++i) split[i] = kp[i].second;
                 size_t mid = split.size() / 2;
+                if (depth < kParDepth && split.size() >= kParItems) {
+                    // both halves at once: the right one on a second thread
+                    RefTree right;
+                    right.nodes.assign(1, RefNode());
+                    Builder rb{boxes, &right};
+                    std::exception_ptr rerr;
+                    std::thread th([&]() {
+                        try {
+                            rb.make(0, split.data() + mid, split.size() - mid, depth + 1);
+                        } catch (...) {
+                            rerr = std::current_exception();
+                        }
+                    });
+                    RefTree left;
+                    left.nodes.assign(1, RefNode());
+                    Builder lb{boxes, &left};
+                    try {
+                        lb.make(0, split.data(), mid, depth + 1);
+                    } catch (...) {
+                        th.join();
+                        throw;
+                    }
+                    th.join();
+                    if (rerr) std::rethrow_exception(rerr);
+                    splice(left);
+                    t->nodes[node].ch = (int32_t) t->nodes.size();
+                    splice(right);
+                    return;
+                }
                 t->nodes.push_back(RefNode());
                 make((int32_t) t->nodes.size() - 1, split.data(), mid, depth + 1);
                 t->nodes[node].ch = (int32_t) t->nodes.size();
@@ -93,7 +147,7 @@ void build_ref_tree(const float* xyz, size_t n, RefTree& out)
         const Box& bb = boxes[i];
         if (bb.mn.x <= bb.mx.x && bb.mn.y <= bb.mx.y && bb.mn.z <= bb.mx.z) ids.push_back((int32_t) i);
     }
-    Builder bld{boxes.data(), &out, std::vector<float>(n)};
+    Builder bld{boxes.data(), &out};
     bld.make(0, ids.data(), ids.size(), 0);
 }
 
