@@ -2412,6 +2412,81 @@ void run_bake(ltr_Scene* S)
         ~JoinReftree() { if (th.joinable()) th.join(); }
     } join_reftree{reftree_thread};
 
+    // ---- BVH: built on its own stream and host thread as soon as the triangle
+    // soup exists, while this thread prepares the raster records (the build
+    // reads its cluster count back now and then, which would hold this thread);
+    // the sample stage waits for it.
+    cudaEvent_t e_dev0 = clock.mark();   // the bake's first device work
+    float* d_tri_xyz = A.upload(tri_xyz);
+    u32* d_tri_meta = A.upload(tri_meta);
+    u32* d_tri_local = A.upload(tri_local);
+    cudaEvent_t e_tri = clock.mark();
+    BvhStorage bvh;
+    BvhBuildInput bin;
+    bin.tri_xyz = d_tri_xyz;
+    bin.tri_meta = d_tri_meta;
+    bin.tri_local = d_tri_local;
+    bin.builder = (int) S->opt.bvh_builder;
+    struct BvhSide {   // its stream, start/end events, and the BVH's storage, released last
+        cudaStream_t st_main = nullptr, st = nullptr;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        BvhStorage* bvh = nullptr;
+        ~BvhSide()
+        {
+            if (st) cudaStreamSynchronize(st);
+            if (st_main) cudaStreamSynchronize(st_main);
+            if (bvh) bvh_free(*bvh, st_main);
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+            if (st) cudaStreamDestroy(st);
+        }
+    } bside;
+    bside.st_main = st;
+    bside.bvh = &bvh;
+    CK(cudaStreamCreateWithFlags(&bside.st, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&bside.e0));
+    CK(cudaEventCreate(&bside.e1));
+    std::exception_ptr bvh_error;
+    HostCounters bvh_counts;
+    std::thread bvh_thread([&]() {
+        try {
+            CK(cudaSetDevice(S->opt.device));
+            cudaStream_t bs = bside.st;
+            CK(cudaStreamWaitEvent(bs, e_tri, 0));
+            CK(cudaEventRecord(bside.e0, bs));
+            std::vector<u32> ref_tri;
+            std::vector<float> ref_box;
+            float rmin[3], rmax[3];
+            build_refs(tri_xyz, ref_tri, ref_box, rmin, rmax);
+            u32* d_ref_tri = nullptr;
+            float* d_ref_box = nullptr;
+            CK(cudaMallocAsync(&d_ref_tri, std::max<size_t>(ref_tri.size(), 1) * sizeof(u32), bs));
+            CK(cudaMallocAsync(&d_ref_box, std::max<size_t>(ref_box.size(), 1) * sizeof(float), bs));
+            struct FreeRefs {
+                cudaStream_t s; void* p[2];
+                ~FreeRefs() { for (void* q : p) cudaFreeAsync(q, s); }
+            } free_refs{bs, {d_ref_tri, d_ref_box}};
+            if (!ref_tri.empty())
+                CK(cudaMemcpyAsync(d_ref_tri, ref_tri.data(), ref_tri.size() * sizeof(u32), cudaMemcpyHostToDevice, bs));
+            if (!ref_box.empty())
+                CK(cudaMemcpyAsync(d_ref_box, ref_box.data(), ref_box.size() * sizeof(float), cudaMemcpyHostToDevice, bs));
+            note_h2d(ref_tri.size() * sizeof(u32) + ref_box.size() * sizeof(float));
+            bin.ref_tri = d_ref_tri;
+            bin.ref_box = d_ref_box;
+            bin.n = (int) ref_tri.size();
+            for (int c = 0; c < 3; ++c) { bin.scene_min[c] = bin.n ? rmin[c] : 0; bin.scene_max[c] = bin.n ? rmax[c] : 0; }
+            bvh_build(bin, bvh, bs);
+            CK(cudaEventRecord(bside.e1, bs));
+        } catch (...) {
+            bvh_error = std::current_exception();
+        }
+        bvh_counts = host_counters();   // this thread's launches and copies
+    });
+    struct JoinBvh {   // joined on every way out (the thread uses this frame's variables)
+        std::thread& th;
+        ~JoinBvh() { if (th.joinable()) th.join(); }
+    } join_bvh{bvh_thread};
+
     const int n_lights = (int) S->lights.size();
     std::vector<unsigned char> lit((size_t) n_lights * n_inst, 0);
     std::vector<DLight> dl(n_lights);
@@ -2546,9 +2621,6 @@ void run_bake(ltr_Scene* S)
     // ---- upload
     cudaEvent_t e_up0 = clock.mark();
     const u32 n_probe = (u32) S->samples.size();
-    float* d_tri_xyz = A.upload(tri_xyz);
-    u32* d_tri_meta = A.upload(tri_meta);
-    u32* d_tri_local = A.upload(tri_local);
     unsigned char* d_lit = A.upload(lit);
     DLight* d_lights = A.upload(dl);
     float* d_rt = A.upload(rt);
@@ -2567,24 +2639,14 @@ void run_bake(ltr_Scene* S)
     check_abort(S);
 
     TRACE("upload issued");
-    // ---- BVH
-    BvhStorage bvh;
-    BvhBuildInput bin;
-    bin.tri_xyz = d_tri_xyz;
-    bin.tri_meta = d_tri_meta;
-    bin.tri_local = d_tri_local;
-    std::vector<u32> ref_tri;
-    std::vector<float> ref_box;
-    float rmin[3], rmax[3];
-    build_refs(tri_xyz, ref_tri, ref_box, rmin, rmax);
-    bin.ref_tri = A.upload(ref_tri);
-    bin.ref_box = A.upload(ref_box);
-    bin.n = (int) ref_tri.size();
-    bin.builder = (int) S->opt.bvh_builder;
-    for (int c = 0; c < 3; ++c) { bin.scene_min[c] = bin.n ? rmin[c] : 0; bin.scene_max[c] = bin.n ? rmax[c] : 0; }
+    // ---- BVH (joined)
+    bvh_thread.join();
+    if (bvh_error) std::rethrow_exception(bvh_error);
+    host_counters().launches += bvh_counts.launches;
+    host_counters().h2d += bvh_counts.h2d;
+    host_counters().d2h += bvh_counts.d2h;
+    CK(cudaStreamWaitEvent(st, bside.e1, 0));
     S->stats.reserved[0] = (uint64_t) bin.n;   // leaf references
-    bvh_build(bin, bvh, st);
-    struct BvhGuard { BvhStorage* b; cudaStream_t s; ~BvhGuard() { bvh_free(*b, s); } } bvh_guard{&bvh, st};
     BvhView bv = bvh.view();
     bv.watertight = S->opt.intersect_mode == LTRG_ISECT_WATERTIGHT ? 1 : 0;
     cudaEvent_t e_bvh = clock.mark();
@@ -3355,7 +3417,7 @@ void run_bake(ltr_Scene* S)
 
     TRACE("outputs assembled");
     S->stats.ms_upload = StageClock::ms(e_up0, e_up1);
-    S->stats.ms_bvh = StageClock::ms(e_up1, e_bvh);
+    S->stats.ms_bvh = StageClock::ms(bside.e0, bside.e1);
     S->stats.ms_samples = StageClock::ms(e_bvh, e_samples);
     S->stats.ms_direct = StageClock::ms(e_samples, e_direct);
     S->stats.ms_ao = StageClock::ms(e_ao0, e_ao1);
@@ -3372,7 +3434,7 @@ void run_bake(ltr_Scene* S)
     S->stats.kernel_launches = host_counters().launches;
     S->stats.bytes_h2d = host_counters().h2d;
     S->stats.bytes_d2h = host_counters().d2h;
-    S->stats.ms_device = StageClock::ms(e_up1, e_fin);
+    S->stats.ms_device = StageClock::ms(e_dev0, e_fin);
     (void) e_rad_links;
     (void) e_rad_bounce;
 }
