@@ -2443,16 +2443,16 @@ void run_bake(ltr_Scene* S)
     } bside;
     bside.st_main = st;
     bside.bvh = &bvh;
-    CK(cudaStreamCreateWithFlags(&bside.st, cudaStreamNonBlocking));
+    if (!batch) CK(cudaStreamCreateWithFlags(&bside.st, cudaStreamNonBlocking));
     CK(cudaEventCreate(&bside.e0));
     CK(cudaEventCreate(&bside.e1));
     std::exception_ptr bvh_error;
     HostCounters bvh_counts;
-    std::thread bvh_thread([&]() {
+    auto bvh_job = [&]() {
         try {
             CK(cudaSetDevice(S->opt.device));
-            cudaStream_t bs = bside.st;
-            CK(cudaStreamWaitEvent(bs, e_tri, 0));
+            cudaStream_t bs = bside.st ? bside.st : st;
+            if (bs != st) CK(cudaStreamWaitEvent(bs, e_tri, 0));
             CK(cudaEventRecord(bside.e0, bs));
             std::vector<u32> ref_tri;
             std::vector<float> ref_box;
@@ -2480,8 +2480,21 @@ void run_bake(ltr_Scene* S)
         } catch (...) {
             bvh_error = std::current_exception();
         }
-        bvh_counts = host_counters();   // this thread's launches and copies
-    });
+    };
+    // A scene of a batch builds on its own thread and stream: the other scenes'
+    // work fills the GPU and the host meanwhile, an extra waiting thread per scene
+    // (the build's read-backs) would take host cores from the scenes still
+    // preparing, and with a second stream per scene the 256-scene batch measured
+    // 5.0 s instead of 0.8 s.
+    std::thread bvh_thread;
+    if (batch) {
+        bvh_job();
+    } else {
+        bvh_thread = std::thread([&]() {
+            bvh_job();
+            bvh_counts = host_counters();   // this thread's launches and copies
+        });
+    }
     struct JoinBvh {   // joined on every way out (the thread uses this frame's variables)
         std::thread& th;
         ~JoinBvh() { if (th.joinable()) th.join(); }
@@ -2640,12 +2653,12 @@ void run_bake(ltr_Scene* S)
 
     TRACE("upload issued");
     // ---- BVH (joined)
-    bvh_thread.join();
+    if (bvh_thread.joinable()) bvh_thread.join();
     if (bvh_error) std::rethrow_exception(bvh_error);
     host_counters().launches += bvh_counts.launches;
     host_counters().h2d += bvh_counts.h2d;
     host_counters().d2h += bvh_counts.d2h;
-    CK(cudaStreamWaitEvent(st, bside.e1, 0));
+    if (bside.st) CK(cudaStreamWaitEvent(st, bside.e1, 0));
     S->stats.reserved[0] = (uint64_t) bin.n;   // leaf references
     BvhView bv = bvh.view();
     bv.watertight = S->opt.intersect_mode == LTRG_ISECT_WATERTIGHT ? 1 : 0;
