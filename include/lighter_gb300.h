@@ -67,7 +67,10 @@ typedef struct ltrg_Options {
                                  only the trace times do. Default LTRG_BVH_PLOC */
     uint32_t shadow_mode;     /* LTRG_SHADOW_*, default LTRG_SHADOW_SPHERE */
     uint32_t intersect_mode;  /* LTRG_ISECT_*, default LTRG_ISECT_REFERENCE */
-    uint32_t reserved[7];
+    uint32_t encode_rgbe;     /* 1: the bake also encodes every lightmap as Radiance RGBE (4 bytes
+                                 per texel, Ward's shared exponent) on the GPU after the finalize
+                                 stage; read with ltrg_GetWorkOutputRGBE. Default 0 */
+    uint32_t reserved[6];
 } ltrg_Options;
 
 /* Per-stage device times (CUDA events on the bake stream) and work counters
@@ -110,6 +113,11 @@ typedef struct ltrg_Stats {
 /* Options are read at ltr_Start; returns 0 on an invalid value. */
 LTRAPI void ltrg_GetOptions(ltr_Scene* scene, ltrg_Options* out);
 LTRAPI LTRBOOL ltrg_SetOptions(ltr_Scene* scene, const ltrg_Options* opt);
+/* The RGBE encoding of work output `which` (ltrg_Options::encode_rgbe): w x h
+ * pixels of 4 bytes (R, G, B mantissas, exponent + 128), rows as the float
+ * image's; scene-owned, valid until the next bake or ltr_DestroyScene. Returns
+ * 0 when the last bake did not encode. */
+LTRAPI LTRBOOL ltrg_GetWorkOutputRGBE(ltr_Scene* scene, u32 which, const unsigned char** rgbe);
 LTRAPI LTRBOOL ltrg_GetStats(ltr_Scene* scene, ltrg_Stats* out);
 /* Text of the error that ended the last bake, or NULL. */
 LTRAPI const char* ltrg_LastError(ltr_Scene* scene);

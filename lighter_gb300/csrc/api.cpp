@@ -31,6 +31,7 @@ ltr_Scene::ltr_Scene()
 void ltr_Scene::clear_outputs()
 {
     outputs.clear();   // the buffers live in `pinned`, which the next bake reuses
+    outputs_rgbe.clear();
     dump.clear();
     rad_dump = lg::RadDump();
 }
@@ -377,9 +378,16 @@ LTRAPI LTRBOOL ltrg_SetOptions(ltr_Scene* scene, const ltrg_Options* o)
 {
     if (o->device < 0 || o->radiosity_links < 0 || o->radiosity_links > 1 || o->radiosity_precision < 0 ||
         o->radiosity_precision > 2 || o->refine_steps < 0 || o->refine_steps > 16 || o->bvh_builder > 1 ||
-        o->shadow_mode > 1 || o->intersect_mode > 1)
+        o->shadow_mode > 1 || o->intersect_mode > 1 || o->encode_rgbe > 1)
         return 0;
     scene->opt = *o;
+    return 1;
+}
+
+LTRAPI LTRBOOL ltrg_GetWorkOutputRGBE(ltr_Scene* scene, u32 which, const unsigned char** rgbe)
+{
+    if (!scene || !rgbe || scene->running.load() || which >= scene->outputs_rgbe.size()) return 0;
+    *rgbe = scene->outputs_rgbe[which];
     return 1;
 }
 

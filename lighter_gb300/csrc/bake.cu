@@ -1597,6 +1597,32 @@ __global__ void k_conv_t(unsigned long long ntex, int n_inst, const unsigned lon
 }
 
 // Downsample2X (lighter_math.cpp:400-424) into a separate per-instance layout.
+// Radiance RGBE of float RGB texels (Ward's shared-exponent format, "Real Pixels",
+// Graphics Gems II): v = the largest channel (negatives clamp to 0); for
+// v > 1e-32, v = m 2^e with m in [0.5, 1), each channel becomes
+// min(255, floor(c m 256 / v)) and the fourth byte e + 128; else all four are 0.
+// Computed in double, as the host encoder does, so both give the same bytes.
+__global__ void k_encode_rgbe(unsigned long long n, const float* __restrict__ rgb, uchar4* __restrict__ out)
+{
+    for (unsigned long long g = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; g < n;
+         g += (unsigned long long) gridDim.x * blockDim.x) {
+        const double r = fmax((double) rgb[3 * g], 0.0), gr = fmax((double) rgb[3 * g + 1], 0.0),
+                     b = fmax((double) rgb[3 * g + 2], 0.0);
+        const double v = fmax(r, fmax(gr, b));
+        uchar4 o = make_uchar4(0, 0, 0, 0);
+        if (v > 1e-32) {
+            int e = 0;
+            const double m = frexp(v, &e);
+            const double sc = m * 256.0 / v;
+            o.x = (unsigned char) fmin(floor(r * sc), 255.0);
+            o.y = (unsigned char) fmin(floor(gr * sc), 255.0);
+            o.z = (unsigned char) fmin(floor(b * sc), 255.0);
+            o.w = (unsigned char) (e + 128);
+        }
+        out[g] = o;
+    }
+}
+
 __global__ void k_ds2x(unsigned long long nout, int n_inst, const unsigned long long* __restrict__ out_off,
                        const unsigned long long* __restrict__ tex_off, const u32* __restrict__ inst_w,
                        const u32* __restrict__ inst_h, const float* __restrict__ src, float* __restrict__ dst)
@@ -3330,6 +3356,12 @@ void run_bake(ltr_Scene* S)
             CK(cudaGetLastError());
         }
     }
+    uchar4* d_rgbe = nullptr;
+    if (S->opt.encode_rgbe && nout) {
+        d_rgbe = A.alloc<uchar4>(nout);
+        k_encode_rgbe<<<blocks_for(nout), kThreads, 0, st>>>(nout, d_out, d_rgbe); note_launch();
+        CK(cudaGetLastError());
+    }
     TRACE("finalize issued");
     cudaEvent_t e_fin = clock.mark();
 
@@ -3340,7 +3372,7 @@ void run_bake(ltr_Scene* S)
     CK(cudaMemcpyAsync(&cnt, d_cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st)); note_d2h(sizeof(Counters));
     // Outputs land directly in the scene's page-locked buffer (kept across
     // bakes, freed with the scene); the work outputs point into it.
-    const size_t out_floats = 3 * (size_t) nout + (d_nimg ? 4 * (size_t) nout : 0);
+    const size_t out_floats = 3 * (size_t) nout + (d_nimg ? 4 * (size_t) nout : 0) + (d_rgbe ? (size_t) nout : 0);
     if (S->pinned_bytes < out_floats * sizeof(float)) {
         if (S->pinned) cudaFreeHost(S->pinned);
         S->pinned = nullptr;
@@ -3352,6 +3384,8 @@ void run_bake(ltr_Scene* S)
     float* hnimg = himg + 3 * (size_t) nout;
     if (nout) CK(cudaMemcpyAsync(himg, d_out, 3 * (size_t) nout * sizeof(float), cudaMemcpyDeviceToHost, st)); note_d2h(3 * (size_t) nout * sizeof(float));
     if (d_nimg) CK(cudaMemcpyAsync(hnimg, d_nimg, 4 * (size_t) nout * sizeof(float), cudaMemcpyDeviceToHost, st)); note_d2h(4 * (size_t) nout * sizeof(float));
+    unsigned char* hrgbe = (unsigned char*) (hnimg + (d_nimg ? 4 * (size_t) nout : 0));
+    if (d_rgbe) { CK(cudaMemcpyAsync(hrgbe, d_rgbe, 4 * (size_t) nout, cudaMemcpyDeviceToHost, st)); note_d2h(4 * (size_t) nout); }
     std::vector<float4> probe_lm(n_probe);
     if (n_probe) CK(cudaMemcpyAsync(probe_lm.data(), d_lm, n_probe * sizeof(float4), cudaMemcpyDeviceToHost, st)); note_d2h(n_probe * sizeof(float4));
     std::vector<float4> dpos, dnrm, drad, dlm;
@@ -3403,6 +3437,7 @@ void run_bake(ltr_Scene* S)
         ltr_WorkOutput wo = {(u32) i, mi->mesh->ident.c_str(), mi->mesh->ident.size(), mi->ident.c_str(),
                              mi->ident.size(), img, nimg, out_w[i], out_h[i]};
         S->outputs.push_back(wo);
+        if (d_rgbe) S->outputs_rgbe.push_back(hrgbe + 4 * out_off[i]);
     }
     if (S->opt.keep_samples) {
         S->dump.assign(n_inst, SampleDump());

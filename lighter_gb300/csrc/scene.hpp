@@ -92,6 +92,7 @@ struct ltr_Scene {
     std::vector<lg::HostLight> lights;
     std::vector<ltr_SampleInfo> samples;
     std::vector<ltr_WorkOutput> outputs;   // buffers point into `pinned`
+    std::vector<const unsigned char*> outputs_rgbe;   // RGBE encodings (ltrg_Options::encode_rgbe), in `pinned`
     void* pinned = nullptr;                 // page-locked output storage, reused across bakes
     size_t pinned_bytes = 0;
     float* ao_pinned = nullptr;             // page-locked AO random offsets, reused across bakes

@@ -25,7 +25,8 @@ class Options(C.Structure):
         ("bvh_builder", u32),
         ("shadow_mode", u32),
         ("intersect_mode", u32),
-        ("reserved", u32 * 7),
+        ("encode_rgbe", u32),
+        ("reserved", u32 * 6),
     ]
 
 
@@ -46,6 +47,7 @@ EXT_API = {
     "ltrg_GetOptions": (None, [C.c_void_p, C.POINTER(Options)]),
     "ltrg_SetOptions": (C.c_int, [C.c_void_p, C.POINTER(Options)]),
     "ltrg_GetStats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "ltrg_GetWorkOutputRGBE": (C.c_int, [C.c_void_p, u32, C.POINTER(C.POINTER(C.c_ubyte))]),
     "ltrg_LastError": (C.c_char_p, [C.c_void_p]),
     "ltrg_Wait": (C.c_int, [C.c_void_p]),
     "ltrg_StartBatch": (C.c_int, [C.POINTER(C.c_void_p), u32]),

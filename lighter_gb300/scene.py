@@ -99,6 +99,7 @@ class BakeResult:
     debug: list = field(default_factory=list)   # per instance dict of sample arrays
     final_stage: str = ""
     radiosity: Optional[dict] = None             # ext.get_radiosity of the bake (bake(..., radiosity=True))
+    rgbe: list = field(default_factory=list)     # per lightmap (h,w,4) uint8 when encode_rgbe was set
 
 
 def _vec3(v):
@@ -315,6 +316,13 @@ def _collect(lib, scene, debug, stages, wall, final, n_lights: int = 0, ao_ns: i
         mid = C.string_at(wo.mesh_ident, wo.mesh_ident_size).decode() if wo.mesh_ident else ""
         iid = C.string_at(wo.inst_ident, wo.inst_ident_size).decode() if wo.inst_ident else ""
         lms.append((wo.uid, mid, iid, rgb, nrm))
+    rgbe = []
+    if hasattr(lib, "ltrg_GetWorkOutputRGBE"):
+        for k, (_, _, _, rgb, _) in enumerate(lms):
+            p = C.POINTER(C.c_ubyte)()
+            if lib.ltrg_GetWorkOutputRGBE(scene, k, C.byref(p)):
+                h, w = rgb.shape[:2]
+                rgbe.append(np.ctypeslib.as_array(p, shape=(h * w * 4,)).copy().reshape(h, w, 4))
     colors = np.zeros((info.sample_count, 3), np.float32)
     for k in range(info.sample_count):
         colors[k] = info.samples[k].out_color[:]
@@ -341,7 +349,7 @@ def _collect(lib, scene, debug, stages, wall, final, n_lights: int = 0, ao_ns: i
                     if ao_ns:
                         d["ao"] = ao
             dbg.append(d)
-    return BakeResult(lms, colors, stages, wall, dbg, final)
+    return BakeResult(lms, colors, stages, wall, dbg, final, rgbe=rgbe)
 
 
 def bake_batch(lib, descs, debug: bool = False, gpu_options: Optional[dict] = None, stats: Optional[list] = None,

@@ -189,6 +189,22 @@ def test_patch_radiosity_runs_and_adds_light(gpu):
     assert gain > 0
 
 
+@pytest.mark.parametrize("cfg", [{}, {"ds2x": 1}, {"blur_size": 1.5}])
+def test_gpu_rgbe_encoding_matches_the_host_encoder(gpu, cfg):
+    """encode_rgbe: the GPU's RGBE images are the host encoder's bytes of the
+    float outputs (images.rgbe), with and without downsampling and blur; a bake
+    without the option returns none."""
+    from lighter_gb300 import images
+    d = scenes.cornell(3, lm=64, bounces=1, ao=True)
+    d.config.update(cfg)
+    res = bake(gpu, d, gpu_options={"encode_rgbe": 1})
+    assert len(res.rgbe) == len(res.lightmaps) > 0
+    for lm, px in zip(res.lightmaps, res.rgbe):
+        np.testing.assert_array_equal(px, images.rgbe(lm[3]))
+    assert (np.concatenate([p[..., 3].ravel() for p in res.rgbe]) > 0).any()
+    assert bake(gpu, d).rgbe == []
+
+
 def test_bounce_wait_expiry_fails_the_bake_and_the_next_bake_matches(gpu):
     """The bounce kernel's bounded waits: a bounce whose copy producer issues nothing
     gives up after 20 ms (test limit), the radiosity error word (bit 1) ends that bake
