@@ -2688,6 +2688,13 @@ void run_bake(ltr_Scene* S)
     S->stats.reserved[0] = (uint64_t) bin.n;   // leaf references
     BvhView bv = bvh.view();
     bv.watertight = S->opt.intersect_mode == LTRG_ISECT_WATERTIGHT ? 1 : 0;
+    {
+        // rounding bound of the distance test against the plane distance: a few
+        // single-precision dot products over coordinates up to the scene's largest
+        float mx = 0.0f;
+        for (float v : tri_xyz) mx = fmaxf(mx, fabsf(v));
+        bv.dist_margin = std::isfinite(mx) ? 4e-6f * (1.0f + mx) : INFINITY;
+    }
     cudaEvent_t e_bvh = clock.mark();
     // LTRG_VALIDATE=1: re-check the BVH topology after every stage
     const bool validate = getenv("LTRG_VALIDATE") && getenv("LTRG_VALIDATE")[0] == '1';

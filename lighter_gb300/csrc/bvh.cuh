@@ -39,6 +39,9 @@ struct BvhView {
     const float4* nodes4;   // 4-wide nodes (see below)
     int root4;              // >= 0 4-wide node, < 0 leaf
     int watertight;         // segment queries use seg_tri_wt instead of the reference's test
+    float dist_margin = INFINITY;   // warp_distance: bound on how far the exact point/triangle test can
+                            // fall below the triangle's plane distance by rounding (infinite: the
+                            // plane test that skips hopeless leaves is off)
 };
 
 // 4-wide nodes, used by the any-hit walk: the binary nodes at even depth with
@@ -560,11 +563,23 @@ __device__ __forceinline__ float warp_distance(const BvhView& b, V3 p, float d0,
             if (mr) { cur = nb.r; continue; }
         } else {
             const int t = ~cur;
-            const u32 meta = __float_as_uint(__ldg(&b.drec[8 * (size_t) t + 4]).w);
-            if (counter && (meta & kOccluderBit)) ++nt;
-            if (active && (meta & kOccluderBit)) {
-                const float nd = point_tri_dist_rec(b, t, p);
-                if (nd < dist) dist = nd;
+            const float4* r = b.drec + 8 * (size_t) t;
+            const u32 meta = __float_as_uint(__ldg(r + 4).w);
+            if (meta & kOccluderBit) {
+                // The exact test returns the plane distance pd or more (less rounding,
+                // at most dist_margin), so a lane whose limit is below pd - margin
+                // cannot take a smaller distance from this triangle; the warp runs the
+                // test only if some lane can (then for every lane, as before).
+                const float4 f0 = __ldg(r);
+                const float pd = fabsf(dot(mk(f0.x, f0.y, f0.z), p) - f0.w);
+                const bool may = active && !(pd > dist + b.dist_margin);
+                if (__any_sync(0xffffffffu, may)) {
+                    if (counter) ++nt;
+                    if (active) {
+                        const float nd = point_tri_dist_rec(b, t, p);
+                        if (nd < dist) dist = nd;
+                    }
+                }
             }
         }
         if (sp == 0) break;
@@ -736,7 +751,7 @@ struct BvhStorage {
     int root4 = 0;
     size_t bytes = 0;
     void* scratch = nullptr;   // build scratch, freed by bvh_free
-    BvhView view() const { BvhView v = {nodes, tris, srec, drec, n_tris, root, nodes4, root4, 0}; return v; }
+    BvhView view() const { BvhView v = {nodes, tris, srec, drec, n_tris, root, nodes4, root4, 0, INFINITY}; return v; }
 };
 
 // Builds into `out` on `stream` (allocations with cudaMallocAsync on that stream).
