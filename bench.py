@@ -750,6 +750,11 @@ def main():
         "ao": _trace_roofline("k_ao_rays", "k_ao_rays_mid512.md", s0["ao_rays"], s0["ms_ao_trace"],
                               clocks.get("sm_mhz"), n_sm, "AO ray"),
     }
+    # the resource that binds the dominant kernel, beside its HBM figure
+    sh = line["trace_rooflines"]["shadow"]
+    if sh and sh.get("frac") is not None:
+        line["roofline"]["binding_resource"] = "instruction issue (trace_rooflines.shadow)"
+        line["roofline"]["binding_frac"] = sh["frac"]
     if not args.no_sampled:
         line["sampled_shadows"] = run_sampled(args, local)
     if not args.no_large and args.scene == "mid":
