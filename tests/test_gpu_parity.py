@@ -123,6 +123,21 @@ def test_bench_cpu_sample_mid256(gpu, oracle):
     assert st["ao_rays"] == st["samples"] * 32 and st["shadow_evals"] > 100_000
 
 
+def test_benchmarked_mid1024_direct_and_ao(gpu, oracle):
+    """The bench's timed workload at its own size: the mid scene at 4 x 1024^2
+    lightmaps with every light and AO 32 rays, radiosity off (the oracle restates
+    the reference's per-sample radiosity, which is not runnable at this size; the
+    patch radiosity has its own tests), against the oracle on all host threads,
+    with the CPU sample's bars."""
+    import os
+    d = scenes.mid(seed=1, lm=1024, bounces=0)
+    st = {}
+    rg = bake(gpu, d, stats=st)
+    ro = bake(oracle, d, threads=os.cpu_count() or 1)
+    compare(rg, ro, "mid1024", max_tol=1e-5, mean_tol=1e-6, texel_frac=0.0)
+    assert st["ao_rays"] == st["samples"] * 32 and st["shadow_pairs"] > 1_500_000
+
+
 def test_c1_cornell_128_bit_exact(gpu, oracle):
     """C1 at its configured 128^2 lightmaps (8 lightmaps, point + directional
     light, no spot light and power 1, so no powf/acosf rounding enters), no
