@@ -350,6 +350,11 @@ LTRAPI LTRBOOL ltrdbg_TraceSegments(const float* tri_xyz, u32 n_tris, const floa
  * them, leaving the C library's generator where those calls would (the AO
  * stage's bulk draw, exposed for testing). */
 LTRAPI void ltrdbg_DrawRandFloats(float* out, u32 n);
+/* The sample-offset pass's reference-shaped tree over a triangle soup (n_tris x
+ * 9 floats), built with (threads != 0) or without its threaded top levels:
+ * out3 = {node count, item-list length, FNV-1a hash of the node and item
+ * arrays}. Host only; for tests. */
+LTRAPI LTRBOOL ltrdbg_RefTreeDigest(const float* tri_xyz, u32 n_tris, int threads, uint64_t* out3);
 
 #ifdef __cplusplus
 }

@@ -1,6 +1,8 @@
 // Host build of the reference-shaped per-instance trees (see reftree.hpp).
 #include "reftree.hpp"
 
+#include "../../include/lighter_gb300.h"
+
 #include <algorithm>
 #include <cfloat>
 #include <exception>
@@ -23,6 +25,7 @@ constexpr int kParDepth = 4;
 struct Builder {
     const Box* boxes;
     RefTree* t;
+    int par_depth;   // levels whose halves are built on two threads (kParDepth, or -1: none)
 
     // Appends `sub` (built with its root at index 0 and its own item list) as the
     // subtree whose root gets the next node index.
@@ -84,11 +87,11 @@ struct Builder {
                 });
                 for (size_t i = 0; i < split.size(); ++i) split[i] = kp[i].second;
                 size_t mid = split.size() / 2;
-                if (depth < kParDepth && split.size() >= kParItems) {
+                if (depth < par_depth && split.size() >= kParItems) {
                     // both halves at once: the right one on a second thread
                     RefTree right;
                     right.nodes.assign(1, RefNode());
-                    Builder rb{boxes, &right};
+                    Builder rb{boxes, &right, par_depth};
                     std::exception_ptr rerr;
                     std::thread th([&]() {
                         try {
@@ -99,7 +102,7 @@ struct Builder {
                     });
                     RefTree left;
                     left.nodes.assign(1, RefNode());
-                    Builder lb{boxes, &left};
+                    Builder lb{boxes, &left, par_depth};
                     try {
                         lb.make(0, split.data(), mid, depth + 1);
                     } catch (...) {
@@ -127,7 +130,7 @@ struct Builder {
 
 }  // namespace
 
-void build_ref_tree(const float* xyz, size_t n, RefTree& out)
+void build_ref_tree(const float* xyz, size_t n, RefTree& out, bool threads)
 {
     out.nodes.assign(1, RefNode());
     out.items.clear();
@@ -147,8 +150,30 @@ void build_ref_tree(const float* xyz, size_t n, RefTree& out)
         const Box& bb = boxes[i];
         if (bb.mn.x <= bb.mx.x && bb.mn.y <= bb.mx.y && bb.mn.z <= bb.mx.z) ids.push_back((int32_t) i);
     }
-    Builder bld{boxes.data(), &out};
+    Builder bld{boxes.data(), &out, threads ? kParDepth : -1};
     bld.make(0, ids.data(), ids.size(), 0);
 }
 
 }  // namespace lg
+
+extern "C" LTRAPI LTRBOOL ltrdbg_RefTreeDigest(const float* tri_xyz, u32 n_tris, int threads, uint64_t* out3)
+{
+    if ((!tri_xyz && n_tris) || !out3) return 0;
+    try {
+        lg::RefTree t;
+        lg::build_ref_tree(tri_xyz, n_tris, t, threads != 0);
+        uint64_t h = 1469598103934665603ull;   // FNV-1a over the node and item arrays
+        auto mix = [&](const void* p, size_t bytes) {
+            const unsigned char* c = (const unsigned char*) p;
+            for (size_t i = 0; i < bytes; ++i) { h ^= c[i]; h *= 1099511628211ull; }
+        };
+        mix(t.nodes.data(), t.nodes.size() * sizeof(lg::RefNode));
+        mix(t.items.data(), t.items.size() * sizeof(int32_t));
+        out3[0] = t.nodes.size();
+        out3[1] = t.items.size();
+        out3[2] = h;
+    } catch (...) {
+        return 0;
+    }
+    return 1;
+}

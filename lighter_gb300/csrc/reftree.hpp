@@ -31,7 +31,9 @@ struct RefTree {
     std::vector<int32_t> items;
 };
 
-// Builds the tree over `n` triangles given as 9 floats each (P1, P2, P3).
-void build_ref_tree(const float* tri_xyz, size_t n, RefTree& out);
+// Builds the tree over `n` triangles given as 9 floats each (P1, P2, P3); with
+// `threads`, the halves of the top levels are built on two threads each (the
+// layout is the same either way).
+void build_ref_tree(const float* tri_xyz, size_t n, RefTree& out, bool threads = true);
 
 }  // namespace lg

@@ -167,6 +167,7 @@ EXT_API.update({
     "ltrdbg_GatherHostPath": (C.c_int, [C.c_void_p, C.c_int]),
     "ltrdbg_GatherHostPathUsed": (C.c_int, [C.c_void_p]),
     "ltrdbg_RadiosityStallNextBounce": (C.c_int, [u32]),
+    "ltrdbg_RefTreeDigest": (C.c_int, [C.c_void_p, u32, C.c_int, C.c_void_p]),
     "ltrg_GatherSolve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, u32, C.c_int, C.c_int, C.c_int, C.c_void_p,
                                    C.POINTER(GatherStats)]),
     "ltrg_GatherSolveDevice": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, u32, C.c_int, C.c_int, C.c_int,
