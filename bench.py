@@ -17,7 +17,8 @@ triangles (~21k triangles), four 1024^2 lightmaps, 8 point + 2 spot lights,
   cpu_baseline  the CPU oracle port (all host threads) on a bounded sample.
 
 --impl reference times the reference's CPU bake on the host cores instead
-(the oracle port: the reference's own sources are not present on this machine).
+(the oracle port: the reference's own sources are not present where the
+bench runs).
 Multi-GPU runs are replicas (each rank bakes its own copy); the bake has no
 exchange step, so there is no collective on the data path.
 """
