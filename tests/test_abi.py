@@ -170,6 +170,18 @@ def test_options_validation(gpu):
         assert gpu.ltrg_SetOptions(s, C.byref(o)) == 0
         o.radiosity_precision = 1
         assert gpu.ltrg_SetOptions(s, C.byref(o)) == 1
+        assert o.shadow_mode == 0 and o.intersect_mode == 0 and o.encode_rgbe == 0
+        for field, bad, good in (("shadow_mode", 2, 1), ("intersect_mode", 2, 1), ("encode_rgbe", 2, 1)):
+            setattr(o, field, bad)
+            assert gpu.ltrg_SetOptions(s, C.byref(o)) == 0, field
+            setattr(o, field, good)
+            assert gpu.ltrg_SetOptions(s, C.byref(o)) == 1, field
+        back = ext.Options()
+        gpu.ltrg_GetOptions(s, C.byref(back))
+        assert (back.shadow_mode, back.intersect_mode, back.encode_rgbe) == (1, 1, 1)
+        # no bake has run: no encoded outputs
+        px = C.POINTER(C.c_ubyte)()
+        assert gpu.ltrg_GetWorkOutputRGBE(s, 0, C.byref(px)) == 0
     finally:
         gpu.ltr_DestroyScene(s)
 
