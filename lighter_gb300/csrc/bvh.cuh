@@ -179,7 +179,9 @@ __device__ __forceinline__ float box_d2(V3 mn, V3 mx, V3 p)
     float dx = fmaxf(fmaxf(mn.x - p.x, p.x - mx.x), 0.0f);
     float dy = fmaxf(fmaxf(mn.y - p.y, p.y - mx.y), 0.0f);
     float dz = fmaxf(fmaxf(mn.z - p.z, p.z - mx.z), 0.0f);
-    return dx * dx + dy * dy + dz * dz;
+    // a pruning bound only (never a result): fused multiply-adds are within an ulp
+    // of the separate products, far inside the boxes' inflation
+    return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, dz * dz));
 }
 
 __device__ __forceinline__ bool box_overlap(V3 mn, V3 mx, V3 qmn, V3 qmx)
