@@ -573,7 +573,8 @@ __device__ __forceinline__ float warp_distance(const BvhView& b, V3 p, float d0,
                 // cannot take a smaller distance from this triangle; the warp runs the
                 // test only if some lane can (then for every lane, as before).
                 const float4 f0 = __ldg(r);
-                const float pd = fabsf(dot(mk(f0.x, f0.y, f0.z), p) - f0.w);
+                // a skip test only: fused multiply-adds move pd by far less than the margin
+                const float pd = fabsf(__fmaf_rn(f0.x, p.x, __fmaf_rn(f0.y, p.y, __fmaf_rn(f0.z, p.z, -f0.w))));
                 const bool may = active && !(pd > dist + b.dist_margin);
                 if (__any_sync(0xffffffffu, may)) {
                     if (counter) ++nt;
