@@ -758,6 +758,9 @@ def main():
         line["roofline"]["binding_frac"] = sh["frac"]
     if not args.no_sampled:
         line["sampled_shadows"] = run_sampled(args, local)
+        ss = line["sampled_shadows"]
+        ss["roofline"] = _trace_roofline("k_direct_trace (sampled shadows)", "k_direct_trace_sampled_mid512.md",
+                                         ss["shadow_rays"], ss["kernel_ms"], clocks.get("sm_mhz"), n_sm, "shadow ray")
     if not args.no_large and args.scene == "mid":
         line["large_scene"] = run_large(args, local)
     if not args.no_rad_precisions:
