@@ -1486,9 +1486,20 @@ __global__ void k_ao(AoArgs a, const float* __restrict__ hits)
          s += (unsigned long long) gridDim.x * blockDim.x) {
         const float* h = hits + s * (unsigned long long) a.ns;
         float f = 0;
-        for (int r = 0; r < a.ns; ++r) {
-            float v = h[r];
-            if (v < 1.0f) f += 1.0f - v;
+        if ((a.ns & 3) == 0) {   // 16-byte loads (each sample's run starts on a 16-byte boundary); same order
+            const float4* h4 = reinterpret_cast<const float4*>(h);
+            for (int r = 0; r < a.ns / 4; ++r) {
+                const float4 v = __ldcs(&h4[r]);
+                if (v.x < 1.0f) f += 1.0f - v.x;
+                if (v.y < 1.0f) f += 1.0f - v.y;
+                if (v.z < 1.0f) f += 1.0f - v.z;
+                if (v.w < 1.0f) f += 1.0f - v.w;
+            }
+        } else {
+            for (int r = 0; r < a.ns; ++r) {
+                float v = h[r];
+                if (v < 1.0f) f += 1.0f - v;
+            }
         }
         {
             f /= a.ns;
